@@ -1,0 +1,139 @@
+// Shared device helpers for the sm_103a interpolation kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "../../include/arbinterp.h"
+
+#define ARB_MAX_AXIS_CAP (1 << 20)
+
+namespace arb {
+
+// -- status helpers ----------------------------------------------------------
+__device__ __forceinline__ void set_status(int32_t *status, int32_t bits) {
+  if (status) atomicOr(status, bits);
+}
+
+static inline int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ARB_OK : ARB_ERR_CUDA;
+}
+
+// -- Catmull-Rom weights ------------------------------------------------------
+// The reference's 3D A = inv(B) D is exactly kron(A1, A1, A1) with A1 the
+// 4x4 Catmull-Rom matrix (cubic Hermite with central-difference slopes), so
+// p(x) . (A f) == sum_o w(x)_o f_o with w(t) = A1^T [1, t, t^2, t^3].
+template <typename T>
+__device__ __forceinline__ void cr_weights(T t, T w[4]) {
+  const T h = T(0.5);
+  w[0] = t * (-h + t * (T(1) - h * t));
+  w[1] = T(1) + t * t * (T(-2.5) + T(1.5) * t);
+  w[2] = t * (h + t * (T(2) - T(1.5) * t));
+  w[3] = t * t * (-h + h * t);
+}
+
+template <typename T>
+__device__ __forceinline__ void cr_dweights(T t, T d[4]) {
+  d[0] = T(-0.5) + t * (T(2) - T(1.5) * t);
+  d[1] = t * (T(-5) + T(4.5) * t);
+  d[2] = T(0.5) + t * (T(4) - T(4.5) * t);
+  d[3] = t * (T(-1) + T(1.5) * t);
+}
+
+// Cubic Hermite basis for the slope at t=0 (c=0) and at t=1 (c=1), and their
+// derivatives: the 1D factors of the inv(B) columns of the d4f/dxdydzdt rows.
+template <typename T>
+__device__ __forceinline__ void hermite_slope(T t, T hb[2], T dhb[2]) {
+  const T u = T(1) - t;
+  hb[0] = t * u * u;
+  hb[1] = t * t * (t - T(1));
+  dhb[0] = T(1) + t * (T(-4) + T(3) * t);
+  dhb[1] = t * (T(3) * t - T(2));
+}
+
+// -- coordinate step ---------------------------------------------------------
+// The reference computes iu = (q - IntMin) / h in float64, floors it, and
+// builds the flat cell index from the floors (ARB:471-483).  Division must
+// be the IEEE one so floors (hence cell indices) are bit-exact.
+struct CoordStep {
+  int64_t idx;       // flat cell index, as the reference computes it
+  bool oob;          // some coordinate outside [lo, hi]  -> row written NaN
+  bool nan;          // some coordinate NaN (row not rewritten, outputs NaN)
+};
+
+// exact == true: IEEE division (used by the float64 path).
+// exact == false: multiply by 1/h and fall back to the division only when the
+// product lies within a few ulps of an integer, so floor() still matches.
+template <int DIM, bool EXACT>
+__device__ __forceinline__ CoordStep coord_step(const double *qrow, const arb_grid &g,
+                                                const double *inv_h, double frac[DIM]) {
+  CoordStep s;
+  s.oob = false;
+  s.nan = false;
+  int64_t fl[DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    const double q = qrow[a];
+    if (q < g.lo[a] || q > g.hi[a]) s.oob = true;
+    if (q != q) s.nan = true;
+    const double d = q - g.lo[a];
+    double iu, k;
+    if (EXACT) {
+      iu = d / g.h[a];
+      k = floor(iu);
+    } else {
+      iu = d * inv_h[a];
+      k = floor(iu);
+      const double guard = fmax(fabs(iu), 1.0) * 1.7763568394002505e-15;  // 8 ulp(1)
+      if (iu - k < guard || (k + 1.0) - iu < guard) {
+        iu = d / g.h[a];
+        k = floor(iu);
+      }
+    }
+    frac[a] = iu - k;
+    fl[a] = (int64_t)k;
+  }
+  if (s.oob || s.nan) {
+    s.idx = g.nc;
+    return s;
+  }
+  int64_t idx = fl[DIM - 1];
+#pragma unroll
+  for (int a = DIM - 2; a >= 0; --a) idx = idx * (g.n[a] - 3) + fl[a];
+  s.idx = idx;
+  return s;
+}
+
+// Cell coordinates of a flat index (the reference's upper-face aliasing
+// falls out of this: (nPos, iy, iz) decodes as (0, iy+1, iz)).
+template <int DIM>
+__device__ __forceinline__ void cell_coords(int64_t idx, const arb_grid &g, int64_t c[DIM]) {
+#pragma unroll
+  for (int a = 0; a < DIM - 1; ++a) {
+    const int64_t m = g.n[a] - 3;
+    c[a] = idx % m;
+    idx /= m;
+  }
+  c[DIM - 1] = idx;
+}
+
+__device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }
+
+// Warp-aggregated append of an out-of-volume row index.
+__device__ __forceinline__ void append_oob(const arb_query_out &o, int64_t row, bool pred) {
+  if (!o.oob_rows) return;
+  const unsigned mask = __ballot_sync(__activemask(), pred);
+  if (!pred) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(o.oob_count, (unsigned long long)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  const int rank = __popc(mask & ((1u << lane) - 1));
+  o.oob_rows[base + rank] = row;
+}
+
+}  // namespace arb

@@ -1,0 +1,310 @@
+// Field ingest: axis discovery and scatter of field rows into the z-major
+// (x fastest, t slowest) grid.  Replaces the reference's three/four argsorts
+// and exact-equality axis scans (src/ARBInterp/ARBInterp.py:528-568,
+// 1264-1320).
+//
+// For a full tensor grid the position of a row in the reference's
+// lexicographic sort is ix + nx*(iy + ny*(iz + nz*it)) with i_a the rank of
+// the row's a-coordinate among that axis' samples, so the sort becomes an
+// O(N log n) scatter with no global sort.  Rows that are not a full tensor
+// grid (missing or duplicate points, a coordinate not on its axis) set
+// ARB_ERR_IRREGULAR_GRID instead of silently producing garbage.
+#include "arb_common.cuh"
+
+namespace arb {
+
+// Order-preserving map of a double onto uint64 (for atomicMin).
+__device__ __forceinline__ unsigned long long ord_key(double v) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ double ord_val(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+template <typename TF>
+__device__ __forceinline__ double ld(const TF *p) { return (double)p[0]; }
+
+struct AxesWork {
+  unsigned long long minkey[4];
+  unsigned long long count[4];
+};
+
+__global__ void axes_init_kernel(AxesWork *w) {
+  if (threadIdx.x < 4) {
+    w->minkey[threadIdx.x] = ~0ULL;
+    w->count[threadIdx.x] = 0ULL;
+  }
+}
+
+template <typename TF>
+__global__ void axes_min_kernel(const TF *field, int64_t npts, int ncol, int dim, AxesWork *w,
+                                int32_t *status) {
+  unsigned long long m[4] = {~0ULL, ~0ULL, ~0ULL, ~0ULL};
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    for (int a = 0; a < dim; ++a) {
+      const double v = ld(field + i * ncol + a);
+      if (v != v) bad = true;
+      const unsigned long long k = ord_key(v);
+      m[a] = k < m[a] ? k : m[a];
+    }
+  }
+  if (bad) set_status(status, ARB_ERR_IRREGULAR_GRID);
+  for (int a = 0; a < dim; ++a) {
+    unsigned long long v = m[a];
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long u = __shfl_down_sync(0xffffffffu, v, o);
+      v = u < v ? u : v;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMin(&w->minkey[a], v);
+  }
+}
+
+// Appends every row that lies on the axis line of axis a through the minimum
+// corner (all other coordinates equal to their minimum).
+template <typename TF>
+__global__ void axes_collect_kernel(const TF *field, int64_t npts, int ncol, int dim, AxesWork *w,
+                                    double *raw_axes, int64_t cap, int32_t *status) {
+  double mn[4];
+  for (int a = 0; a < dim; ++a) mn[a] = ord_val(w->minkey[a]);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v[4];
+    int neq = 0, which = -1;
+    for (int a = 0; a < dim; ++a) {
+      v[a] = ld(field + i * ncol + a);
+      if (v[a] != mn[a]) {
+        ++neq;
+        which = a;
+      }
+    }
+    if (neq > 1) continue;
+    // neq == 0: the corner itself belongs to every axis line
+    for (int a = 0; a < dim; ++a) {
+      if (neq == 1 && a != which) continue;
+      const unsigned long long slot = atomicAdd(&w->count[a], 1ULL);
+      if ((int64_t)slot < cap)
+        raw_axes[a * cap + slot] = v[a];
+      else
+        set_status(status, ARB_ERR_CAPACITY);
+    }
+  }
+}
+
+// Rank sort of each (short) axis list; equal samples mean duplicate points.
+__global__ void axes_sort_kernel(const double *raw_axes, const AxesWork *w, int dim, int64_t cap,
+                                 double *axis_out, int64_t *axis_count, int32_t *status) {
+  const int a = blockIdx.y;
+  const int64_t n = (int64_t)min(w->count[a], (unsigned long long)cap);
+  if (blockIdx.x == 0 && threadIdx.x == 0) axis_count[a] = (int64_t)w->count[a];
+  const double *src = raw_axes + a * cap;
+  extern __shared__ double tile[];
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    const double v = i < n ? src[i] : 0.0;
+    int64_t rank = 0;
+    bool dup = false;
+    for (int64_t t0 = 0; t0 < n; t0 += blockDim.x) {
+      __syncthreads();
+      if (t0 + threadIdx.x < n) tile[threadIdx.x] = src[t0 + threadIdx.x];
+      __syncthreads();
+      const int64_t lim = min((int64_t)blockDim.x, n - t0);
+      if (i < n) {
+        for (int64_t j = 0; j < lim; ++j) {
+          const double u = tile[j];
+          rank += (u < v);
+          dup |= (u == v) && (t0 + j != i);
+        }
+      }
+    }
+    if (i < n) {
+      if (dup) set_status(status, ARB_ERR_IRREGULAR_GRID);
+      axis_out[a * cap + rank] = v;
+    }
+  }
+}
+
+__device__ __forceinline__ int64_t find_exact(const double *ax, int64_t n, double v) {
+  int64_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (ax[mid] < v)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return ax[lo] == v ? lo : -1;
+}
+
+template <typename TF, int KIND>
+__global__ void scatter_kernel(const TF *field, int64_t npts, int ncol, int dim, const double *axes,
+                               int64_t cap, int64_t n0, int64_t n1, int64_t n2, int64_t n3,
+                               double *grid64, float *grid32, double *raw_out, uint32_t *claim,
+                               int32_t *status) {
+  const int64_t nn[4] = {n0, n1, n2, n3};
+  constexpr int F = (KIND == ARB_KIND_VECTOR) ? 3 : (KIND == ARB_KIND_BOTH ? 4 : 1);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const TF *row = field + i * ncol;
+    int64_t dest = 0;
+    bool ok = true;
+    for (int a = dim - 1; a >= 0; --a) {
+      const int64_t r = find_exact(axes + a * cap, nn[a], (double)row[a]);
+      ok &= (r >= 0);
+      dest = dest * nn[a] + (r < 0 ? 0 : r);
+    }
+    if (!ok) {
+      set_status(status, ARB_ERR_IRREGULAR_GRID);
+      continue;
+    }
+    if (atomicAdd(&claim[dest], 1u) != 0u) {
+      set_status(status, ARB_ERR_IRREGULAR_GRID);
+      continue;
+    }
+    double out[4];
+    if (KIND == ARB_KIND_SCALAR) {
+      out[0] = (double)row[dim];
+    } else {
+      const TF bx = row[dim], by = row[dim + 1], bz = row[dim + 2];
+      out[0] = (double)bx;
+      out[1] = (double)by;
+      out[2] = (double)bz;
+      if (KIND == ARB_KIND_NORM || KIND == ARB_KIND_BOTH) {
+        // ||B|| at the grid point, evaluated in the field's own precision
+        // as NumPy's norm does: sqrt((bx*bx + by*by) + bz*bz).
+        double nrm;
+        if (sizeof(TF) == 8) {
+          nrm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn((double)bx, (double)bx),
+                                               __dmul_rn((double)by, (double)by)),
+                                     __dmul_rn((double)bz, (double)bz)));
+        } else {
+          nrm = (double)__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn((float)bx, (float)bx),
+                                                       __fmul_rn((float)by, (float)by)),
+                                             __fmul_rn((float)bz, (float)bz)));
+        }
+        if (KIND == ARB_KIND_NORM) out[0] = nrm;
+        else out[3] = nrm;
+      }
+      if (raw_out) {
+        raw_out[dest * 3 + 0] = (double)bx;
+        raw_out[dest * 3 + 1] = (double)by;
+        raw_out[dest * 3 + 2] = (double)bz;
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < F; ++f) grid64[dest * F + f] = out[f];
+    if (grid32) {
+#pragma unroll
+      for (int f = 0; f < F; ++f) {
+        const float hi = __double2float_rn(out[f]);
+        const float lo = __double2float_rn(out[f] - (double)hi);
+        reinterpret_cast<float2 *>(grid32)[dest * F + f] = make_float2(hi, lo);
+      }
+    }
+    if (KIND == ARB_KIND_SCALAR && raw_out) raw_out[dest] = out[0];
+  }
+}
+
+static int grid_blocks(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b > 152 * 64) b = 152 * 64;
+  return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace arb
+
+using namespace arb;
+
+extern "C" size_t arb_ingest_axes_work_bytes(int32_t dim) {
+  (void)dim;
+  return sizeof(AxesWork) + 256;
+}
+
+extern "C" int arb_ingest_axes(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                               int32_t dim, int64_t axis_cap, double *axis_out, int64_t *axis_count,
+                               void *work, size_t work_bytes, int32_t *status, arb_stream_t stream) {
+  if (!field || !axis_out || !axis_count || !work || !status) return ARB_ERR_INVALID;
+  if ((dim != 3 && dim != 4) || npts <= 0 || ncol < dim + 1 || axis_cap <= 0 ||
+      axis_cap > ARB_MAX_AXIS_CAP || work_bytes < arb_ingest_axes_work_bytes(dim))
+    return ARB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  AxesWork *w = (AxesWork *)work;
+  // The unsorted axis lists are staged in the second half of axis_out
+  // (callers allocate 2 * dim * axis_cap doubles).
+  double *raw = axis_out + (int64_t)dim * axis_cap;
+  axes_init_kernel<<<1, 32, 0, s>>>(w);
+  const int T = 256;
+  const int B = grid_blocks(npts, T);
+  if (field_is_f32) {
+    axes_min_kernel<float><<<B, T, 0, s>>>((const float *)field, npts, ncol, dim, w, status);
+    axes_collect_kernel<float>
+        <<<B, T, 0, s>>>((const float *)field, npts, ncol, dim, w, raw, axis_cap, status);
+  } else {
+    axes_min_kernel<double><<<B, T, 0, s>>>((const double *)field, npts, ncol, dim, w, status);
+    axes_collect_kernel<double>
+        <<<B, T, 0, s>>>((const double *)field, npts, ncol, dim, w, raw, axis_cap, status);
+  }
+  int sb = (int)((axis_cap + T - 1) / T);
+  if (sb > 1024) sb = 1024;
+  axes_sort_kernel<<<dim3(sb, dim), T, T * sizeof(double), s>>>(raw, w, dim, axis_cap, axis_out,
+                                                                axis_count, status);
+  return launch_status();
+}
+
+extern "C" int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64_t npts,
+                                  int32_t ncol, int32_t dim, const double *axes, int64_t axis_cap,
+                                  const int64_t *n, int32_t kind, double *grid64, float *grid32,
+                                  double *raw_out, uint32_t *claim, int32_t *status,
+                                  arb_stream_t stream) {
+  if (!field || !axes || !n || !grid64 || !claim || !status) return ARB_ERR_INVALID;
+  if (dim != 3 && dim != 4) return ARB_ERR_INVALID;
+  int64_t prod = 1;
+  for (int a = 0; a < dim; ++a) {
+    if (n[a] < 4 || n[a] > axis_cap) return ARB_ERR_INVALID;
+    prod *= n[a];
+  }
+  if (prod != npts) return ARB_ERR_IRREGULAR_GRID;
+  const int nval = ncol - dim;
+  if (kind == ARB_KIND_SCALAR ? nval != 1 : nval != 3) return ARB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(claim, 0, sizeof(uint32_t) * npts, s) != cudaSuccess) return ARB_ERR_CUDA;
+  const int T = 256;
+  const int B = grid_blocks(npts, T);
+  const int64_t n3 = dim == 4 ? n[3] : 1;
+#define ARB_SCATTER(TF, K)                                                                       \
+  scatter_kernel<TF, K><<<B, T, 0, s>>>((const TF *)field, npts, ncol, dim, axes, axis_cap, n[0], \
+                                        n[1], n[2], n3, grid64, grid32, raw_out, claim, status)
+#define ARB_SCATTER_KIND(TF)                              \
+  switch (kind) {                                         \
+    case ARB_KIND_SCALAR: ARB_SCATTER(TF, ARB_KIND_SCALAR); break; \
+    case ARB_KIND_VECTOR: ARB_SCATTER(TF, ARB_KIND_VECTOR); break; \
+    case ARB_KIND_NORM: ARB_SCATTER(TF, ARB_KIND_NORM); break;     \
+    case ARB_KIND_BOTH: ARB_SCATTER(TF, ARB_KIND_BOTH); break;     \
+    default: return ARB_ERR_INVALID;                      \
+  }
+  if (field_is_f32) {
+    ARB_SCATTER_KIND(float)
+  } else {
+    ARB_SCATTER_KIND(double)
+  }
+#undef ARB_SCATTER_KIND
+#undef ARB_SCATTER
+  return launch_status();
+}
+
+extern "C" int arb_status_fetch(int32_t *status, arb_stream_t stream) {
+  if (!status) return ARB_ERR_INVALID;
+  int32_t h = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(&h, status, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return ARB_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return ARB_ERR_CUDA;
+  if (h != 0 && cudaMemsetAsync(status, 0, sizeof(int32_t), s) != cudaSuccess) return ARB_ERR_CUDA;
+  return h;
+}
+
+extern "C" const char *arb_version(void) { return "arbinterp-gb300 0.1.0 sm_103a"; }

@@ -1,0 +1,506 @@
+"""GB300-native drop-in for ``ARBInterp.tricubic`` / ``ARBInterp.quadcubic``.
+
+Mirrors the reference class API (src/ARBInterp/ARBInterp.py:8-621 and
+627-1381): constructor ``cls(field, *args, **kwargs)`` on an N x 4/6 (3D) or
+N x 5/7 (4D) row array in any row order, ``'quiet'`` among the positional
+args, ``mode='vector'|'norm'|'both'``; ``Query``/``rQuery``/``sQuery``,
+``allCoeffs``, ``calcCoefficients``, ``neighbourInd`` and the public
+attributes.  All arithmetic runs in CUDA kernels of ``libarbinterp.so``;
+torch is used only for device memory and streams.
+
+Extra keyword arguments (reference-compatible defaults):
+  precision  'fp64' (default; matches the reference to <=1e-12) or 'mixed'
+             (split-precision tensor-core / float32 evaluation, <=1e-6)
+  strategy   'auto' (default), 'otf' (evaluate from the grid) or 'table'
+             (evaluate from the full coefficient table)
+  device     CUDA device (default: the current one)
+  check      True (default): synchronise after each query to raise the
+             reference's errors; False: fully asynchronous device queries
+
+Inputs may be NumPy arrays (outputs are NumPy, as in the reference) or torch
+CUDA tensors (outputs stay on the device).  Differences from the reference on
+inputs it does not handle: rows that are not a full regular grid raise
+ValueError instead of producing undefined results.
+"""
+from __future__ import annotations
+
+import ctypes
+import sys
+
+import numpy as np
+import torch
+
+from . import _lib
+from . import matrices
+from ._lib import ArbGrid, ArbQueryOut, lib, check
+
+__version__ = "1.8"
+
+_F = {_lib.KIND_SCALAR: 1, _lib.KIND_VECTOR: 3, _lib.KIND_NORM: 1, _lib.KIND_BOTH: 4}
+_AXIS_CAP = 1 << 17
+
+_BANNERS = {
+    "scalar": "--- Scalar field, ignoring switches, interpolating for magnitude and gradient --- \n",
+    "vector": "--- Vector field, interpolating for vector components --- \n",
+    "norm": "--- Vector field, interpolating for magnitude and gradient --- \n",
+    "both": "--- Vector field, interpolating vector components plus magnitude and gradient --- \n",
+    "invalid": "--- Vector field, invalid option, defaulting to interpolating for vector components --- \n",
+    "none": "--- Vector field, no option selected, defaulting to interpolating for vector components --- \n",
+}
+
+
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+class _Interpolant:
+    __version__ = "1.8"
+    _dim = 3
+
+    def __init__(self, field, *args, **kwargs):
+        self.eps = 10 * np.finfo(float).eps
+        quiet = "quiet" in args
+        dim = self._dim
+        prec = kwargs.get("precision", "fp64")
+        if prec not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = prec
+        self.strategy = kwargs.get("strategy", "auto")
+        if self.strategy not in ("auto", "otf", "table"):
+            raise ValueError("strategy must be 'auto', 'otf' or 'table'")
+        self.check = bool(kwargs.get("check", True))
+        ncol = int(field.shape[1])
+        # mode dispatch (ARB:24-104, 641-723)
+        extra_col = False
+        sentinel_nan = True
+        if ncol == dim + 1:
+            kind, banner = _lib.KIND_SCALAR, "scalar"
+            sentinel_nan = False
+        elif ncol == dim + 3:
+            if "mode" in kwargs:
+                m = kwargs["mode"]
+                if m == "vector":
+                    kind, banner, extra_col, sentinel_nan = _lib.KIND_VECTOR, "vector", True, False
+                elif m == "norm":
+                    kind, banner = _lib.KIND_NORM, "norm"
+                elif m == "both":
+                    kind, banner = _lib.KIND_BOTH, "both"
+                else:
+                    kind, banner = _lib.KIND_VECTOR, "invalid"
+            else:
+                kind, banner = _lib.KIND_VECTOR, "none"
+        else:
+            lo, hi = (4, 6) if dim == 3 else (5, 7)
+            sys.exit(f"--- Input not shaped as expected - should be N x {lo} or N x {hi} ---")
+        dev = kwargs.get("device", None)
+        self.device = torch.device("cuda", torch.cuda.current_device()) if dev is None else torch.device(dev)
+        self._kind = kind
+        self._F = _F[kind]
+        self._extra_col = extra_col
+        self._sentinel_nan = sentinel_nan
+        self._ingest(field)
+        if not quiet:
+            print(_BANNERS[banner])
+        self._table = None
+        self._table_prec = None
+        self._solved = None          # host bool mask of solved cells (partial solves)
+        self._last_inds = None
+        self._last_ind = None
+
+    # ------------------------------------------------------------------ ingest
+    def _ingest(self, field):
+        L = lib()
+        dim = self._dim
+        dev = self.device
+        if isinstance(field, torch.Tensor):
+            ft = field.to(dev)
+        else:
+            fa = np.asarray(field)
+            if fa.dtype not in (np.float32, np.float64):
+                fa = fa.astype(np.float64)
+            ft = torch.from_numpy(np.ascontiguousarray(fa)).to(dev, non_blocking=True)
+        if ft.dtype not in (torch.float32, torch.float64):
+            ft = ft.to(torch.float64)
+        ft = ft.contiguous()
+        self._field_dtype = np.float32 if ft.dtype == torch.float32 else np.float64
+        npts, ncol = int(ft.shape[0]), int(ft.shape[1])
+        is32 = int(ft.dtype == torch.float32)
+        cap = max(4, min(npts, _AXIS_CAP))
+        axes = torch.empty(2 * dim * cap, dtype=torch.float64, device=dev)
+        counts = torch.zeros(dim, dtype=torch.int64, device=dev)
+        wb = L.arb_ingest_axes_work_bytes(dim)
+        work = torch.empty(int(wb), dtype=torch.uint8, device=dev)
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        s = _stream()
+        check(L.arb_ingest_axes(ft.data_ptr(), is32, npts, ncol, dim, cap, axes.data_ptr(),
+                                counts.data_ptr(), work.data_ptr(), wb, status.data_ptr(), s),
+              "arb_ingest_axes")
+        st = L.arb_status_fetch(status.data_ptr(), s)
+        n = [int(v) for v in counts.cpu()]
+        if st & _lib.ARB_ERR_CAPACITY:
+            raise ValueError(f"an axis has more than {cap} grid samples")
+        if st:
+            raise ValueError("field rows are not a regular grid (NaN coordinates or duplicate points)")
+        if any(v < 4 for v in n):
+            raise ValueError("every axis needs at least 4 grid points")
+        if int(np.prod(n)) != npts:
+            raise ValueError(f"field rows do not form a full regular grid: {npts} rows, axes {n}")
+        ax64 = axes[: dim * cap].view(dim, cap)
+        self._axes_dev = [ax64[a, : n[a]].clone() for a in range(dim)]
+        ax = [t.cpu().numpy().astype(self._field_dtype) for t in self._axes_dev]
+        self._n = n
+        self._npts = npts
+        kind, F = self._kind, self._F
+        grid64 = torch.empty(npts * F, dtype=torch.float64, device=dev)
+        grid32 = torch.empty(npts * F * 2, dtype=torch.float32, device=dev) if self.precision == "mixed" else None
+        raw = torch.empty(npts * 3, dtype=torch.float64, device=dev) if kind == _lib.KIND_NORM else None
+        claim = torch.empty(npts, dtype=torch.int32, device=dev)
+        n_c = (ctypes.c_int64 * 4)(*(n + [1] * (4 - dim)))
+        check(L.arb_ingest_scatter(ft.data_ptr(), is32, npts, ncol, dim, ax64.data_ptr(), cap,
+                                   n_c, kind, grid64.data_ptr(), _ptr(grid32), _ptr(raw),
+                                   claim.data_ptr(), status.data_ptr(), s), "arb_ingest_scatter")
+        if self.check:
+            st = L.arb_status_fetch(status.data_ptr(), s)
+            if st:
+                raise ValueError("field rows are not a full regular grid (duplicate or off-axis points)")
+        del claim
+        self._grid64, self._grid32, self._raw = grid64, grid32, raw
+        self._status = status
+        # reference attributes, computed in the field's own dtype (ARB:541-568)
+        h = [np.abs(ax[a][0] - ax[a][1]) for a in range(dim)]
+        lo = [ax[a][1] for a in range(dim)]
+        hi = [ax[a][n[a] - 2] for a in range(dim)]
+        self._h, self._lo, self._hi = h, lo, hi
+        names = "xyzt"
+        for a in range(dim):
+            setattr(self, "h" + names[a], h[a])
+            setattr(self, names[a] + "IntMin", lo[a])
+            setattr(self, names[a] + "IntMax", hi[a])
+        self.nc = int(np.prod([v - 3 for v in n]))
+        self._set_counts(n)
+        g = ArbGrid()
+        g.dim = dim
+        g.kind = kind
+        g.nfield = F
+        g.sentinel_nan = int(self._sentinel_nan)
+        for a in range(4):
+            g.n[a] = n[a] if a < dim else 1
+            g.lo[a] = float(lo[a]) if a < dim else 0.0
+            g.hi[a] = float(hi[a]) if a < dim else 0.0
+            g.h[a] = float(h[a]) if a < dim else 1.0
+        g.nc = self.nc
+        g.grid64 = grid64.data_ptr()
+        g.grid32 = _ptr(grid32)
+        g.table = None
+        g.table_prec = 0
+        self._g = g
+
+    def _set_counts(self, n):
+        raise NotImplementedError
+
+    # ------------------------------------------------------------ coefficients
+    @property
+    def _M(self):
+        return 4 ** self._dim
+
+    def _ensure_table(self):
+        if self._table is None:
+            dt = torch.float64 if self.precision == "fp64" else torch.float32
+            self._table = torch.zeros(self.nc * self._F * self._M, dtype=dt, device=self.device)
+            self._table_prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_MIXED
+            self._g.table = self._table.data_ptr()
+            self._g.table_prec = self._table_prec
+            self._solved = np.zeros(self.nc, dtype=bool)
+
+    def _solve(self, cell0, ncells):
+        self._ensure_table()
+        L = lib()
+        rc = L.arb_coef_solve(self._g, self._table_prec, cell0, ncells,
+                              self._table.data_ptr() + cell0 * self._F * self._M * self._table.element_size(),
+                              self._status.data_ptr(), _stream())
+        check(rc, "arb_coef_solve")
+        self._solved[cell0:cell0 + ncells] = True
+
+    def allCoeffs(self):
+        """Solve every cell's coefficients (ARB:523-525, 1260-1262)."""
+        self._solve(0, self.nc)
+
+    def calcCoefficients(self, alphaindex):
+        """Solve one cell (ARB:570-603, 1322-1355)."""
+        i = int(alphaindex)
+        if 0 <= i < self.nc and (self._solved is None or not self._solved[i]):
+            self._solve(i, 1)
+
+    @property
+    def _table_complete(self):
+        return self._solved is not None and bool(self._solved.all())
+
+    # ------------------------------------------------------------------ queries
+    def _use_table(self):
+        if self.strategy == "table":
+            if not self._table_complete:
+                self.allCoeffs()
+            return True
+        if self.strategy == "otf":
+            return False
+        return self._table_complete
+
+    def _run(self, qd, n, qs, writeback, want_oob):
+        """Launch the evaluation kernel on device rows qd; returns device outputs."""
+        L = lib()
+        dev = self.device
+        dim, kind = self._dim, self._kind
+        f64 = dict(dtype=torch.float64, device=dev)
+        comps = torch.empty((n, 3), **f64) if kind in (_lib.KIND_VECTOR, _lib.KIND_BOTH) else None
+        norms = torch.empty((n, 1), **f64) if kind != _lib.KIND_VECTOR else None
+        grads = torch.empty((n, dim), **f64) if kind != _lib.KIND_VECTOR else None
+        inds = torch.empty(n, dtype=torch.int64, device=dev)
+        oob = torch.empty(n, dtype=torch.int64, device=dev) if want_oob else None
+        cnt = torch.zeros(1, dtype=torch.int64, device=dev) if want_oob else None
+        out = ArbQueryOut(_ptr(comps), _ptr(norms), _ptr(grads), _ptr(inds), _ptr(oob), _ptr(cnt))
+        s = _stream()
+        if self._use_table():
+            rc = L.arb_query_eval(self._g, qd.data_ptr(), n, qs, int(writeback), out,
+                                  self._status.data_ptr(), s)
+        else:
+            prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_MIXED
+            rc = L.arb_query_eval_otf(self._g, prec, qd.data_ptr(), n, qs, int(writeback), out,
+                                      self._status.data_ptr(), s)
+        check(rc, "query evaluation")
+        return comps, norms, grads, inds, oob, cnt
+
+    def _fetch_status(self):
+        return lib().arb_status_fetch(self._status.data_ptr(), _stream())
+
+    def _pack(self, comps, norms, grads):
+        k = self._kind
+        if k == _lib.KIND_VECTOR:
+            return comps
+        if k == _lib.KIND_BOTH:
+            return comps, norms, grads
+        return norms, grads
+
+    def rQuery(self, query):
+        """Range query (rQuery1/2/3, ARB:344-521 / 1064-1258).  Rows outside
+        the interpolation volume come back NaN and are overwritten with NaN
+        in the caller's array, as the reference does."""
+        dim = self._dim
+        if isinstance(query, torch.Tensor) and query.is_cuda:
+            n, qs = int(query.shape[0]), int(query.shape[1])
+            if qs < dim:
+                raise IndexError("query rows need at least %d columns" % dim)
+            direct = query.dtype == torch.float64 and query.is_contiguous()
+            qd = query if direct else query.to(torch.float64).contiguous()
+            res = self._run(qd, n, qs, True, False)
+            if not direct:
+                query.copy_(qd.to(query.dtype))
+            self._last_inds = res[3]
+            if self.check:
+                st = self._fetch_status()
+                if st & _lib.ARB_ERR_CELL_INDEX:
+                    raise IndexError("cell index beyond the coefficient table (query on an upper face)")
+            return self._pack(*res[:3])
+        qa = query if isinstance(query, np.ndarray) else np.asarray(query)
+        n, qs = int(qa.shape[0]), int(qa.shape[1])
+        if qs < dim:
+            raise IndexError("query rows need at least %d columns" % dim)
+        qc = np.ascontiguousarray(qa, dtype=np.float64)
+        qd = torch.from_numpy(qc).to(self.device, non_blocking=True)
+        comps, norms, grads, inds, oob, cnt = self._run(qd, n, qs, False, True)
+        host = []
+        for t in (comps, norms, grads):
+            if t is None:
+                host.append(None)
+                continue
+            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+            h.copy_(t, non_blocking=True)
+            host.append(h)
+        st = self._fetch_status()          # synchronises the stream
+        nbad = int(cnt.item())
+        if nbad:
+            rows = oob[:nbad].cpu().numpy()
+            qa[rows] = np.nan              # in-place on the caller's array
+        self._last_inds = inds
+        if st & _lib.ARB_ERR_CELL_INDEX:
+            raise IndexError("cell index beyond the coefficient table (query on an upper face)")
+        out = [None if h is None else h.numpy() for h in host]
+        return self._pack(*out)
+
+    def sQuery(self, query):
+        """Single point (sQuery1/2/3, ARB:213-342 / 916-1062): np.nan outside
+        the volume, otherwise components / (value, gradient) / both."""
+        dim = self._dim
+        is_t = isinstance(query, torch.Tensor)
+        qv = [float(query[a]) for a in range(dim)]
+        for a in range(dim):
+            if qv[a] < self._lo[a] or qv[a] > self._hi[a]:
+                return np.nan
+        row = torch.tensor([qv], dtype=torch.float64).to(self.device)
+        comps, norms, grads, inds, _, _ = self._run(row, 1, dim, False, False)
+        st = self._fetch_status()
+        self._last_ind = inds
+        if st & _lib.ARB_ERR_CELL_INDEX:
+            raise IndexError("cell index beyond the coefficient table (query on an upper face)")
+        k = self._kind
+        if is_t:
+            c = None if comps is None else comps[0]
+            nv = None if norms is None else norms[0, 0]
+            gv = None if grads is None else grads[0]
+        else:
+            c = None if comps is None else comps[0].cpu().numpy()
+            nv = None if norms is None else np.float64(norms[0, 0].item())
+            gv = None if grads is None else grads[0].cpu().numpy()
+        if k == _lib.KIND_VECTOR:
+            return c
+        if k == _lib.KIND_BOTH:
+            return c, nv, gv
+        return nv, gv
+
+    def Query(self, query):
+        """Shape dispatch (Query1/2/3, ARB:177-211): rows -> rQuery, a single
+        point -> sQuery."""
+        shape = tuple(query.shape)
+        if len(shape) >= 2 and shape[1] > 1:
+            try:
+                return self.rQuery(query)
+            except IndexError:
+                # The reference catches rQuery's IndexError and retries sQuery
+                # on the 2-D array, whose scalar comparison raises ValueError.
+                raise ValueError("The truth value of an array with more than one element is ambiguous. "
+                                 "Use a.any() or a.all() (a query row fell on an upper face and its "
+                                 "cell index exceeded the coefficient table)") from None
+        return self.sQuery(query)
+
+    # ---------------------------------------------------------- attributes
+    @property
+    def queryInds(self):
+        return None if self._last_inds is None else self._last_inds.cpu().numpy()
+
+    @property
+    def queryInd(self):
+        return None if self._last_ind is None else int(self._last_ind[0].item())
+
+    @property
+    def A(self):
+        return matrices.A3() if self._dim == 3 else matrices.A4()
+
+    @property
+    def alphamask(self):
+        m = np.zeros((self.nc + 1, 1))
+        if self._solved is not None:
+            m[:-1, 0] = self._solved
+        m[-1] = 1
+        return m
+
+    def _alpha(self, f):
+        cols = self.nc + 1 + (1 if self._extra_col else 0)
+        out = np.zeros((self._M, cols))
+        if self._table is not None:
+            t = self._table.view(self.nc, self._F, self._M)[:, f, :]
+            out[:, :self.nc] = t.to(torch.float64).T.cpu().numpy()
+        if self._extra_col:
+            out[:, -1] = np.nan
+        elif self._sentinel_nan:
+            out[:, self.nc] = np.nan
+        return out
+
+    def _field_index(self, name):
+        k = self._kind
+        if k == _lib.KIND_VECTOR:
+            return {"alphax": 0, "alphay": 1, "alphaz": 2}.get(name)
+        if k == _lib.KIND_BOTH:
+            return {"alphax": 0, "alphay": 1, "alphaz": 2, "alphan": 3}.get(name)
+        return {"alphan": 0}.get(name)
+
+    def __getattr__(self, name):
+        # lazily materialised reference attributes (device -> host on demand)
+        if name in ("alphax", "alphay", "alphaz", "alphan"):
+            f = self._field_index(name)
+            if f is None:
+                raise AttributeError(name)
+            return self._alpha(f)
+        if name in ("Bx", "By", "Bz", "Bn"):
+            return self._values(name)
+        if name == "inputfield":
+            return self._inputfield()
+        if name == "basePointInds":
+            return self._base_point_inds()
+        raise AttributeError(name)
+
+    def _grid_vals(self):
+        return self._grid64.view(self._npts, self._F)
+
+    def _values(self, name):
+        k = self._kind
+        g = self._grid_vals()
+        comp = {"Bx": 0, "By": 1, "Bz": 2}
+        if name == "Bn":
+            if k in (_lib.KIND_SCALAR, _lib.KIND_NORM):
+                return g[:, 0].cpu().numpy()
+            if k == _lib.KIND_BOTH:
+                return g[:, 3].cpu().numpy()
+            raise AttributeError(name)
+        if k in (_lib.KIND_VECTOR, _lib.KIND_BOTH):
+            return g[:, comp[name]].cpu().numpy()
+        raise AttributeError(name)
+
+    def _inputfield(self):
+        dim = self._dim
+        grids = torch.meshgrid(*reversed(self._axes_dev), indexing="ij")
+        coords = [grids[dim - 1 - a].reshape(-1) for a in range(dim)]
+        k = self._kind
+        g = self._grid_vals()
+        if k == _lib.KIND_SCALAR:
+            vals = [g[:, 0]]
+        elif k == _lib.KIND_NORM:
+            r = self._raw.view(self._npts, 3)
+            vals = [r[:, 0], r[:, 1], r[:, 2]]
+        else:
+            vals = [g[:, 0], g[:, 1], g[:, 2]]
+        out = torch.stack(coords + vals, dim=1).cpu().numpy()
+        return out.astype(self._field_dtype)
+
+    def _base_point_inds(self):
+        n = self._n
+        idx = [np.arange(1, v - 2) for v in n]
+        strides = np.cumprod([1] + n[:-1])
+        tot = np.zeros(1, dtype=np.int64)
+        for a in reversed(range(self._dim)):
+            tot = (tot[:, None] + idx[a][None, :] * strides[a]).reshape(-1)
+        return np.sort(tot)
+
+
+class tricubic(_Interpolant):
+    """Tricubic interpolant of a 3D scalar (N x 4) or vector (N x 6) field."""
+    __version__ = "1.8"
+    _dim = 3
+
+    def _set_counts(self, n):
+        self.nPos = np.array([n[0] - 3, n[1] - 3, n[2] - 3])
+
+    def neighbourInd(self, ind0):
+        """64 flat grid indices of the 4x4x4 block around base index ind0 (ARB:605-621)."""
+        nx, ny = self._n[0], self._n[1]
+        o = np.arange(4) - 1
+        return (int(ind0) + (o[None, None, :] + nx * o[None, :, None] + nx * ny * o[:, None, None])).ravel()
+
+
+class quadcubic(_Interpolant):
+    """Quadcubic interpolant of a 4D scalar (N x 5) or vector (N x 7) field."""
+    __version__ = "1.8"
+    _dim = 4
+
+    def _set_counts(self, n):
+        self.nPosx, self.nPosy, self.nPosz, self.nPost = n
+
+    def neighbourInd(self, ind0):
+        """256 flat grid indices of the 4^4 block around base index ind0 (ARB:1357-1381)."""
+        nx, ny, nz = self._n[0], self._n[1], self._n[2]
+        o = np.arange(4) - 1
+        off = (o[None, None, None, :] + nx * o[None, None, :, None] + nx * ny * o[None, :, None, None]
+               + nx * ny * nz * o[:, None, None, None])
+        return (int(ind0) + off).ravel()

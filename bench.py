@@ -1,0 +1,388 @@
+#!/usr/bin/env python
+"""Benchmark: tricubic 'both'-mode queries/s on a 256^3 dipole vector field.
+
+One step = the whole interpolation job on one batch: construct the
+interpolant from the N x 6 field (ingest, per-mode fields) and evaluate
+1.01e7 query rows (1e7 uniform in the interpolation volume + 1e5 just
+outside it, which must come back NaN), in the precision under test
+(default 'mixed': split float32 evaluation with a float64 index step).
+The float64 drop-in path is timed beside it.
+
+value: queries/s with the field and queries already resident in HBM.
+e2e:   the same job through the public API with host (pinned NumPy) buffers:
+       field + queries host->device and comps/norms/grads device->host inside
+       the timed region.
+Inputs are larger than L2 (field 805 MB, queries 242 MB), so no flush.
+
+Multi-GPU: replicas (every rank builds the full field and evaluates its own
+1.01e7 queries; no collective): scaling "weak", value = all ranks' queries /
+max-over-ranks time.
+
+--impl reference times the CPU oracle port of the reference's algorithm
+(lazy per-cell A @ f solve + monomial evaluation, NumPy/BLAS on all host
+threads) on fresh 1e5-row samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tricubic queries/s at 256³ 'both': split-BF16 vs FP64 GPU at ≤1e-6 rel err"
+N_IN, N_OUT = 10_000_000, 100_000
+GRID = (256, 256, 256)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--strategy", default="auto", choices=["auto", "otf", "table"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--kernel-only", action="store_true", help="time only the query kernel (profiling)")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6789.0), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- workload
+def make_workload(device, rank=0):
+    import torch
+    from arbinterp_gb300 import synth
+    field = synth.dipole_field3(n=GRID, seed=1, device=device)
+    h = 2.0 / (GRID[0] - 1)
+    ax = -1.0 + h * torch.arange(GRID[0], dtype=torch.float64)
+    lo = [float(ax[1])] * 3
+    hi = [float(ax[GRID[0] - 2])] * 3
+    q = synth.uniform_queries(lo, hi, N_IN, N_OUT, [h] * 3, seed=10 + rank, device=device)
+    return field, q, lo, hi, [h] * 3
+
+
+def cuda_time(fn, steps, warmup, barrier=None):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    if barrier:
+        barrier()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(steps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    if barrier:
+        barrier()
+    return s.elapsed_time(e) / 1000.0
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(field_np, q_np, lo, hi, h, budget_s=25.0, sample=100_000):
+    """Time the oracle port on the host: construct once, then fresh cold
+    samples (lazy solve of each sample's cells + evaluation).  The whole-job
+    time is estimated as construct + N * eval/query + D * solve/cell with D
+    the expected number of distinct cells 1.01e7 uniform queries touch."""
+    import numpy as np
+    from oracle.arb_oracle import OracleTricubic
+    t0 = time.perf_counter()
+    o = OracleTricubic(field_np, mode="both")
+    t_con = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    ev, sv, nq, ncell = 0.0, 0.0, 0, 0
+    t_start = time.perf_counter()
+    while time.perf_counter() - t_start < budget_s or nq == 0:
+        idx = rng.integers(0, len(q_np), sample)
+        qs = q_np[idx].copy()
+        bad = np.zeros(len(qs), bool)
+        for a in range(3):
+            bad |= (qs[:, a] < lo[a]) | (qs[:, a] > hi[a])
+        qq = qs[~bad]
+        fl = [np.floor((qq[:, a] - o.lo[a]) / o.h[a]) for a in range(3)]
+        cells = np.unique((fl[0] + fl[1] * o.ncell[0] + fl[2] * o.ncell[0] * o.ncell[1]).astype(np.int64))
+        cells = cells[(cells < o.nc) & ~o.solved[cells]]
+        t1 = time.perf_counter()
+        o._solve(cells)
+        t2 = time.perf_counter()
+        o.query(qs)
+        t3 = time.perf_counter()
+        sv += t2 - t1
+        ev += t3 - t2
+        nq += len(qs)
+        ncell += len(cells)
+    n_total = N_IN + N_OUT
+    D = o.nc * (1.0 - math.exp(-N_IN / o.nc))
+    t_est = t_con + n_total * ev / nq + D * sv / max(ncell, 1)
+    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return {
+        "value": n_total / t_est, "unit": "queries/s", "cores": threads, "kind": "port",
+        "sample": (f"oracle port (NumPy/BLAS, {threads} host threads): construct 256^3 once "
+                   f"({t_con:.1f} s) + {nq} cold sample queries solving {ncell} cells; "
+                   f"whole-job time estimated for 1.01e7 queries and {D:.3g} distinct cells"),
+        "construct_s": t_con, "solve_us_per_cell": 1e6 * sv / max(ncell, 1),
+        "eval_us_per_query": 1e6 * ev / nq,
+    }
+
+
+def run_reference(args):
+    """Reference arm: the CPU oracle port (the reference is pure Python and
+    does not travel to the GPU host); each step = one fresh 1e5-row sample
+    with the lazy coefficient solve of its cells."""
+    import numpy as np
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.arb_oracle import OracleTricubic
+    field, q, lo, hi, h = make_workload("cpu")
+    field_np, q_np = field.numpy(), q.numpy()
+    t0 = time.perf_counter()
+    o = OracleTricubic(field_np, mode="both")
+    t_con = time.perf_counter() - t0
+    rng = np.random.default_rng(1)
+    S = 100_000
+
+    def step():
+        qs = q_np[rng.integers(0, len(q_np), S)].copy()
+        o.query(qs)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    val = S * args.steps / dt
+    line = {
+        "metric": METRIC, "value": val, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "tricubic 256^3 dipole vector field, mode both; 1e5-row samples of the "
+                               "1.01e7-query set (1% outside the volume)",
+                   "construct_s": t_con},
+        "cpu_baseline": {"value": val, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"each step: {S} fresh rows, lazy A@f solve of their new cells + "
+                                   f"monomial evaluation (oracle port, NumPy/BLAS {threads} threads); "
+                                   f"construction ({t_con:.1f} s) outside the timed steps"},
+        "e2e": {"value": val, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    del torch
+
+
+# ---------------------------------------------------------------- our arm
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    barrier = (lambda: dist.barrier()) if world > 1 else None
+
+    from arbinterp_gb300 import tricubic, _lib
+    _lib.lib()
+    dev = torch.device("cuda", local)
+    field, q, lo, hi, h = make_workload(dev, rank)
+    nq = q.shape[0]
+    prec, strat = args.precision, args.strategy
+
+    def step_dev():
+        o = tricubic(field, "quiet", mode="both", precision=prec, strategy=strat)
+        return o.Query(q)
+
+    def tmax(t):
+        if world == 1:
+            return t
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        return float(tt.item())
+
+    gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0]) if \
+        os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local
+
+    if args.kernel_only:
+        o = tricubic(field, "quiet", mode="both", precision=prec, strategy=strat)
+        t = cuda_time(lambda: o._run(q, nq, 3, False, False), args.steps, args.warmup)
+        print(json.dumps({"kernel_ms": 1000 * t / args.steps}))
+        return
+
+    with ClockSampler(gpu_index) as clk:
+        dt = cuda_time(step_dev, args.steps, args.warmup, barrier)
+    dt = tmax(dt)
+    value = world * nq * args.steps / dt
+
+    # per-launch time of the query kernel alone (the dominant kernel)
+    o = tricubic(field, "quiet", mode="both", precision=prec, strategy=strat)
+    use_tab = o._use_table()
+    kt = cuda_time(lambda: o._run(q, nq, 3, False, False), 5, 2) / 5
+    F = 4
+    grid_bytes = o._npts * F * (8 if prec == "mixed" else 8)
+    io_bytes = nq * (3 * 8 + 7 * 8 + 8)
+    if use_tab:
+        algo = nq * F * 64 * (4 if prec == "mixed" else 8) + io_bytes
+        kname = "tab_kernel<3,4>"
+    else:
+        algo = grid_bytes + io_bytes
+        kname = "otf3_kernel<4,%s>" % ("true" if prec == "mixed" else "false")
+    peak, peak_src = measured_peaks()
+    achieved = algo / kt / 1e9
+
+    # precision of the mixed path against the float64 GPU path (pinned to the oracle)
+    extra = {}
+    if not args.no_fp64:
+        o64 = tricubic(field, "quiet", mode="both", precision="fp64", strategy="otf")
+        t64 = cuda_time(lambda: tricubic(field, "quiet", mode="both", precision="fp64").Query(q),
+                        max(2, args.steps // 3), 1)
+        t64 = tmax(t64)
+        v64 = world * nq * max(2, args.steps // 3) / t64
+        ref = o64.Query(q.clone())
+        got = o.Query(q.clone())
+        errs = {}
+        for name, a, b in zip(("comps", "norms", "grads"), got, ref):
+            m = torch.isfinite(b).all(1)
+            assert torch.equal(torch.isnan(a), torch.isnan(b)), name
+            d = (a[m] - b[m]).abs().amax(0) / b[m].abs().amax(0)
+            errs[name] = [float(x) for x in d]
+        same_inds = bool(torch.equal(o._last_inds, o64._last_inds))
+        extra = {"fp64_path": {"value": v64, "unit": "queries/s", "ms_per_step": 1000 * t64 / max(2, args.steps // 3)},
+                 "speedup_vs_fp64": value / v64,
+                 "max_rel_err_vs_fp64": errs, "indices_bitexact": same_inds}
+
+    # warm query-only throughput (interpolant already constructed)
+    tq = cuda_time(lambda: o.Query(q), 5, 2) / 5
+    extra["warm_query_only"] = {"value": world * nq / tq, "unit": "queries/s"}
+
+    e2e = None
+    if not args.no_e2e:
+        field_h = torch.empty(field.shape, dtype=field.dtype, pin_memory=True)
+        field_h.copy_(field)
+        q_h = torch.empty(q.shape, dtype=q.dtype, pin_memory=True)
+        q_h.copy_(q)
+        fnp, qnp = field_h.numpy(), q_h.numpy()
+        last = {}
+
+        def step_host():
+            ob = tricubic(fnp, "quiet", mode="both", precision=prec, strategy=strat)
+            last["out"] = ob.Query(qnp)
+
+        te = cuda_time(step_host, max(3, args.steps // 2), 2, barrier)
+        te = tmax(te)
+        ksteps = max(3, args.steps // 2)
+        d2h = sum(a.nbytes for a in last["out"])
+        e2e = {"value": world * nq * ksteps / te, "unit": "queries/s",
+               "h2d_bytes_per_step": int(fnp.nbytes + qnp.nbytes), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": 1000 * te / ksteps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(field.cpu().numpy(), q.cpu().numpy(), lo, hi, h)
+
+    if rank == 0:
+        launches_per_step = 6   # ingest: init, min, collect, sort, scatter; query: 1
+        line = {
+            "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == "mixed" else "f64",
+            "data": "synthetic",
+            "config": {"workload": "tricubic 256^3 dipole vector field (16 dipoles outside the box), mode both, "
+                                   "construct + 1.01e7 queries (1% outside the volume)",
+                       "precision": prec, "strategy": "table" if use_tab else "otf",
+                       "l2": "inputs larger than L2 (field 805 MB, queries 242 MB); no flush"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": kname,
+                         "kernel_ms": 1000 * kt, "algorithmic_bytes": algo, "peak_source": peak_src},
+            "clocks": clk.summary(),
+            "gpu_launches": launches_per_step * args.steps,
+            "e2e": e2e, "cpu_baseline": cpu,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

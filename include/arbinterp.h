@@ -1,0 +1,161 @@
+/*
+ * arbinterp.h — C ABI of the GB300 (sm_103a) Lekien–Marsden tricubic /
+ * quadcubic interpolation path.
+ *
+ * Every entry point takes DEVICE pointers, sizes and a CUDA stream, launches
+ * work on that stream and returns an arb_status.  Nothing here allocates
+ * device memory: callers (the Python drop-in, or any C/C++ host) own every
+ * buffer.  Errors found on the device (an irregular grid, a cell index past
+ * the table) are OR-ed into a caller-owned device status word; read it with
+ * arb_status_fetch() after the stream work is done.  No C++ exception crosses
+ * this boundary.
+ *
+ * Data layout in device memory (see arb_grid):
+ *   grid64  [npts][F] float64, points z-major with x fastest (t slowest in 4D)
+ *   grid32  [npts][F][2] float32 (hi, lo) with hi + lo == value to ~2^-48
+ *   table   [nc][F][M] coefficients (M = 64 in 3D, 256 in 4D), float64 or
+ *           float32, monomial index ex + 4 ey + 16 ez (+ 64 et)
+ * F (fields) is 1 for scalar and norm modes, 3 for vector mode and 4 for
+ * both mode (order Bx, By, Bz, |B|).
+ *
+ * The reference (DurhamDecLab/ARBInterp v1.8) is a pure Python/NumPy module
+ * with no FFI; each function below cites the reference method whose work it
+ * replaces (paths relative to the reference project root).
+ */
+#ifndef ARBINTERP_H
+#define ARBINTERP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *arb_stream_t; /* same type as cudaStream_t */
+
+enum arb_status {
+  ARB_OK = 0,
+  ARB_ERR_INVALID = 1,        /* bad argument: null pointer, bad sizes      */
+  ARB_ERR_CUDA = 2,           /* a CUDA runtime call or launch failed        */
+  ARB_ERR_IRREGULAR_GRID = 4, /* field rows are not a full tensor grid       */
+  ARB_ERR_CELL_INDEX = 8,     /* a query's cell index exceeded nc            */
+  ARB_ERR_CAPACITY = 16,      /* an axis has more points than axis_cap       */
+  ARB_ERR_TIMEOUT = 32,       /* a bounded device wait gave up               */
+  ARB_ERR_UNSUPPORTED = 64    /* combination not built (e.g. dim/F/precision) */
+};
+
+enum arb_precision {
+  ARB_PREC_FP64 = 0,  /* everything in float64 (parity with the reference)  */
+  ARB_PREC_MIXED = 1  /* split-precision tensor-core / float32 evaluation   */
+};
+
+enum arb_kind {
+  ARB_KIND_SCALAR = 0, /* N x 4 (3D) / N x 5 (4D) input: value + gradient   */
+  ARB_KIND_VECTOR = 1, /* components only                                   */
+  ARB_KIND_NORM = 2,   /* |B| interpolated as its own field + gradient      */
+  ARB_KIND_BOTH = 3    /* components, |B| and its gradient                  */
+};
+
+/* A constructed interpolant: grid geometry plus device buffers. */
+typedef struct arb_grid {
+  int32_t dim;          /* 3 or 4                                           */
+  int32_t kind;         /* enum arb_kind                                    */
+  int32_t nfield;       /* F                                                */
+  int32_t sentinel_nan; /* cell index == nc: 1 -> NaN row, 0 -> zero row   */
+  int64_t n[4];         /* grid points per axis (x, y, z, t)                */
+  int64_t nc;           /* cells = prod(n[a] - 3)                           */
+  double lo[4];         /* xIntMin.. : second grid coordinate per axis      */
+  double hi[4];         /* xIntMax.. : second-to-last grid coordinate       */
+  double h[4];          /* spacing from the first two axis samples          */
+  const double *grid64; /* [npts][F]                                        */
+  const float *grid32;  /* [npts][F][2] or NULL                             */
+  const void *table;    /* [nc][F][M] or NULL                               */
+  int32_t table_prec;   /* enum arb_precision of table (FP64: double)      */
+  int32_t reserved;
+} arb_grid;
+
+/* Query outputs.  Any pointer may be NULL when not wanted.  Row-major like
+ * the reference's return arrays. */
+typedef struct arb_query_out {
+  double *comps;     /* [nq][3]   vector and both modes                     */
+  double *norms;     /* [nq]      scalar, norm and both modes               */
+  double *grads;     /* [nq][dim] scalar, norm and both modes               */
+  int64_t *inds;     /* [nq]      cell index per row (queryInds)            */
+  int64_t *oob_rows; /* [nq]      rows found outside the volume, any order  */
+  unsigned long long *oob_count; /* device counter for oob_rows (zeroed by caller) */
+} arb_query_out;
+
+/* ---- ingest: replaces getFieldParams (src/ARBInterp/ARBInterp.py:528-568,
+ *      1264-1320), the argsort-based lexicographic sort and exact-equality
+ *      axis discovery. ------------------------------------------------------ */
+
+/* Scratch bytes arb_ingest_axes needs in `work`. */
+size_t arb_ingest_axes_work_bytes(int32_t dim);
+
+/* Finds each axis' sample values (points on the axis lines through the
+ * lexicographically smallest point), sorted ascending.  Writes
+ * axis_out[a * axis_cap + i] and axis_count[a] (device).  axis_out holds
+ * 2 * dim * axis_cap doubles: the second half stages the unsorted lists.
+ * field is [npts][ncol] float64 (field_is_f32 == 0) or float32. */
+int arb_ingest_axes(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                    int32_t dim, int64_t axis_cap, double *axis_out, int64_t *axis_count,
+                    void *work, size_t work_bytes, int32_t *status, arb_stream_t stream);
+
+/* Scatters every field row to its grid slot (the sorted order the reference
+ * builds with argsort) and writes the per-mode interpolated fields: grid64,
+ * optionally grid32 (hi/lo split) and, when raw_out is given, the raw value
+ * columns [npts][ncol-dim] in sorted order.  claim is npts uint32 of scratch
+ * (zeroed here) used to detect duplicate points.  n holds the host-side axis
+ * counts returned by arb_ingest_axes. */
+int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                       int32_t dim, const double *axes, int64_t axis_cap, const int64_t *n,
+                       int32_t kind, double *grid64, float *grid32, double *raw_out,
+                       uint32_t *claim, int32_t *status, arb_stream_t stream);
+
+/* ---- finite-difference planes: replaces the D matrix of makeAMatrix
+ *      (src/ARBInterp/ARBInterp.py:129-173, 762-876) applied per grid point.
+ *      planes is [2^dim][npts][F] float64: kind r (f, fx, fy, fz, fxy, fxz,
+ *      fyz, fxyz in 3D; the reference's 16 kinds in 4D) as central
+ *      differences in unit-cell units.  Boundary points (no neighbour on an
+ *      axis) get NaN for kinds that need it. ------------------------------ */
+int arb_fd_planes(const arb_grid *g, double *planes, arb_stream_t stream);
+
+/* ---- coefficient solve: replaces calcCoefficients1/2/3 and allCoeffs
+ *      (src/ARBInterp/ARBInterp.py:523-525, 570-603; 4D 1260-1262,
+ *      1322-1355).  Writes table[cell][F][M] for cells [cell0, cell0+ncells).
+ *      ARB_PREC_FP64: float64 table, exact separable form of A = inv(B) D.
+ *      ARB_PREC_MIXED: float32 table from the tcgen05 tensor-core GEMM with
+ *      split-precision operands. ------------------------------------------ */
+int arb_coef_solve(const arb_grid *g, int32_t precision, int64_t cell0, int64_t ncells,
+                   void *table, int32_t *status, arb_stream_t stream);
+
+/* ---- query evaluation from the coefficient table: replaces rQuery1/2/3
+ *      (src/ARBInterp/ARBInterp.py:344-521; 4D 1064-1258).  q is [nq] rows
+ *      of q_stride doubles (x, y, z[, t], ...).  Rows outside
+ *      [IntMin, IntMax] on any axis come back NaN in every output; when
+ *      q_writeback is nonzero those rows of q are overwritten with NaN in
+ *      place, like the reference does to its caller's array. -------------- */
+int arb_query_eval(const arb_grid *g, double *q, int64_t nq, int64_t q_stride,
+                   int32_t q_writeback, const arb_query_out *out, int32_t *status,
+                   arb_stream_t stream);
+
+/* ---- on-the-fly evaluation straight from the grid (no table): same
+ *      contract as arb_query_eval; precision selects float64 or the
+ *      split float32 (hi/lo delta) evaluation that needs g->grid32. ------- */
+int arb_query_eval_otf(const arb_grid *g, int32_t precision, double *q, int64_t nq,
+                       int64_t q_stride, int32_t q_writeback, const arb_query_out *out,
+                       int32_t *status, arb_stream_t stream);
+
+/* Reads (and clears) the device status word after the stream's work is
+ * done; returns ARB_OK, an arb_status bit set, or ARB_ERR_CUDA. */
+int arb_status_fetch(int32_t *status, arb_stream_t stream);
+
+/* Library version string ("arbinterp-gb300 <ver> sm_103a"). */
+const char *arb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ARBINTERP_H */

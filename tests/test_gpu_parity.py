@@ -1,0 +1,253 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's golden
+outputs (small cases) and the CPU oracle (seeded synthetic fields).
+
+Bars: cell indices, NaN masks and the in-place NaN rows of the caller's query
+array bit-exact; values <= 1e-12 normwise in float64, <= 1e-6 in mixed
+precision (normwise = max|got - ref| / max|ref| per output column)."""
+import numpy as np
+import pytest
+
+from conftest import c0_field, normwise
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "mixed": 1e-6}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from arbinterp_gb300 import _lib
+    _lib.lib()
+
+
+def _mods():
+    from arbinterp_gb300 import tricubic, quadcubic
+    return tricubic, quadcubic
+
+
+def _check(res, g, prefix, qafter, inds, tol):
+    assert np.array_equal(inds, g[prefix + "inds"])
+    assert np.array_equal(np.isnan(qafter).all(axis=1), g[prefix + "nanrows"])
+    names = [k for k in ("comps", "norms", "grads") if prefix + k in g]
+    if len(names) == 1:
+        res = (res,)
+    for k, got in zip(names, res):
+        ref = g[prefix + k]
+        assert got.shape == ref.shape, k
+        assert np.array_equal(np.isnan(got), np.isnan(ref)), k
+        err = normwise(got, ref)
+        assert (err <= tol).all(), (k, err)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("strategy", ["otf", "table"])
+def test_c0_scalar_golden(golden, prec, strategy):
+    tricubic, _ = _mods()
+    g = golden
+    o = tricubic(c0_field(g), "quiet", precision=prec, strategy=strategy)
+    assert np.array_equal(o.nPos, g["c0_p_nPos"]) and o.nc == int(g["c0_p_nc"])
+    assert np.array_equal(np.array([o.hx, o.hy, o.hz]), g["c0_p_h"])
+    assert np.array_equal(np.array([o.xIntMin, o.yIntMin, o.zIntMin]), g["c0_p_lo"])
+    assert np.array_equal(np.array([o.xIntMax, o.yIntMax, o.zIntMax]), g["c0_p_hi"])
+    assert np.array_equal(o.basePointInds, g["c0_p_basePointInds"])
+    q = g["c0_q"].copy()
+    res = o.Query(q)
+    _check(res, g, "c0_", q, o.queryInds, TOL[prec])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("tag,mode", [("both", "both"), ("norm", "norm"), ("vector", "vector"),
+                                      ("default", None), ("invalid", "sideways")])
+def test_vector_modes_golden(golden, prec, tag, mode):
+    tricubic, _ = _mods()
+    g = golden
+    kw = {} if mode is None else {"mode": mode}
+    o = tricubic(g["vec_field"], "quiet", precision=prec, **kw)
+    q = g[f"vec_{tag}_q"].copy()
+    res = o.Query(q)
+    _check(res, g, f"vec_{tag}_", q, o.queryInds, TOL[prec])
+    # single points: statuses and values as the reference returned them
+    pts = g[f"vec_{tag}_sp_pts"]
+    for p, st, vals in zip(pts, g[f"vec_{tag}_sp_status"], g[f"vec_{tag}_sp_vals"]):
+        if st == "ok":
+            r = o.Query(p.copy())
+            flat = np.concatenate([np.atleast_1d(np.asarray(v, float)) for v in (r if isinstance(r, tuple) else (r,))])
+            want = vals[:len(flat)]
+            assert np.array_equal(np.isnan(flat), np.isnan(want))
+            m = np.isfinite(want)
+            assert np.abs(flat[m] - want[m]).max() <= 10 * TOL[prec] * max(1.0, np.abs(want[m]).max())
+        else:
+            # out of volume: bare NaN; in norm/both mode the reference's
+            # tuple-unpack of that NaN raises TypeError
+            r = o.sQuery(p.copy())
+            assert isinstance(r, float) and np.isnan(r)
+
+
+def test_both_coefficients_and_attributes(golden):
+    tricubic, _ = _mods()
+    g = golden
+    o = tricubic(g["vec_field"], "quiet", mode="both")
+    assert np.array_equal(o.inputfield, g["vec_inputfield"])
+    o.allCoeffs()
+    for name in ("alphax", "alphan"):
+        ref = g[f"vec_both_{name}"]
+        mine = getattr(o, name)
+        assert mine.shape == ref.shape
+        assert np.array_equal(np.isnan(mine), np.isnan(ref))
+        m = np.isfinite(ref)
+        assert np.abs(mine[m] - ref[m]).max() <= 1e-12 * np.abs(ref[m]).max()
+    assert np.array_equal(o.alphamask[:, 0], g["vec_both_mask"])
+    ov = tricubic(g["vec_field"], "quiet", mode="vector")
+    ov.allCoeffs()
+    ref = g["vec_vector_alphay"]
+    mine = ov.alphay
+    assert mine.shape == ref.shape and np.array_equal(np.isnan(mine), np.isnan(ref))
+    m = np.isfinite(ref)
+    assert np.abs(mine[m] - ref[m]).max() <= 1e-12 * np.abs(ref[m]).max()
+
+
+@pytest.mark.parametrize("strategy", ["otf", "table"])
+@pytest.mark.parametrize("tag,mode", [("scalar", None), ("norm", "norm")])
+def test_upper_face_aliasing_and_errors(golden, strategy, tag, mode):
+    tricubic, _ = _mods()
+    g = golden
+    fld = g["face_field"] if tag == "scalar" else np.hstack([g["face_field"][:, :3], g["face_norm_vals"]])
+    kw = {} if mode is None else {"mode": mode}
+    o = tricubic(fld, "quiet", strategy=strategy, **kw)
+    q = g[f"face_{tag}_q"].copy()
+    res = o.Query(q)
+    _check(res, g, f"face_{tag}_", q, o.queryInds, 1e-12)
+    assert str(g[f"face_{tag}_err_rQuery"]) == "IndexError"
+    assert str(g[f"face_{tag}_err_Query"]) == "ValueError"
+    with pytest.raises(IndexError):
+        o.rQuery(g[f"face_{tag}_qerr"].copy())
+    with pytest.raises(ValueError):
+        o.Query(g[f"face_{tag}_qerr"].copy())
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_float32_field_golden(golden, prec):
+    tricubic, _ = _mods()
+    g = golden
+    o = tricubic(g["f32_field"], "quiet", precision=prec)
+    assert o.hx.dtype == np.float32
+    assert np.array_equal(np.array([o.hx, o.hy, o.hz], dtype=np.float64), g["f32_p_h"])
+    q = g["f32_q"].copy()
+    res = o.Query(q)
+    _check(res, g, "f32_", q, o.queryInds, TOL[prec])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("strategy", ["otf", "table"])
+def test_quadcubic_golden(golden, prec, strategy):
+    _, quadcubic = _mods()
+    g = golden
+    o = quadcubic(g["q4_field"], "quiet", precision=prec, strategy=strategy)
+    assert np.array_equal(o.inputfield, g["q4_inputfield"])
+    assert np.array_equal(o.basePointInds, g["q4_p_basePointInds"])
+    q = g["q4_q"].copy()
+    res = o.Query(q)
+    _check(res, g, "q4_", q, o.queryInds, TOL[prec])
+    o2 = quadcubic(g["q4v_field"], "quiet", mode="both", precision=prec, strategy=strategy)
+    q = g["q4v_q"].copy()
+    _check(o2.Query(q), g, "q4v_", q, o2.queryInds, TOL[prec])
+    o3 = quadcubic(g["q4v_field"], "quiet", mode="vector", precision=prec, strategy=strategy)
+    q = g["q4v_q"].copy()
+    _check(o3.Query(q), g, "q4vv_", q, o3.queryInds, TOL[prec])
+
+
+def test_quadcubic_alpha_and_kat(golden):
+    _, quadcubic = _mods()
+    g = golden
+    o = quadcubic(g["q4v_field"], "quiet", mode="both")
+    o.allCoeffs()
+    ref = g["q4v_alphan"]
+    mine = o.alphan
+    assert np.array_equal(np.isnan(mine), np.isnan(ref))
+    m = np.isfinite(ref)
+    assert np.abs(mine[m] - ref[m]).max() <= 1e-12 * np.abs(ref[m]).max()
+    ax = [np.arange(6) * 0.5] * 4
+    X, Y, Z, T = np.meshgrid(*ax, indexing="ij")
+    fk = np.stack([X.ravel(), Y.ravel(), Z.ravel(), T.ravel(), (X * Y * Z * T).ravel()], 1)
+    n, _ = quadcubic(fk, "quiet").Query(g["kat4_q"].copy())
+    assert np.abs(n - g["kat4_norms"]).max() <= 1e-12
+
+
+def test_quadcubic_single_points(golden):
+    _, quadcubic = _mods()
+    g = golden
+    o = quadcubic(g["q4_field"], "quiet")
+    for p, st, vals in zip(g["q4_sp_pts"], g["q4_sp_status"], g["q4_sp_vals"]):
+        if st == "ok":
+            nv, gv = o.Query(p.copy())
+            flat = np.concatenate([[nv], gv])
+            assert np.abs(flat - vals[:5]).max() <= 1e-12 * max(1, np.abs(vals[:5]).max())
+        else:
+            assert np.isnan(o.sQuery(p.copy()))
+
+
+def test_irregular_grid_rejected():
+    tricubic, _ = _mods()
+    from arbinterp_gb300 import synth
+    f = synth.gaussian_field3(n=(6, 6, 6), seed=1).numpy()
+    with pytest.raises(ValueError):
+        tricubic(f[:-1], "quiet")          # a missing point
+    f2 = f.copy()
+    f2[5, 0] += 1e-9                        # a coordinate off its axis
+    with pytest.raises(ValueError):
+        tricubic(f2, "quiet")
+    with pytest.raises(SystemExit):
+        tricubic(f[:, :5], "quiet")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_random_both_vs_oracle(prec):
+    """64^3 dipole field, 'both' mode, 2e5 queries against the CPU oracle."""
+    import torch
+    tricubic, _ = _mods()
+    from arbinterp_gb300 import synth
+    from oracle.arb_oracle import OracleTricubic
+    f = synth.dipole_field3(n=(40, 48, 44), seed=3).numpy()
+    ref = OracleTricubic(f, mode="both")
+    q = synth.uniform_queries(ref.lo, ref.hi, 200000, 2000, ref.h, seed=4).numpy()
+    want = ref.query(q.copy())
+    for strategy in ("otf", "table"):
+        o = tricubic(f, "quiet", mode="both", precision=prec, strategy=strategy)
+        qq = q.copy()
+        comps, norms, grads = o.Query(qq)
+        assert np.array_equal(o.queryInds, want["inds"])
+        for got, k in ((comps, "comps"), (norms, "norms"), (grads, "grads")):
+            assert np.array_equal(np.isnan(got), np.isnan(want[k]))
+            assert (normwise(got, want[k]) <= TOL[prec]).all(), (strategy, k, normwise(got, want[k]))
+        # device-tensor queries: outputs stay on the device, OOB rows NaN'd in place
+        qd = torch.from_numpy(q.copy()).cuda()
+        c2, n2, g2 = o.Query(qd)
+        assert np.array_equal(torch.isnan(qd).all(1).cpu().numpy(), np.isnan(qq).all(1))
+        assert np.array_equal(c2.cpu().numpy(), comps, equal_nan=True)
+
+
+def test_fd_planes_match_D_matrix():
+    """arb_fd_planes equals the reference's D-matrix stencils at cell corners."""
+    import torch
+    tricubic, _ = _mods()
+    from arbinterp_gb300 import synth, _lib
+    from oracle import arb_oracle as O
+    f = synth.gaussian_field3(n=(7, 8, 9), seed=2).numpy()
+    o = tricubic(f, "quiet")
+    npts = o._npts
+    planes = torch.empty(8 * npts, dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().arb_fd_planes(o._g, planes.data_ptr(), torch.cuda.current_stream().cuda_stream),
+               "arb_fd_planes")
+    P = planes.view(8, npts).cpu().numpy()
+    ref = O.OracleTricubic(f)
+    D = O.build_D3()
+    vals = ref.fields["n"]
+    for cell in (0, 5, ref.nc - 1):
+        block = vals[ref.basePointInds[cell] + ref.block_offsets]
+        b = D @ block                       # b[8r + k]: kind r at corner k
+        for k in range(8):
+            p = ref.basePointInds[cell] + (k & 1) + ref.nx * ((k >> 1) & 1) + ref.nx * ref.ny * (k >> 2)
+            assert np.allclose(P[:, p], b[k::8], rtol=0, atol=1e-13)
