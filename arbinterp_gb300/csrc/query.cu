@@ -15,242 +15,26 @@
 // index.  MIXED reads the (hi, lo) float32 split of the grid (or a float32
 // table) and evaluates in float32; the cell index and fractional offset are
 // still formed in float64 so indices and NaN masks are bit-exact.
-#include "arb_common.cuh"
+#include "eval.cuh"
 
 namespace arb {
 
-struct KParams {
-  double inv_h[4];
-  float inv_hf[4];
-};
-
-template <int DIM, int F>
-__device__ __forceinline__ void write_const(const arb_query_out &o, int64_t i, double v) {
-  if (F >= 3 && o.comps) {
-    o.comps[i * 3 + 0] = v;
-    o.comps[i * 3 + 1] = v;
-    o.comps[i * 3 + 2] = v;
-  }
-  if (F != 3) {
-    if (o.norms) o.norms[i] = v;
-    if (o.grads) {
-#pragma unroll
-      for (int a = 0; a < DIM; ++a) o.grads[i * DIM + a] = v;
-    }
-  }
-}
-
-template <int DIM, int F>
-__device__ __forceinline__ void write_vals(const arb_query_out &o, int64_t i, const double *val,
-                                           const double *grad) {
-  if (F >= 3 && o.comps) {
-    o.comps[i * 3 + 0] = val[0];
-    o.comps[i * 3 + 1] = val[1];
-    o.comps[i * 3 + 2] = val[2];
-  }
-  if (F != 3) {
-    if (o.norms) o.norms[i] = val[F - 1];
-    if (o.grads) {
-#pragma unroll
-      for (int a = 0; a < DIM; ++a) o.grads[i * DIM + a] = grad[a];
-    }
-  }
-}
-
-// Shared prologue: cell index, out-of-volume handling, sentinel semantics.
-// Returns true when the row still needs evaluating.
-template <int DIM, int F, bool EXACT>
-__device__ __forceinline__ bool query_prologue(const arb_grid &g, const KParams &kp, double *q,
-                                               int64_t i, int64_t qs, int wb,
-                                               const arb_query_out &o, int32_t *status,
-                                               double frac[DIM], int64_t &idx) {
-  double *qr = q + i * qs;
-  double qv[DIM];
-#pragma unroll
-  for (int a = 0; a < DIM; ++a) qv[a] = qr[a];
-  const CoordStep s = coord_step<DIM, EXACT>(qv, g, kp.inv_h, frac);
-  append_oob(o, i, s.oob);
-  if (s.oob && wb) {
-    for (int64_t c = 0; c < qs; ++c) qr[c] = qnan();
-  }
-  if (o.inds) o.inds[i] = s.idx;
-  idx = s.idx;
-  if (s.oob || s.nan) {
-    write_const<DIM, F>(o, i, qnan());
-    return false;
-  }
-  if (s.idx > g.nc) {
-    // the reference's alphamask lookup raises here (IndexError)
-    set_status(status, ARB_ERR_CELL_INDEX);
-    write_const<DIM, F>(o, i, qnan());
-    return false;
-  }
-  if (s.idx == g.nc) {
-    // in-volume query aliased onto the sentinel column (upper faces)
-    write_const<DIM, F>(o, i, g.sentinel_nan ? qnan() : 0.0);
-    return false;
-  }
-  return true;
-}
-
-// ---- row loaders ------------------------------------------------------------
-// 4 consecutive grid points x F fields starting at flat point p.
-template <int F>
-__device__ __forceinline__ void load_row64(const double *grid, int64_t p, double v[4][F]) {
-  const double *r = grid + p * F;
-  if (F == 4) {
-    const double2 *r2 = reinterpret_cast<const double2 *>(r);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const double2 a = __ldg(r2 + 2 * i), b = __ldg(r2 + 2 * i + 1);
-      v[i][0] = a.x;
-      v[i][1 % F] = a.y;
-      v[i][2 % F] = b.x;
-      v[i][3 % F] = b.y;
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int f = 0; f < F; ++f) v[i][f] = __ldg(r + i * F + f);
-  }
-}
-
-// Deltas against the reference point: (hi - rhi) + (lo - rlo) is accurate to
-// float32 rounding of the DIFFERENCE, so gradients keep full relative
-// precision even where |f| >> h |grad f|.
-template <int F>
-__device__ __forceinline__ void load_row32(const float *grid, int64_t p, const float *rhi,
-                                           const float *rlo, float v[4][F]) {
-  const float2 *r = reinterpret_cast<const float2 *>(grid) + p * F;
-  if (F == 4) {
-    const float4 *r4 = reinterpret_cast<const float4 *>(r);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const float4 a = __ldg(r4 + 2 * i), b = __ldg(r4 + 2 * i + 1);
-      v[i][0] = (a.x - rhi[0]) + (a.y - rlo[0]);
-      v[i][1 % F] = (a.z - rhi[1 % F]) + (a.w - rlo[1 % F]);
-      v[i][2 % F] = (b.x - rhi[2 % F]) + (b.y - rlo[2 % F]);
-      v[i][3 % F] = (b.z - rhi[3 % F]) + (b.w - rlo[3 % F]);
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int f = 0; f < F; ++f) {
-        const float2 a = __ldg(r + i * F + f);
-        v[i][f] = (a.x - rhi[f]) + (a.y - rlo[f]);
-      }
-  }
-}
-
-template <int F, bool MIXED, typename T>
-__device__ __forceinline__ void load_row(const arb_grid &g, int64_t p, const float *rhi,
-                                         const float *rlo, T v[4][F]) {
-  if constexpr (MIXED)
-    load_row32<F>(g.grid32, p, rhi, rlo, v);
-  else
-    load_row64<F>(g.grid64, p, v);
-}
-
-// ---- 3D on-the-fly ---------------------------------------------------------
 template <int F, bool MIXED>
 __global__ void __launch_bounds__(256) otf3_kernel(arb_grid g, KParams kp, double *q, int64_t nq,
                                                    int64_t qs, int wb, arb_query_out o,
                                                    int32_t *status) {
   using T = typename std::conditional<MIXED, float, double>::type;
-  constexpr bool GRAD = (F != 3);
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
   double frac[3];
   int64_t idx;
   if (!query_prologue<3, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac, idx)) return;
-  int64_t c[3];
-  cell_coords<3>(idx, g, c);
-  const int64_t nx = g.n[0], ny = g.n[1];
-  T wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
-  cr_weights<T>((T)frac[0], wx);
-  cr_weights<T>((T)frac[1], wy);
-  cr_weights<T>((T)frac[2], wz);
-  if (GRAD) {
-    cr_dweights<T>((T)frac[0], dx);
-    cr_dweights<T>((T)frac[1], dy);
-    cr_dweights<T>((T)frac[2], dz);
-  }
-  float rhi[F], rlo[F];
-  if constexpr (MIXED) {
-    // reference point: the cell's own corner, block offset (1, 1, 1)
-    const int64_t pr = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
-    const float2 *r = reinterpret_cast<const float2 *>(g.grid32) + pr * F;
-#pragma unroll
-    for (int f = 0; f < F; ++f) {
-      const float2 a = __ldg(r + f);
-      rhi[f] = a.x;
-      rlo[f] = a.y;
-    }
-  }
-  T acc[F], gx = 0, gy = 0, gz = 0;
-#pragma unroll
-  for (int f = 0; f < F; ++f) acc[f] = 0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    T ay[F], ayx = 0, ayy = 0;
-#pragma unroll
-    for (int f = 0; f < F; ++f) ay[f] = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      T v[4][F];
-      load_row<F, MIXED, T>(g, ((c[2] + k) * ny + (c[1] + j)) * nx + c[0], rhi, rlo, v);
-      T ax[F];
-#pragma unroll
-      for (int f = 0; f < F; ++f)
-        ax[f] = wx[0] * v[0][f] + wx[1] * v[1][f] + wx[2] * v[2][f] + wx[3] * v[3][f];
-#pragma unroll
-      for (int f = 0; f < F; ++f) ay[f] += wy[j] * ax[f];
-      if (GRAD) {
-        const T axd = dx[0] * v[0][F - 1] + dx[1] * v[1][F - 1] + dx[2] * v[2][F - 1] +
-                      dx[3] * v[3][F - 1];
-        ayx += wy[j] * axd;
-        ayy += dy[j] * ax[F - 1];
-      }
-    }
-#pragma unroll
-    for (int f = 0; f < F; ++f) acc[f] += wz[k] * ay[f];
-    if (GRAD) {
-      gx += wz[k] * ayx;
-      gy += wz[k] * ayy;
-      gz += dz[k] * ay[F - 1];
-    }
-  }
+  const T fr[3] = {(T)frac[0], (T)frac[1], (T)frac[2]};
   double val[F], grad[3];
-#pragma unroll
-  for (int f = 0; f < F; ++f) {
-    if constexpr (MIXED)
-      val[f] = (double)(rhi[f] + (rlo[f] + acc[f]));
-    else
-      val[f] = (double)acc[f];
-  }
-  if (GRAD) {
-    if constexpr (MIXED) {
-      grad[0] = (double)(gx * kp.inv_hf[0]);
-      grad[1] = (double)(gy * kp.inv_hf[1]);
-      grad[2] = (double)(gz * kp.inv_hf[2]);
-    } else {
-      grad[0] = (double)gx * kp.inv_h[0];
-      grad[1] = (double)gy * kp.inv_h[1];
-      grad[2] = (double)gz * kp.inv_h[2];
-    }
-  }
+  eval_otf3<F, MIXED>(g, kp, idx, fr, val, grad);
   write_vals<3, F>(o, i, val, grad);
 }
 
-// ---- 4D on-the-fly ---------------------------------------------------------
-// value = sum_o W_o(x) f_o  +  sum_c (H_{c+1}(x) - H_c(x)) S_c
-// with W the 4-fold Catmull-Rom tensor, S_c the (1/16) mixed fourth
-// difference centred on cell corner c, H_c(x) the tensor product of cubic
-// slope-Hermite bases at corner c, H_16 = 0.  The second term is the
-// reference's A minus kron(A1,A1,A1,A1) (D row 240 zero, rows 241..255
-// shifted by one corner).
 template <int F, bool MIXED>
 __global__ void __launch_bounds__(128) otf4_kernel(arb_grid g, KParams kp, double *q, int64_t nq,
                                                    int64_t qs, int wb, arb_query_out o,
@@ -261,160 +45,10 @@ __global__ void __launch_bounds__(128) otf4_kernel(arb_grid g, KParams kp, doubl
   double frac[4];
   int64_t idx;
   if (!query_prologue<4, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac, idx)) return;
-  int64_t c[4];
-  cell_coords<4>(idx, g, c);
-  const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
-  T w[4][4], dw[4][4], hb[4][2], dhb[4][2];
-#pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    cr_weights<T>((T)frac[a], w[a]);
-    cr_dweights<T>((T)frac[a], dw[a]);
-    hermite_slope<T>((T)frac[a], hb[a], dhb[a]);
-  }
-  const float2 *g32 = reinterpret_cast<const float2 *>(g.grid32);
-  const int64_t pref = (((c[3] + 1) * nz + (c[2] + 1)) * ny + (c[1] + 1)) * nx + (c[0] + 1);
+  const T fr[4] = {(T)frac[0], (T)frac[1], (T)frac[2], (T)frac[3]};
   double val[F], grad[4] = {0, 0, 0, 0};
-#pragma unroll 1
-  for (int f = 0; f < F; ++f) {
-    const bool gradf = (F != 3) && (f == F - 1);
-    float rhi = 0.f, rlo = 0.f;
-    if constexpr (MIXED) {
-      const float2 a = __ldg(g32 + pref * F + f);
-      rhi = a.x;
-      rlo = a.y;
-    }
-    T V = 0, Vg[4] = {0, 0, 0, 0};
-    T S[16];
-#pragma unroll
-    for (int m = 0; m < 16; ++m) S[m] = 0;
-#pragma unroll
-    for (int l = 0; l < 4; ++l) {
-      T Az = 0, Azg[4] = {0, 0, 0, 0};
-      T E2[8];
-#pragma unroll
-      for (int m = 0; m < 8; ++m) E2[m] = 0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        T Ay = 0, Ayx = 0, Ayy = 0;
-        T E1[4] = {0, 0, 0, 0};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int64_t p = (((c[3] + l) * nz + (c[2] + k)) * ny + (c[1] + j)) * nx + c[0];
-          T r[4];
-#pragma unroll
-          for (int ii = 0; ii < 4; ++ii) {
-            if constexpr (MIXED) {
-              const float2 a = __ldg(g32 + (p + ii) * F + f);
-              r[ii] = (a.x - rhi) + (a.y - rlo);
-            } else {
-              r[ii] = __ldg(g.grid64 + (p + ii) * F + f);
-            }
-          }
-          const T ax = w[0][0] * r[0] + w[0][1] * r[1] + w[0][2] * r[2] + w[0][3] * r[3];
-          Ay += w[1][j] * ax;
-          if (gradf) {
-            const T axd = dw[0][0] * r[0] + dw[0][1] * r[1] + dw[0][2] * r[2] + dw[0][3] * r[3];
-            Ayx += w[1][j] * axd;
-            Ayy += dw[1][j] * ax;
-          }
-          const T sj = (j >= 2) ? T(0.5) : T(-0.5);
-          E1[0 + 2 * (j & 1)] += sj * (T(0.5) * (r[2] - r[0]));
-          E1[1 + 2 * (j & 1)] += sj * (T(0.5) * (r[3] - r[1]));
-        }
-        Az += w[2][k] * Ay;
-        if (gradf) {
-          Azg[0] += w[2][k] * Ayx;
-          Azg[1] += w[2][k] * Ayy;
-          Azg[2] += dw[2][k] * Ay;
-        }
-        const T sk = (k >= 2) ? T(0.5) : T(-0.5);
-#pragma unroll
-        for (int m = 0; m < 4; ++m) E2[m + 4 * (k & 1)] += sk * E1[m];
-      }
-      V += w[3][l] * Az;
-      if (gradf) {
-        Vg[0] += w[3][l] * Azg[0];
-        Vg[1] += w[3][l] * Azg[1];
-        Vg[2] += w[3][l] * Azg[2];
-        Vg[3] += dw[3][l] * Az;
-      }
-      const T sl = (l >= 2) ? T(0.5) : T(-0.5);
-#pragma unroll
-      for (int m = 0; m < 8; ++m) S[m + 8 * (l & 1)] += sl * E2[m];
-    }
-    // T_c = S_{c-1} - S_c, then contract with the slope-Hermite tensor
-    T Tc[16];
-    Tc[0] = -S[0];
-#pragma unroll
-    for (int m = 1; m < 16; ++m) Tc[m] = S[m - 1] - S[m];
-    T Cx[8], Cdx[8];
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      Cx[m] = hb[0][0] * Tc[2 * m] + hb[0][1] * Tc[2 * m + 1];
-      Cdx[m] = dhb[0][0] * Tc[2 * m] + dhb[0][1] * Tc[2 * m + 1];
-    }
-    T Cy[4], Cyx[4], Cyy[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      Cy[m] = hb[1][0] * Cx[2 * m] + hb[1][1] * Cx[2 * m + 1];
-      Cyx[m] = hb[1][0] * Cdx[2 * m] + hb[1][1] * Cdx[2 * m + 1];
-      Cyy[m] = dhb[1][0] * Cx[2 * m] + dhb[1][1] * Cx[2 * m + 1];
-    }
-    T Cz[2], Czx[2], Czy[2], Czz[2];
-#pragma unroll
-    for (int m = 0; m < 2; ++m) {
-      Cz[m] = hb[2][0] * Cy[2 * m] + hb[2][1] * Cy[2 * m + 1];
-      Czx[m] = hb[2][0] * Cyx[2 * m] + hb[2][1] * Cyx[2 * m + 1];
-      Czy[m] = hb[2][0] * Cyy[2 * m] + hb[2][1] * Cyy[2 * m + 1];
-      Czz[m] = dhb[2][0] * Cy[2 * m] + dhb[2][1] * Cy[2 * m + 1];
-    }
-    const T C = hb[3][0] * Cz[0] + hb[3][1] * Cz[1];
-    const T total = V + C;
-    if constexpr (MIXED)
-      val[f] = (double)(rhi + (rlo + total));
-    else
-      val[f] = (double)total;
-    if (gradf) {
-      const T G[4] = {Vg[0] + (hb[3][0] * Czx[0] + hb[3][1] * Czx[1]),
-                      Vg[1] + (hb[3][0] * Czy[0] + hb[3][1] * Czy[1]),
-                      Vg[2] + (hb[3][0] * Czz[0] + hb[3][1] * Czz[1]),
-                      Vg[3] + (dhb[3][0] * Cz[0] + dhb[3][1] * Cz[1])};
-#pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        if constexpr (MIXED)
-          grad[a] = (double)(G[a] * kp.inv_hf[a]);
-        else
-          grad[a] = (double)G[a] * kp.inv_h[a];
-      }
-    }
-  }
+  eval_otf4<F, MIXED>(g, kp, idx, fr, val, grad);
   write_vals<4, F>(o, i, val, grad);
-}
-
-// ---- table evaluation ------------------------------------------------------
-// Horner along x for one 4-coefficient row: value and d/dx.
-template <typename T>
-__device__ __forceinline__ void horner_x(const T a[4], T x, T &v, T &d) {
-  v = ((a[3] * x + a[2]) * x + a[1]) * x + a[0];
-  d = (T(3) * a[3] * x + T(2) * a[2]) * x + a[1];
-}
-
-template <typename T>
-__device__ __forceinline__ void load4(const T *p, T a[4]) {
-  if constexpr (sizeof(T) == 8) {
-    const double2 u = __ldg(reinterpret_cast<const double2 *>(p));
-    const double2 w = __ldg(reinterpret_cast<const double2 *>(p) + 1);
-    a[0] = u.x;
-    a[1] = u.y;
-    a[2] = w.x;
-    a[3] = w.y;
-  } else {
-    const float4 u = __ldg(reinterpret_cast<const float4 *>(p));
-    a[0] = u.x;
-    a[1] = u.y;
-    a[2] = u.z;
-    a[3] = u.w;
-  }
 }
 
 template <int DIM, int F, bool MIXED>
@@ -422,7 +56,6 @@ __global__ void __launch_bounds__(256) tab_kernel(arb_grid g, KParams kp, double
                                                   int64_t qs, int wb, arb_query_out o,
                                                   int32_t *status) {
   using T = typename std::conditional<MIXED, float, double>::type;
-  constexpr int M = DIM == 3 ? 64 : 256;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
   double frac[DIM];
@@ -431,84 +64,9 @@ __global__ void __launch_bounds__(256) tab_kernel(arb_grid g, KParams kp, double
   T x[DIM];
 #pragma unroll
   for (int a = 0; a < DIM; ++a) x[a] = (T)frac[a];
-  const T *tab = reinterpret_cast<const T *>(g.table) + idx * (int64_t)F * M;
   double val[F], grad[DIM];
-#pragma unroll 1
-  for (int f = 0; f < F; ++f) {
-    const bool gradf = (F != 3) && (f == F - 1);
-    const T *a = tab + f * M;
-    // nested Horner: rows (ey, ez[, et]) of 4 x-coefficients
-    T V = 0, G[DIM];
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) G[d] = 0;
-    const int NT = DIM == 4 ? 4 : 1;
-#pragma unroll 1
-    for (int et = NT - 1; et >= 0; --et) {
-      T Vz = 0, Gz[3] = {0, 0, 0};
-#pragma unroll
-      for (int ez = 3; ez >= 0; --ez) {
-        T Vy = 0, Gyx = 0, Gyy = 0;
-#pragma unroll
-        for (int ey = 3; ey >= 0; --ey) {
-          T r[4];
-          load4<T>(a + ((et * 4 + ez) * 4 + ey) * 4, r);
-          T vx, dxv;
-          horner_x<T>(r, x[0], vx, dxv);
-          // Horner in y: derivative first (uses the old Vy)
-          Gyy = Gyy * x[1] + Vy;
-          Vy = Vy * x[1] + vx;
-          Gyx = Gyx * x[1] + dxv;
-        }
-        Gz[2] = Gz[2] * x[2] + Vz;
-        Vz = Vz * x[2] + Vy;
-        Gz[0] = Gz[0] * x[2] + Gyx;
-        Gz[1] = Gz[1] * x[2] + Gyy;
-      }
-      if (DIM == 4) {
-        G[DIM - 1] = G[DIM - 1] * x[DIM - 1] + V;
-        V = V * x[DIM - 1] + Vz;
-        G[0] = G[0] * x[DIM - 1] + Gz[0];
-        G[1] = G[1] * x[DIM - 1] + Gz[1];
-        G[2] = G[2] * x[DIM - 1] + Gz[2];
-      } else {
-        V = Vz;
-        G[0] = Gz[0];
-        G[1] = Gz[1];
-        G[2] = Gz[2];
-      }
-    }
-    val[f] = (double)V;
-    if (gradf) {
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        if constexpr (MIXED)
-          grad[d] = (double)(G[d] * kp.inv_hf[d]);
-        else
-          grad[d] = (double)G[d] * kp.inv_h[d];
-      }
-    }
-  }
+  eval_tab<DIM, F, MIXED>(g, kp, idx, x, val, grad);
   write_vals<DIM, F>(o, i, val, grad);
-}
-
-static KParams make_kparams(const arb_grid *g) {
-  KParams kp;
-  for (int a = 0; a < 4; ++a) {
-    const double h = a < g->dim ? g->h[a] : 1.0;
-    kp.inv_h[a] = 1.0 / h;
-    kp.inv_hf[a] = (float)(1.0 / h);
-  }
-  return kp;
-}
-
-static int check_query_args(const arb_grid *g, const double *q, int64_t nq, int64_t qs,
-                            const arb_query_out *out) {
-  if (!g || !out || (nq > 0 && !q)) return ARB_ERR_INVALID;
-  if (g->dim != 3 && g->dim != 4) return ARB_ERR_INVALID;
-  if (qs < g->dim || nq < 0) return ARB_ERR_INVALID;
-  if (g->nfield != 1 && g->nfield != 3 && g->nfield != 4) return ARB_ERR_INVALID;
-  if (out->oob_rows && !out->oob_count) return ARB_ERR_INVALID;
-  return ARB_OK;
 }
 
 }  // namespace arb

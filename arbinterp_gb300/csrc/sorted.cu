@@ -1,0 +1,249 @@
+// Cell-grouped query evaluation.
+//
+// Random query order makes every query's 4^dim grid block (or coefficient
+// row) a cold gather from a field far larger than L2.  Here the queries are
+// first grouped by spatial bin (8^3 cells in 3D, 4^4 in 4D) with a counting
+// sort, then evaluated bin by bin, so neighbouring threads share grid data in
+// L1/L2 and each grid point is fetched from HBM about once.
+//
+//   locate   : float64 cell index + fractional offset (exactly the
+//              reference's iu = (q - IntMin)/h, floor, flat index), the
+//              out-of-volume bookkeeping of rQuery (NaN rows, queryInds), and
+//              bin id + rank within the bin (atomic histogram)
+//   scan     : exclusive prefix sum of the bin histogram
+//   scatter  : records (code, row, frac) into bin order
+//   evaluate : on-the-fly or table evaluation in bin order, outputs written
+//              to the query's original row
+// The float64 index step runs once per query; the evaluation pass does no
+// float64 arithmetic in mixed precision.
+#include "eval.cuh"
+
+namespace arb {
+
+struct SortedWork {
+  uint32_t *hist;    // nbins + 1 (exclusive offsets after the scan)
+  uint2 *binrank;    // nq
+  int64_t *code;     // nq: cell index, nc = sentinel, -1 = NaN row
+  void *frac;        // nq * DIM values of T
+  int64_t *s_code;   // nq, bin order
+  int64_t *s_row;    // nq
+  void *s_frac;      // nq * DIM
+};
+
+struct BinGeom {
+  int64_t nb[4];     // bins per axis
+  int64_t nbins;     // product (the special bin is index nbins)
+  int shift;         // log2 cells per bin edge
+};
+
+static inline BinGeom bin_geom(const arb_grid *g) {
+  BinGeom b;
+  b.shift = g->dim == 3 ? 3 : 2;
+  b.nbins = 1;
+  for (int a = 0; a < 4; ++a) {
+    if (a < g->dim) {
+      const int64_t cells = g->n[a] - 3;
+      b.nb[a] = (cells + (1 << b.shift) - 1) >> b.shift;
+    } else {
+      b.nb[a] = 1;
+    }
+    b.nbins *= b.nb[a];
+  }
+  return b;
+}
+
+static inline size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static size_t carve(SortedWork *w, void *base, const arb_grid *g, int precision, int64_t nq) {
+  const BinGeom bg = bin_geom(g);
+  const size_t tsz = precision == ARB_PREC_MIXED ? 4 : 8;
+  size_t off = 0;
+  char *p = (char *)base;
+  auto take = [&](size_t bytes) {
+    void *r = p ? (void *)(p + off) : nullptr;
+    off += align_up(bytes);
+    return r;
+  };
+  SortedWork t;
+  t.hist = (uint32_t *)take(sizeof(uint32_t) * (bg.nbins + 1));
+  t.binrank = (uint2 *)take(sizeof(uint2) * nq);
+  t.code = (int64_t *)take(sizeof(int64_t) * nq);
+  t.frac = take(tsz * g->dim * nq);
+  t.s_code = (int64_t *)take(sizeof(int64_t) * nq);
+  t.s_row = (int64_t *)take(sizeof(int64_t) * nq);
+  t.s_frac = take(tsz * g->dim * nq);
+  if (w) *w = t;
+  return off;
+}
+
+template <int DIM, bool EXACT, typename T>
+__global__ void __launch_bounds__(256) locate_kernel(arb_grid g, KParams kp, BinGeom bg, double *q,
+                                                     int64_t nq, int64_t qs, int wb, arb_query_out o,
+                                                     int32_t *status, SortedWork w) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  double *qr = q + i * qs;
+  double qv[DIM], frac[DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) qv[a] = qr[a];
+  const CoordStep s = coord_step<DIM, EXACT>(qv, g, kp.inv_h, frac);
+  append_oob(o, i, s.oob);
+  if (s.oob && wb)
+    for (int64_t c = 0; c < qs; ++c) qr[c] = qnan();
+  if (o.inds) o.inds[i] = s.idx;
+  int64_t code;
+  int64_t bin = bg.nbins;
+  if (s.oob || s.nan) {
+    code = -1;
+  } else if (s.idx > g.nc) {
+    set_status(status, ARB_ERR_CELL_INDEX);
+    code = -1;
+  } else if (s.idx == g.nc) {
+    code = g.nc;
+  } else {
+    code = s.idx;
+    int64_t c[DIM];
+    cell_coords<DIM>(s.idx, g, c);
+    bin = c[DIM - 1] >> bg.shift;
+#pragma unroll
+    for (int a = DIM - 2; a >= 0; --a) bin = bin * bg.nb[a] + (c[a] >> bg.shift);
+  }
+  const uint32_t rank = atomicAdd(&w.hist[bin], 1u);
+  w.binrank[i] = make_uint2((uint32_t)bin, rank);
+  w.code[i] = code;
+  T *fr = reinterpret_cast<T *>(w.frac) + i * DIM;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) fr[a] = (T)frac[a];
+}
+
+// Exclusive scan of n counters in one block (n up to a few million).
+__global__ void __launch_bounds__(1024) scan_kernel(uint32_t *hist, int64_t n) {
+  __shared__ uint32_t part[1024];
+  const int64_t per = (n + blockDim.x - 1) / blockDim.x;
+  const int64_t b = threadIdx.x * per, e = min(b + per, n);
+  uint32_t sum = 0;
+  for (int64_t k = b; k < e; ++k) sum += hist[k];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const uint32_t v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - sum;
+  for (int64_t k = b; k < e; ++k) {
+    const uint32_t c = hist[k];
+    hist[k] = run;
+    run += c;
+  }
+}
+
+template <int DIM, typename T>
+__global__ void __launch_bounds__(256) scatter_kernel(int64_t nq, SortedWork w) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  const uint2 br = w.binrank[i];
+  const int64_t pos = (int64_t)w.hist[br.x] + br.y;
+  w.s_code[pos] = w.code[i];
+  w.s_row[pos] = i;
+  const T *src = reinterpret_cast<const T *>(w.frac) + i * DIM;
+  T *dst = reinterpret_cast<T *>(w.s_frac) + pos * DIM;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) dst[a] = src[a];
+}
+
+template <int DIM, int F, bool MIXED, bool TABLE>
+__global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_grid g, KParams kp,
+                                                                           int64_t nq, arb_query_out o,
+                                                                           SortedWork w) {
+  using T = typename std::conditional<MIXED, float, double>::type;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nq) return;
+  const int64_t code = w.s_code[t];
+  const int64_t i = w.s_row[t];
+  if (code < 0) {
+    write_const<DIM, F>(o, i, qnan());
+    return;
+  }
+  if (code == g.nc) {
+    write_const<DIM, F>(o, i, g.sentinel_nan ? qnan() : 0.0);
+    return;
+  }
+  T fr[DIM];
+  const T *src = reinterpret_cast<const T *>(w.s_frac) + t * DIM;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) fr[a] = src[a];
+  double val[F], grad[DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) grad[a] = 0.0;
+  if constexpr (TABLE) {
+    eval_tab<DIM, F, MIXED>(g, kp, code, fr, val, grad);
+  } else if constexpr (DIM == 3) {
+    eval_otf3<F, MIXED>(g, kp, code, fr, val, grad);
+  } else {
+    eval_otf4<F, MIXED>(g, kp, code, fr, val, grad);
+  }
+  write_vals<DIM, F>(o, i, val, grad);
+}
+
+template <int DIM, bool MIXED>
+static void launch_sorted(const arb_grid *g, const KParams &kp, const BinGeom &bg, double *q, int64_t nq,
+                          int64_t qs, int wb, const arb_query_out *out, int32_t *status,
+                          const SortedWork &w, bool table, cudaStream_t s) {
+  using T = typename std::conditional<MIXED, float, double>::type;
+  const int TB = 256;
+  const unsigned B = (unsigned)((nq + TB - 1) / TB);
+  locate_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, wb, *out, status, w);
+  scan_kernel<<<1, 1024, 0, s>>>(w.hist, bg.nbins + 1);
+  scatter_kernel<DIM, T><<<B, TB, 0, s>>>(nq, w);
+  const int TE = DIM == 3 ? 256 : 128;
+  const unsigned BE = (unsigned)((nq + TE - 1) / TE);
+#define ES(FF, TAB) eval_sorted_kernel<DIM, FF, MIXED, TAB><<<BE, TE, 0, s>>>(*g, kp, nq, *out, w)
+  if (table) {
+    switch (g->nfield) { case 1: ES(1, true); break; case 3: ES(3, true); break; default: ES(4, true); break; }
+  } else {
+    switch (g->nfield) { case 1: ES(1, false); break; case 3: ES(3, false); break; default: ES(4, false); break; }
+  }
+#undef ES
+}
+
+}  // namespace arb
+
+using namespace arb;
+
+extern "C" size_t arb_query_sorted_work_bytes(const arb_grid *g, int32_t precision, int64_t nq) {
+  if (!g || nq < 0 || (g->dim != 3 && g->dim != 4)) return 0;
+  return carve(nullptr, nullptr, g, precision, nq);
+}
+
+extern "C" int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32_t use_table,
+                                     double *q, int64_t nq, int64_t q_stride, int32_t q_writeback,
+                                     const arb_query_out *out, void *work, size_t work_bytes,
+                                     int32_t *status, arb_stream_t stream) {
+  int rc = check_query_args(g, q, nq, q_stride, out);
+  if (rc) return rc;
+  if (nq == 0) return ARB_OK;
+  if (!work || !status) return ARB_ERR_INVALID;
+  if (nq >= (int64_t)1 << 32) return ARB_ERR_UNSUPPORTED;
+  const bool mixed = precision == ARB_PREC_MIXED;
+  if (use_table) {
+    if (!g->table || g->table_prec != precision) return ARB_ERR_INVALID;
+  } else if (mixed ? !g->grid32 : !g->grid64) {
+    return ARB_ERR_INVALID;
+  }
+  SortedWork w;
+  if (carve(&w, work, g, precision, nq) > work_bytes) return ARB_ERR_INVALID;
+  const BinGeom bg = bin_geom(g);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nbins + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
+  const KParams kp = make_kparams(g);
+  if (g->dim == 3) {
+    if (mixed) launch_sorted<3, true>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
+    else launch_sorted<3, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
+  } else {
+    if (mixed) launch_sorted<4, true>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
+    else launch_sorted<4, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
+  }
+  return launch_status();
+}

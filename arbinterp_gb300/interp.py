@@ -16,6 +16,9 @@ Extra keyword arguments (reference-compatible defaults):
   device     CUDA device (default: the current one)
   check      True (default): synchronise after each query to raise the
              reference's errors; False: fully asynchronous device queries
+  sort_threshold
+             row count from which queries are grouped by spatial bin before
+             evaluation (default 32768)
 
 Inputs may be NumPy arrays (outputs are NumPy, as in the reference) or torch
 CUDA tensors (outputs stay on the device).  Differences from the reference on
@@ -73,6 +76,8 @@ class _Interpolant:
         if self.strategy not in ("auto", "otf", "table"):
             raise ValueError("strategy must be 'auto', 'otf' or 'table'")
         self.check = bool(kwargs.get("check", True))
+        self.sort_threshold = int(kwargs.get("sort_threshold", 1 << 15))
+        self._ws = None
         ncol = int(field.shape[1])
         # mode dispatch (ARB:24-104, 641-723)
         extra_col = False
@@ -263,11 +268,19 @@ class _Interpolant:
         cnt = torch.zeros(1, dtype=torch.int64, device=dev) if want_oob else None
         out = ArbQueryOut(_ptr(comps), _ptr(norms), _ptr(grads), _ptr(inds), _ptr(oob), _ptr(cnt))
         s = _stream()
-        if self._use_table():
+        table = self._use_table()
+        prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_MIXED
+        if n >= self.sort_threshold:
+            # group queries by spatial bin first (cell-coherent gathers)
+            need = int(L.arb_query_sorted_work_bytes(self._g, prec, n))
+            if self._ws is None or self._ws.numel() < need:
+                self._ws = torch.empty(need, dtype=torch.uint8, device=dev)
+            rc = L.arb_query_eval_sorted(self._g, prec, int(table), qd.data_ptr(), n, qs, int(writeback),
+                                         out, self._ws.data_ptr(), need, self._status.data_ptr(), s)
+        elif table:
             rc = L.arb_query_eval(self._g, qd.data_ptr(), n, qs, int(writeback), out,
                                   self._status.data_ptr(), s)
         else:
-            prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_MIXED
             rc = L.arb_query_eval_otf(self._g, prec, qd.data_ptr(), n, qs, int(writeback), out,
                                       self._status.data_ptr(), s)
         check(rc, "query evaluation")

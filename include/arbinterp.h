@@ -147,6 +147,21 @@ int arb_query_eval_otf(const arb_grid *g, int32_t precision, double *q, int64_t 
                        int64_t q_stride, int32_t q_writeback, const arb_query_out *out,
                        int32_t *status, arb_stream_t stream);
 
+/* ---- cell-grouped evaluation: the same contract as arb_query_eval_otf
+ *      (use_table == 0) or arb_query_eval (use_table != 0, table precision
+ *      must equal `precision`), but queries are first grouped by spatial bin
+ *      with a counting sort so grid blocks / coefficient rows are fetched
+ *      from HBM about once.  Replaces the same reference methods
+ *      (rQuery1/2/3, src/ARBInterp/ARBInterp.py:344-521, 1064-1258).
+ *      work: caller-owned scratch of arb_query_sorted_work_bytes() bytes.
+ *      nq < 2^32. ----------------------------------------------------------- */
+size_t arb_query_sorted_work_bytes(const arb_grid *g, int32_t precision, int64_t nq);
+
+int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32_t use_table, double *q,
+                          int64_t nq, int64_t q_stride, int32_t q_writeback,
+                          const arb_query_out *out, void *work, size_t work_bytes,
+                          int32_t *status, arb_stream_t stream);
+
 /* Reads (and clears) the device status word after the stream's work is
  * done; returns ARB_OK, an arb_status bit set, or ARB_ERR_CUDA. */
 int arb_status_fetch(int32_t *status, arb_stream_t stream);

@@ -110,6 +110,9 @@ def main(ref_path):
     q0 = synth.uniform_queries([o0.xIntMin, o0.yIntMin, o0.zIntMin], [o0.xIntMax, o0.yIntMax, o0.zIntMax],
                                9900, 100, [o0.hx, o0.hy, o0.hz], seed=5).numpy()
     out["c0_U"] = f0[:, 3]
+    # rows are meshgrid(indexing='ij') order; the axes rebuild them exactly
+    for a in range(3):
+        out[f"c0_ax{a}"] = np.unique(f0[:, a])
     out["c0_q"] = q0
     pack("c0_", run_range(o0, q0), out)
     pack("c0_p_", params3(o0), out)
