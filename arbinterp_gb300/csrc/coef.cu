@@ -218,9 +218,16 @@ static int coef_solve_f32_simt(const arb_grid *g, int64_t cell0, int64_t ncells,
   return launch_status();
 }
 
+namespace arb {
+int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *table, int32_t *status,
+                   cudaStream_t s);
+}
+
+// Mixed precision: 3D uses the split-BF16 tcgen05 GEMM; 4D (A not exact in
+// BF16) the float64 separable solve rounded to float32.
 static int coef_solve_mixed(const arb_grid *g, int64_t cell0, int64_t ncells, float *table,
-                                    int32_t *status, cudaStream_t s) {
-  (void)status;
+                            int32_t *status, cudaStream_t s) {
+  if (g->dim == 3 && g->grid32) return arb::coef3_solve_tc(g, cell0, ncells, table, status, s);
   return coef_solve_f32_simt(g, cell0, ncells, table, s);
 }
 

@@ -6,7 +6,8 @@
 // For a full tensor grid the position of a row in the reference's
 // lexicographic sort is ix + nx*(iy + ny*(iz + nz*it)) with i_a the rank of
 // the row's a-coordinate among that axis' samples, so the sort becomes an
-// O(N log n) scatter with no global sort.  Rows that are not a full tensor
+// index pass (binary search per axis, inverse permutation) plus a gather
+// pass with coalesced writes, with no global sort.  Rows that are not a full tensor
 // grid (missing or duplicate points, a coordinate not on its axis) set
 // ARB_ERR_IRREGULAR_GRID instead of silently producing garbage.
 #include "arb_common.cuh"
@@ -128,32 +129,52 @@ __global__ void axes_sort_kernel(const double *raw_axes, const AxesWork *w, int 
   }
 }
 
-__device__ __forceinline__ int64_t find_exact(const double *ax, int64_t n, double v) {
+// Binary search of an ordered key among n sorted axis keys; -1 if absent.
+__device__ __forceinline__ int64_t find_key(const unsigned long long *keys, int64_t n,
+                                            unsigned long long k) {
   int64_t lo = 0, hi = n - 1;
   while (lo < hi) {
     const int64_t mid = (lo + hi) >> 1;
-    if (ax[mid] < v)
+    if (keys[mid] < k)
       lo = mid + 1;
     else
       hi = mid;
   }
-  return ax[lo] == v ? lo : -1;
+  return keys[lo] == k ? lo : -1;
 }
 
-template <typename TF, int KIND>
-__global__ void scatter_kernel(const TF *field, int64_t npts, int ncol, int dim, const double *axes,
-                               int64_t cap, int64_t n0, int64_t n1, int64_t n2, int64_t n3,
-                               double *grid64, float *grid32, double *raw_out, uint32_t *claim,
-                               int32_t *status) {
+// Pass 1 (row order): grid slot of every row from exact axis-key lookups
+// (integer compares on order-preserving keys; no float64 pipe work), and the
+// inverse permutation inv[slot] = row.  inv is 4 bytes per point and stays
+// L2-resident while rows land in scattered slots; a second claim of a slot
+// is a duplicate point.
+template <typename TF>
+__global__ void __launch_bounds__(256) ingest_index_kernel(const TF *field, int64_t npts, int ncol,
+                                                           int dim, const double *axes, int64_t cap,
+                                                           int64_t n0, int64_t n1, int64_t n2,
+                                                           int64_t n3, uint32_t *inv,
+                                                           int32_t *status) {
+  extern __shared__ unsigned long long skeys[];
   const int64_t nn[4] = {n0, n1, n2, n3};
-  constexpr int F = (KIND == ARB_KIND_VECTOR) ? 3 : (KIND == ARB_KIND_BOTH ? 4 : 1);
+  int64_t off[4];
+  int64_t tot = 0;
+  for (int a = 0; a < dim; ++a) {
+    off[a] = tot;
+    tot += nn[a];
+  }
+  for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) {
+    int a = 0;
+    while (a + 1 < dim && e >= off[a + 1]) ++a;
+    skeys[e] = ord_key(axes[a * cap + (e - off[a])]);
+  }
+  __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
        i += (int64_t)gridDim.x * blockDim.x) {
     const TF *row = field + i * ncol;
     int64_t dest = 0;
     bool ok = true;
     for (int a = dim - 1; a >= 0; --a) {
-      const int64_t r = find_exact(axes + a * cap, nn[a], (double)row[a]);
+      const int64_t r = find_key(skeys + off[a], nn[a], ord_key((double)row[a]));
       ok &= (r >= 0);
       dest = dest * nn[a] + (r < 0 ? 0 : r);
     }
@@ -161,10 +182,26 @@ __global__ void scatter_kernel(const TF *field, int64_t npts, int ncol, int dim,
       set_status(status, ARB_ERR_IRREGULAR_GRID);
       continue;
     }
-    if (atomicAdd(&claim[dest], 1u) != 0u) {
+    if (atomicExch(&inv[dest], (uint32_t)i) != 0xffffffffu) set_status(status, ARB_ERR_IRREGULAR_GRID);
+  }
+}
+
+// Pass 2 (grid order): each slot reads its row and writes the per-mode
+// interpolated fields with coalesced stores.
+template <typename TF, int KIND>
+__global__ void __launch_bounds__(256) ingest_gather_kernel(const TF *field, int64_t npts, int ncol,
+                                                            int dim, const uint32_t *inv,
+                                                            double *grid64, float *grid32,
+                                                            double *raw_out, int32_t *status) {
+  constexpr int F = (KIND == ARB_KIND_VECTOR) ? 3 : (KIND == ARB_KIND_BOTH ? 4 : 1);
+  for (int64_t dest = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; dest < npts;
+       dest += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t src = inv[dest];
+    if (src == 0xffffffffu) {
       set_status(status, ARB_ERR_IRREGULAR_GRID);
       continue;
     }
+    const TF *row = field + (int64_t)src * ncol;
     double out[4];
     if (KIND == ARB_KIND_SCALAR) {
       out[0] = (double)row[dim];
@@ -174,8 +211,8 @@ __global__ void scatter_kernel(const TF *field, int64_t npts, int ncol, int dim,
       out[1] = (double)by;
       out[2] = (double)bz;
       if (KIND == ARB_KIND_NORM || KIND == ARB_KIND_BOTH) {
-        // ||B|| at the grid point, evaluated in the field's own precision
-        // as NumPy's norm does: sqrt((bx*bx + by*by) + bz*bz).
+        // ||B|| at the grid point in the field's own precision, as NumPy's
+        // norm evaluates it: sqrt((bx*bx + by*by) + bz*bz).
         double nrm;
         if (sizeof(TF) == 8) {
           nrm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn((double)bx, (double)bx),
@@ -186,8 +223,10 @@ __global__ void scatter_kernel(const TF *field, int64_t npts, int ncol, int dim,
                                                        __fmul_rn((float)by, (float)by)),
                                              __fmul_rn((float)bz, (float)bz)));
         }
-        if (KIND == ARB_KIND_NORM) out[0] = nrm;
-        else out[3] = nrm;
+        if (KIND == ARB_KIND_NORM)
+          out[0] = nrm;
+        else
+          out[3] = nrm;
       }
       if (raw_out) {
         raw_out[dest * 3 + 0] = (double)bx;
@@ -195,14 +234,27 @@ __global__ void scatter_kernel(const TF *field, int64_t npts, int ncol, int dim,
         raw_out[dest * 3 + 2] = (double)bz;
       }
     }
+    if (F == 4) {
+      reinterpret_cast<double2 *>(grid64)[dest * 2] = make_double2(out[0], out[1 % F]);
+      reinterpret_cast<double2 *>(grid64)[dest * 2 + 1] = make_double2(out[2 % F], out[3 % F]);
+    } else {
 #pragma unroll
-    for (int f = 0; f < F; ++f) grid64[dest * F + f] = out[f];
+      for (int f = 0; f < F; ++f) grid64[dest * F + f] = out[f];
+    }
     if (grid32) {
+      float hi[4], lo[4];
 #pragma unroll
       for (int f = 0; f < F; ++f) {
-        const float hi = __double2float_rn(out[f]);
-        const float lo = __double2float_rn(out[f] - (double)hi);
-        reinterpret_cast<float2 *>(grid32)[dest * F + f] = make_float2(hi, lo);
+        hi[f] = __double2float_rn(out[f]);
+        lo[f] = __double2float_rn(out[f] - (double)hi[f]);
+      }
+      if (F == 4) {
+        reinterpret_cast<float4 *>(grid32)[dest * 2] = make_float4(hi[0], lo[0], hi[1 % F], lo[1 % F]);
+        reinterpret_cast<float4 *>(grid32)[dest * 2 + 1] = make_float4(hi[2 % F], lo[2 % F], hi[3 % F], lo[3 % F]);
+      } else {
+#pragma unroll
+        for (int f = 0; f < F; ++f)
+          reinterpret_cast<float2 *>(grid32)[dest * F + f] = make_float2(hi[f], lo[f]);
       }
     }
     if (KIND == ARB_KIND_SCALAR && raw_out) raw_out[dest] = out[0];
@@ -271,28 +323,43 @@ extern "C" int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64
   const int nval = ncol - dim;
   if (kind == ARB_KIND_SCALAR ? nval != 1 : nval != 3) return ARB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
-  if (cudaMemsetAsync(claim, 0, sizeof(uint32_t) * npts, s) != cudaSuccess) return ARB_ERR_CUDA;
+  if (npts >= (int64_t)0xffffffffLL) return ARB_ERR_UNSUPPORTED;
+  if (cudaMemsetAsync(claim, 0xff, sizeof(uint32_t) * npts, s) != cudaSuccess) return ARB_ERR_CUDA;
   const int T = 256;
   const int B = grid_blocks(npts, T);
   const int64_t n3 = dim == 4 ? n[3] : 1;
-#define ARB_SCATTER(TF, K)                                                                       \
-  scatter_kernel<TF, K><<<B, T, 0, s>>>((const TF *)field, npts, ncol, dim, axes, axis_cap, n[0], \
-                                        n[1], n[2], n3, grid64, grid32, raw_out, claim, status)
-#define ARB_SCATTER_KIND(TF)                              \
-  switch (kind) {                                         \
-    case ARB_KIND_SCALAR: ARB_SCATTER(TF, ARB_KIND_SCALAR); break; \
-    case ARB_KIND_VECTOR: ARB_SCATTER(TF, ARB_KIND_VECTOR); break; \
-    case ARB_KIND_NORM: ARB_SCATTER(TF, ARB_KIND_NORM); break;     \
-    case ARB_KIND_BOTH: ARB_SCATTER(TF, ARB_KIND_BOTH); break;     \
-    default: return ARB_ERR_INVALID;                      \
+  int64_t tot = 0;
+  for (int a = 0; a < dim; ++a) tot += n[a];
+  const size_t ksm = sizeof(unsigned long long) * (size_t)tot;
+  if (ksm > 200 * 1024) return ARB_ERR_UNSUPPORTED;
+  if (ksm > 48 * 1024) {
+    cudaFuncSetAttribute(ingest_index_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ksm);
+    cudaFuncSetAttribute(ingest_index_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ksm);
+  }
+  if (field_is_f32)
+    ingest_index_kernel<float><<<B, T, ksm, s>>>((const float *)field, npts, ncol, dim, axes, axis_cap, n[0],
+                                                 n[1], n[2], n3, claim, status);
+  else
+    ingest_index_kernel<double><<<B, T, ksm, s>>>((const double *)field, npts, ncol, dim, axes, axis_cap,
+                                                  n[0], n[1], n[2], n3, claim, status);
+#define ARB_GATHER(TF, K)                                                                             \
+  ingest_gather_kernel<TF, K><<<B, T, 0, s>>>((const TF *)field, npts, ncol, dim, claim, grid64, grid32, \
+                                              raw_out, status)
+#define ARB_GATHER_KIND(TF)                                         \
+  switch (kind) {                                                   \
+    case ARB_KIND_SCALAR: ARB_GATHER(TF, ARB_KIND_SCALAR); break;   \
+    case ARB_KIND_VECTOR: ARB_GATHER(TF, ARB_KIND_VECTOR); break;   \
+    case ARB_KIND_NORM: ARB_GATHER(TF, ARB_KIND_NORM); break;       \
+    case ARB_KIND_BOTH: ARB_GATHER(TF, ARB_KIND_BOTH); break;       \
+    default: return ARB_ERR_INVALID;                                \
   }
   if (field_is_f32) {
-    ARB_SCATTER_KIND(float)
+    ARB_GATHER_KIND(float)
   } else {
-    ARB_SCATTER_KIND(double)
+    ARB_GATHER_KIND(double)
   }
-#undef ARB_SCATTER_KIND
-#undef ARB_SCATTER
+#undef ARB_GATHER_KIND
+#undef ARB_GATHER
   return launch_status();
 }
 

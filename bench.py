@@ -335,6 +335,26 @@ def main():
     tq = cuda_time(lambda: o.Query(q), 5, 2) / 5
     extra["warm_query_only"] = {"value": world * nq / tq, "unit": "queries/s"}
 
+    # the coefficient-table strategy: tensor-core table solve + table evaluation
+    if prec == "mixed" and not args.no_fp64:
+        ot = tricubic(field, "quiet", mode="both", precision=prec, strategy="table")
+        tg = cuda_time(lambda: ot.allCoeffs(), 3, 1) / 3
+        tt = cuda_time(lambda: ot.Query(q), 3, 1) / 3
+        cells = ot.nc
+        gemm_bytes = ot._npts * 4 * 8 + cells * 4 * 64 * 4
+        gemm_flops = 2.0 * 64 * 64 * 4 * cells
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if \
+            os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        extra["table_path"] = {
+            "value": world * nq / (tg + tt), "unit": "queries/s",
+            "coef_gemm_ms": 1000 * tg, "table_eval_ms": 1000 * tt,
+            "coef_gemm_gbs": gemm_bytes / tg / 1e9,
+            "coef_gemm_tflops_algorithmic": gemm_flops / tg / 1e12,
+            "coef_gemm_hbm_frac": gemm_bytes / tg / 1e9 / peak,
+            "coef_gemm_bf16_frac": gemm_flops / tg / 1e12 / peaks.get("bf16_tflops", 1900.0),
+            "note": "table: 16.19M cells x 4 fields x 64 float32 coefficients (16.6 GB) per solve"}
+        del ot
+
     e2e = None
     if not args.no_e2e:
         field_h = torch.empty(field.shape, dtype=field.dtype, pin_memory=True)

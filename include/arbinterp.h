@@ -106,8 +106,9 @@ int arb_ingest_axes(const void *field, int32_t field_is_f32, int64_t npts, int32
  * builds with argsort) and writes the per-mode interpolated fields: grid64,
  * optionally grid32 (hi/lo split) and, when raw_out is given, the raw value
  * columns [npts][ncol-dim] in sorted order.  claim is npts uint32 of scratch
- * (zeroed here) used to detect duplicate points.  n holds the host-side axis
- * counts returned by arb_ingest_axes. */
+ * (it receives the inverse permutation grid slot -> row, and detects
+ * duplicate points).  n holds the host-side axis counts returned by
+ * arb_ingest_axes.  npts < 2^32. */
 int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
                        int32_t dim, const double *axes, int64_t axis_cap, const int64_t *n,
                        int32_t kind, double *grid64, float *grid32, double *raw_out,

@@ -254,3 +254,35 @@ def test_fd_planes_match_D_matrix():
         for k in range(8):
             p = ref.basePointInds[cell] + (k & 1) + ref.nx * ((k >> 1) & 1) + ref.nx * ref.ny * (k >> 2)
             assert np.allclose(P[:, p], b[k::8], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("mode", ["both", "vector", "norm"])
+def test_tensor_core_table_matches_fp64(mode):
+    """Mixed-precision table (split-BF16 tcgen05 GEMM, float32 rows) against
+    the float64 table: every coefficient within 1e-6 of its column's scale,
+    alpha_000 within float32 rounding of the value; single-cell solves
+    (partial tiles, cell offsets) included."""
+    tricubic, _ = _mods()
+    from arbinterp_gb300 import synth
+    f = synth.dipole_field3(n=(23, 19, 21), seed=8).numpy()
+    o64 = tricubic(f, "quiet", mode=mode)
+    o64.allCoeffs()
+    omx = tricubic(f, "quiet", mode=mode, precision="mixed")
+    omx.allCoeffs()
+    names = {"both": ("alphax", "alphay", "alphaz", "alphan"), "vector": ("alphax", "alphay", "alphaz"),
+             "norm": ("alphan",)}[mode]
+    for name in names:
+        a64 = getattr(o64, name)[:, :o64.nc]
+        amx = getattr(omx, name)[:, :o64.nc]
+        scale = np.abs(a64).max(axis=1, keepdims=True)
+        scale[0] = np.abs(a64[0]).max()
+        err = (np.abs(amx - a64) / scale).max()
+        assert err <= 1e-6, (name, err)
+    one = tricubic(f, "quiet", mode=mode, precision="mixed")
+    for cell in (0, 7, one.nc - 1):
+        one.calcCoefficients(cell)
+    a = getattr(one, names[0])
+    ref = getattr(o64, names[0])
+    for cell in (0, 7, one.nc - 1):
+        assert np.abs(a[:, cell] - ref[:, cell]).max() <= 1e-6 * np.abs(ref[:, :o64.nc]).max()
+    assert not a[:, 3].any()      # unsolved cells stay zero
