@@ -107,6 +107,85 @@ __device__ __forceinline__ CoordStep coord_step(const double *qrow, const arb_gr
   return s;
 }
 
+// Order-preserving map of a double onto uint64: a < b <=> key(a) < key(b)
+// for non-NaN values, so bounds tests run on the integer pipe.
+__host__ __device__ __forceinline__ unsigned long long ord_key_bits(unsigned long long b) {
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
+}
+
+struct FastAxis {
+  unsigned long long lo_key, hi_key;  // ord keys of IntMin / IntMax
+  double lo, h, inv_h;
+};
+
+// Mixed-precision coordinate step: the cell index is bit-exact (it equals
+// floor((q - IntMin) / h) with IEEE division, as the reference computes it)
+// and the fractional offset is returned to 2^-24.  Float64-pipe work per
+// axis: one subtraction and one multiplication; the floor and the fraction
+// come from the product's bit pattern with integer operations.  Only when
+// the product lies within 8 ulps of an integer (where multiplying by 1/h
+// and dividing by h could floor differently) is the IEEE division redone.
+template <int DIM>
+__device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const FastAxis *ax,
+                                                     const arb_grid &g, float frac[DIM]) {
+  CoordStep s;
+  s.oob = false;
+  s.nan = false;
+  int64_t fl[DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    const double q = qrow[a];
+    const unsigned long long qb = (unsigned long long)__double_as_longlong(q);
+    const bool isnan = (qb & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL;
+    const unsigned long long k = ord_key_bits(qb);
+    const bool out = !isnan && (k < ax[a].lo_key || k > ax[a].hi_key);
+    s.nan |= isnan;
+    s.oob |= out;
+    if (isnan || out) {
+      fl[a] = 0;
+      frac[a] = 0.f;
+      continue;
+    }
+    const double d = q - ax[a].lo;
+    double iu = d * ax[a].inv_h;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(iu);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    int64_t kk = 0;
+    float fr = 0.f;
+    bool redo = (e > 30);
+    if (e >= -1 && e <= 30) {
+      const int nf = 52 - e;  // 22 .. 53 fraction bits
+      const unsigned long long m = (b & 0xfffffffffffffULL) | (1ULL << 52);
+      const unsigned long long one = 1ULL << nf;
+      const unsigned long long fb = m & (one - 1);
+      kk = (int64_t)(m >> nf);
+      redo = (fb < 8ULL) || (fb > one - 8ULL);
+      // top 24 bits of the fraction, converted exactly, times 2^-24
+      const unsigned f24 = (unsigned)(nf >= 24 ? (fb >> (nf - 24)) : (fb << (24 - nf)));
+      fr = __uint2float_rz(f24) * 5.9604644775390625e-08f;
+    } else if (e < -1) {
+      fr = __double2float_rn(iu);  // iu < 0.5: floor is 0
+    }
+    if (redo) {
+      iu = d / ax[a].h;
+      const double kf = floor(iu);
+      kk = (int64_t)kf;
+      fr = (float)(iu - kf);
+    }
+    fl[a] = kk;
+    frac[a] = fr;
+  }
+  if (s.oob || s.nan) {
+    s.idx = g.nc;
+    return s;
+  }
+  int64_t idx = fl[DIM - 1];
+#pragma unroll
+  for (int a = DIM - 2; a >= 0; --a) idx = idx * (g.n[a] - 3) + fl[a];
+  s.idx = idx;
+  return s;
+}
+
 // Cell coordinates of a flat index (the reference's upper-face aliasing
 // falls out of this: (nPos, iy, iz) decodes as (0, iy+1, iz)).
 template <int DIM>

@@ -3,6 +3,8 @@
 // query prologue (cell index, out-of-volume rows, sentinel semantics).
 #pragma once
 
+#include <string.h>
+
 #include "arb_common.cuh"
 
 namespace arb {
@@ -11,6 +13,7 @@ namespace arb {
 struct KParams {
   double inv_h[4];
   float inv_hf[4];
+  FastAxis ax[4];
 };
 
 template <int DIM, int F>
@@ -48,16 +51,23 @@ __device__ __forceinline__ void write_vals(const arb_query_out &o, int64_t i, co
 
 // Shared prologue: cell index, out-of-volume handling, sentinel semantics.
 // Returns true when the row still needs evaluating.
+// EXACT (float64 path): IEEE division, frac in double.  Otherwise the
+// mixed-precision step (exact index, float frac, two float64 ops per axis).
 template <int DIM, int F, bool EXACT>
 __device__ __forceinline__ bool query_prologue(const arb_grid &g, const KParams &kp, double *q,
                                                int64_t i, int64_t qs, int wb,
                                                const arb_query_out &o, int32_t *status,
-                                               double frac[DIM], int64_t &idx) {
+                                               typename std::conditional<EXACT, double, float>::type frac[DIM],
+                                               int64_t &idx) {
   double *qr = q + i * qs;
   double qv[DIM];
 #pragma unroll
   for (int a = 0; a < DIM; ++a) qv[a] = qr[a];
-  const CoordStep s = coord_step<DIM, EXACT>(qv, g, kp.inv_h, frac);
+  CoordStep s;
+  if constexpr (EXACT)
+    s = coord_step<DIM, true>(qv, g, kp.inv_h, frac);
+  else
+    s = coord_step_fast<DIM>(qv, kp.ax, g, frac);
   append_oob(o, i, s.oob);
   if (s.oob && wb) {
     for (int64_t c = 0; c < qs; ++c) qr[c] = qnan();
@@ -463,6 +473,15 @@ static inline KParams make_kparams(const arb_grid *g) {
     const double h = a < g->dim ? g->h[a] : 1.0;
     kp.inv_h[a] = 1.0 / h;
     kp.inv_hf[a] = (float)(1.0 / h);
+    unsigned long long lb, hb;
+    const double lo = a < g->dim ? g->lo[a] : 0.0, hi = a < g->dim ? g->hi[a] : 0.0;
+    memcpy(&lb, &lo, 8);
+    memcpy(&hb, &hi, 8);
+    kp.ax[a].lo_key = ord_key_bits(lb);
+    kp.ax[a].hi_key = ord_key_bits(hb);
+    kp.ax[a].lo = lo;
+    kp.ax[a].h = h;
+    kp.ax[a].inv_h = 1.0 / h;
   }
   return kp;
 }

@@ -26,10 +26,10 @@ __global__ void __launch_bounds__(256) otf3_kernel(arb_grid g, KParams kp, doubl
   using T = typename std::conditional<MIXED, float, double>::type;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
-  double frac[3];
+  T frac_[3];
   int64_t idx;
-  if (!query_prologue<3, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac, idx)) return;
-  const T fr[3] = {(T)frac[0], (T)frac[1], (T)frac[2]};
+  if (!query_prologue<3, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac_, idx)) return;
+  const T fr[3] = {frac_[0], frac_[1], frac_[2]};
   double val[F], grad[3];
   eval_otf3<F, MIXED>(g, kp, idx, fr, val, grad);
   write_vals<3, F>(o, i, val, grad);
@@ -42,10 +42,10 @@ __global__ void __launch_bounds__(128) otf4_kernel(arb_grid g, KParams kp, doubl
   using T = typename std::conditional<MIXED, float, double>::type;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
-  double frac[4];
+  T frac_[4];
   int64_t idx;
-  if (!query_prologue<4, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac, idx)) return;
-  const T fr[4] = {(T)frac[0], (T)frac[1], (T)frac[2], (T)frac[3]};
+  if (!query_prologue<4, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac_, idx)) return;
+  const T fr[4] = {frac_[0], frac_[1], frac_[2], frac_[3]};
   double val[F], grad[4] = {0, 0, 0, 0};
   eval_otf4<F, MIXED>(g, kp, idx, fr, val, grad);
   write_vals<4, F>(o, i, val, grad);
@@ -58,12 +58,9 @@ __global__ void __launch_bounds__(256) tab_kernel(arb_grid g, KParams kp, double
   using T = typename std::conditional<MIXED, float, double>::type;
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
-  double frac[DIM];
-  int64_t idx;
-  if (!query_prologue<DIM, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac, idx)) return;
   T x[DIM];
-#pragma unroll
-  for (int a = 0; a < DIM; ++a) x[a] = (T)frac[a];
+  int64_t idx;
+  if (!query_prologue<DIM, F, !MIXED>(g, kp, q, i, qs, wb, o, status, x, idx)) return;
   double val[F], grad[DIM];
   eval_tab<DIM, F, MIXED>(g, kp, idx, x, val, grad);
   write_vals<DIM, F>(o, i, val, grad);

@@ -83,10 +83,15 @@ __global__ void __launch_bounds__(256) locate_kernel(arb_grid g, KParams kp, Bin
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
   double *qr = q + i * qs;
-  double qv[DIM], frac[DIM];
+  double qv[DIM];
+  T frac[DIM];
 #pragma unroll
   for (int a = 0; a < DIM; ++a) qv[a] = qr[a];
-  const CoordStep s = coord_step<DIM, EXACT>(qv, g, kp.inv_h, frac);
+  CoordStep s;
+  if constexpr (EXACT)
+    s = coord_step<DIM, true>(qv, g, kp.inv_h, frac);
+  else
+    s = coord_step_fast<DIM>(qv, kp.ax, g, frac);
   append_oob(o, i, s.oob);
   if (s.oob && wb)
     for (int64_t c = 0; c < qs; ++c) qr[c] = qnan();
@@ -113,7 +118,7 @@ __global__ void __launch_bounds__(256) locate_kernel(arb_grid g, KParams kp, Bin
   w.code[i] = code;
   T *fr = reinterpret_cast<T *>(w.frac) + i * DIM;
 #pragma unroll
-  for (int a = 0; a < DIM; ++a) fr[a] = (T)frac[a];
+  for (int a = 0; a < DIM; ++a) fr[a] = frac[a];
 }
 
 // Exclusive scan of n counters in one block (n up to a few million).
@@ -187,6 +192,81 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
   write_vals<DIM, F>(o, i, val, grad);
 }
 
+// 3D, four fields ('both' mode), mixed precision: 8 lanes per query.  One
+// grid row (4 points x 4 fields x (hi, lo) float32 = 128 bytes) is read by 8
+// lanes with one 16-byte load each, so a warp load touches 4 rows instead of
+// 32 scattered lines.  Lane s of a query group holds point s>>1 and fields
+// 2(s&1), 2(s&1)+1; it contracts its 16 rows over y and z, then the 4 lanes
+// of a field pair reduce over x with two butterfly shuffles.
+__global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KParams kp, int64_t nq,
+                                                                arb_query_out o, SortedWork w) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane & 7, p = sub >> 1, fp = sub & 1;
+  const int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 3;
+  if (t >= nq) return;  // whole 8-lane groups leave together
+  const int64_t code = w.s_code[t];
+  const int64_t i = w.s_row[t];
+  if (code < 0 || code == g.nc) {
+    if (sub == 0) write_const<3, 4>(o, i, (code < 0 || g.sentinel_nan) ? qnan() : 0.0);
+    return;
+  }
+  const float *fr = reinterpret_cast<const float *>(w.s_frac) + t * 3;
+  const float fx = fr[0], fy = fr[1], fz = fr[2];
+  float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
+  cr_weights<float>(fx, wx);
+  cr_dweights<float>(fx, dx);
+  cr_weights<float>(fy, wy);
+  cr_dweights<float>(fy, dy);
+  cr_weights<float>(fz, wz);
+  cr_dweights<float>(fz, dz);
+  int64_t c[3];
+  cell_coords<3>(code, g, c);
+  const int64_t nx = g.n[0], ny = g.n[1];
+  const float4 *g4 = reinterpret_cast<const float4 *>(g.grid32);
+  const int64_t pref = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
+  const float4 ref = __ldg(g4 + pref * 2 + fp);
+  float S0 = 0.f, S1 = 0.f, Sy = 0.f, Sz = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t pt = ((c[2] + k) * ny + (c[1] + j)) * nx + c[0] + p;
+      const float4 v = __ldg(g4 + pt * 2 + fp);
+      const float d0 = (v.x - ref.x) + (v.y - ref.y);
+      const float d1 = (v.z - ref.z) + (v.w - ref.w);
+      const float wyz = wy[j] * wz[k];
+      S0 += wyz * d0;
+      S1 += wyz * d1;
+      Sy += (dy[j] * wz[k]) * d1;
+      Sz += (wy[j] * dz[k]) * d1;
+    }
+  }
+  float V0 = wx[p] * S0, V1 = wx[p] * S1, Gx = dx[p] * S1, Gy = wx[p] * Sy, Gz = wx[p] * Sz;
+  const unsigned mask = 0xffu << (lane & 24);
+#pragma unroll
+  for (int off = 2; off <= 4; off <<= 1) {
+    V0 += __shfl_xor_sync(mask, V0, off);
+    V1 += __shfl_xor_sync(mask, V1, off);
+    Gx += __shfl_xor_sync(mask, Gx, off);
+    Gy += __shfl_xor_sync(mask, Gy, off);
+    Gz += __shfl_xor_sync(mask, Gz, off);
+  }
+  if (sub == 0) {
+    if (o.comps) {
+      o.comps[i * 3 + 0] = (double)(ref.x + (ref.y + V0));
+      o.comps[i * 3 + 1] = (double)(ref.z + (ref.w + V1));
+    }
+  } else if (sub == 1) {
+    if (o.comps) o.comps[i * 3 + 2] = (double)(ref.x + (ref.y + V0));
+    if (o.norms) o.norms[i] = (double)(ref.z + (ref.w + V1));
+    if (o.grads) {
+      o.grads[i * 3 + 0] = (double)(Gx * kp.inv_hf[0]);
+      o.grads[i * 3 + 1] = (double)(Gy * kp.inv_hf[1]);
+      o.grads[i * 3 + 2] = (double)(Gz * kp.inv_hf[2]);
+    }
+  }
+}
+
 template <int DIM, bool MIXED>
 static void launch_sorted(const arb_grid *g, const KParams &kp, const BinGeom &bg, double *q, int64_t nq,
                           int64_t qs, int wb, const arb_query_out *out, int32_t *status,
@@ -202,6 +282,9 @@ static void launch_sorted(const arb_grid *g, const KParams &kp, const BinGeom &b
 #define ES(FF, TAB) eval_sorted_kernel<DIM, FF, MIXED, TAB><<<BE, TE, 0, s>>>(*g, kp, nq, *out, w)
   if (table) {
     switch (g->nfield) { case 1: ES(1, true); break; case 3: ES(3, true); break; default: ES(4, true); break; }
+  } else if (DIM == 3 && MIXED && g->nfield == 4) {
+    const unsigned BC = (unsigned)((nq * 8 + 255) / 256);
+    eval_sorted_coop4_kernel<<<BC, 256, 0, s>>>(*g, kp, nq, *out, w);
   } else {
     switch (g->nfield) { case 1: ES(1, false); break; case 3: ES(3, false); break; default: ES(4, false); break; }
   }
