@@ -19,10 +19,6 @@ __device__ __forceinline__ unsigned long long ord_key(double v) {
   unsigned long long b = (unsigned long long)__double_as_longlong(v);
   return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
 }
-__device__ __forceinline__ double ord_val(unsigned long long k) {
-  unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffULL) : ~k;
-  return __longlong_as_double((long long)b);
-}
 
 template <typename TF>
 __device__ __forceinline__ double ld(const TF *p) { return (double)p[0]; }
@@ -39,51 +35,32 @@ __global__ void axes_init_kernel(AxesWork *w) {
   }
 }
 
-template <typename TF>
-__global__ void axes_min_kernel(const TF *field, int64_t npts, int ncol, int dim, AxesWork *w,
-                                int32_t *status) {
-  unsigned long long m[4] = {~0ULL, ~0ULL, ~0ULL, ~0ULL};
-  bool bad = false;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    for (int a = 0; a < dim; ++a) {
-      const double v = ld(field + i * ncol + a);
-      if (v != v) bad = true;
-      const unsigned long long k = ord_key(v);
-      m[a] = k < m[a] ? k : m[a];
-    }
-  }
-  if (bad) set_status(status, ARB_ERR_IRREGULAR_GRID);
-  for (int a = 0; a < dim; ++a) {
-    unsigned long long v = m[a];
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long u = __shfl_down_sync(0xffffffffu, v, o);
-      v = u < v ? u : v;
-    }
-    if ((threadIdx.x & 31) == 0) atomicMin(&w->minkey[a], v);
-  }
-}
-
-// Appends every row that lies on the axis line of axis a through the minimum
-// corner (all other coordinates equal to their minimum).
+// Appends every row that lies on an axis line through row 0 (all other
+// coordinates equal to row 0's).  For a full tensor grid each such line
+// carries exactly that axis' samples, the same set the reference reads off
+// the lines through the first sorted row; the index pass then checks that
+// every row lies on the grid.  NaN coordinates mark the grid irregular.
 template <typename TF>
 __global__ void axes_collect_kernel(const TF *field, int64_t npts, int ncol, int dim, AxesWork *w,
                                     double *raw_axes, int64_t cap, int32_t *status) {
-  double mn[4];
-  for (int a = 0; a < dim; ++a) mn[a] = ord_val(w->minkey[a]);
+  double r0[4];
+  for (int a = 0; a < dim; ++a) r0[a] = ld(field + a);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts;
        i += (int64_t)gridDim.x * blockDim.x) {
     double v[4];
     int neq = 0, which = -1;
+    bool bad = false;
     for (int a = 0; a < dim; ++a) {
       v[a] = ld(field + i * ncol + a);
-      if (v[a] != mn[a]) {
+      bad |= (v[a] != v[a]);
+      if (v[a] != r0[a]) {
         ++neq;
         which = a;
       }
     }
-    if (neq > 1) continue;
-    // neq == 0: the corner itself belongs to every axis line
+    if (bad) set_status(status, ARB_ERR_IRREGULAR_GRID);
+    if (neq > 1 || bad) continue;
+    // neq == 0: row 0 itself belongs to every axis line
     for (int a = 0; a < dim; ++a) {
       if (neq == 1 && a != which) continue;
       const unsigned long long slot = atomicAdd(&w->count[a], 1ULL);
@@ -292,11 +269,9 @@ extern "C" int arb_ingest_axes(const void *field, int32_t field_is_f32, int64_t 
   const int T = 256;
   const int B = grid_blocks(npts, T);
   if (field_is_f32) {
-    axes_min_kernel<float><<<B, T, 0, s>>>((const float *)field, npts, ncol, dim, w, status);
     axes_collect_kernel<float>
         <<<B, T, 0, s>>>((const float *)field, npts, ncol, dim, w, raw, axis_cap, status);
   } else {
-    axes_min_kernel<double><<<B, T, 0, s>>>((const double *)field, npts, ncol, dim, w, status);
     axes_collect_kernel<double>
         <<<B, T, 0, s>>>((const double *)field, npts, ncol, dim, w, raw, axis_cap, status);
   }

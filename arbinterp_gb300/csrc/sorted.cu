@@ -198,17 +198,22 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
 // 32 scattered lines.  Lane s of a query group holds point s>>1 and fields
 // 2(s&1), 2(s&1)+1; it contracts its 16 rows over y and z, then the 4 lanes
 // of a field pair reduce over x with two butterfly shuffles.
+// Each block walks COOP_CHUNK consecutive sorted queries (about one spatial
+// bin) so the bin's grid footprint stays in that SM's L1.
+constexpr int COOP_CHUNK = 256;
+
 __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KParams kp, int64_t nq,
                                                                 arb_query_out o, SortedWork w) {
   const int lane = threadIdx.x & 31;
   const int sub = lane & 7, p = sub >> 1, fp = sub & 1;
-  const int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 3;
-  if (t >= nq) return;  // whole 8-lane groups leave together
+  const int64_t t0 = (int64_t)blockIdx.x * COOP_CHUNK;
+  const int64_t t1 = min(t0 + COOP_CHUNK, nq);
+  for (int64_t t = t0 + (threadIdx.x >> 3); t < t1; t += blockDim.x >> 3) {  // groups stay converged
   const int64_t code = w.s_code[t];
   const int64_t i = w.s_row[t];
   if (code < 0 || code == g.nc) {
     if (sub == 0) write_const<3, 4>(o, i, (code < 0 || g.sentinel_nan) ? qnan() : 0.0);
-    return;
+    continue;
   }
   const float *fr = reinterpret_cast<const float *>(w.s_frac) + t * 3;
   const float fx = fr[0], fy = fr[1], fz = fr[2];
@@ -265,6 +270,7 @@ __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KPar
       o.grads[i * 3 + 2] = (double)(Gz * kp.inv_hf[2]);
     }
   }
+  }
 }
 
 template <int DIM, bool MIXED>
@@ -283,7 +289,7 @@ static void launch_sorted(const arb_grid *g, const KParams &kp, const BinGeom &b
   if (table) {
     switch (g->nfield) { case 1: ES(1, true); break; case 3: ES(3, true); break; default: ES(4, true); break; }
   } else if (DIM == 3 && MIXED && g->nfield == 4) {
-    const unsigned BC = (unsigned)((nq * 8 + 255) / 256);
+    const unsigned BC = (unsigned)((nq + COOP_CHUNK - 1) / COOP_CHUNK);
     eval_sorted_coop4_kernel<<<BC, 256, 0, s>>>(*g, kp, nq, *out, w);
   } else {
     switch (g->nfield) { case 1: ES(1, false); break; case 3: ES(3, false); break; default: ES(4, false); break; }
