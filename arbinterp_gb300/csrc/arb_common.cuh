@@ -188,8 +188,22 @@ __device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const F
 
 // Cell coordinates of a flat index (the reference's upper-face aliasing
 // falls out of this: (nPos, iy, iz) decodes as (0, iy+1, iz)).
+// 64-bit integer division runs on the float64 pipe on this GPU, so indices
+// below 2^32 (every practical grid) take the 32-bit unsigned path.
 template <int DIM>
 __device__ __forceinline__ void cell_coords(int64_t idx, const arb_grid &g, int64_t c[DIM]) {
+  if (idx < 0x100000000LL) {
+    uint32_t u = (uint32_t)idx;
+#pragma unroll
+    for (int a = 0; a < DIM - 1; ++a) {
+      const uint32_t m = (uint32_t)(g.n[a] - 3);
+      const uint32_t qd = u / m;
+      c[a] = (int64_t)(u - qd * m);
+      u = qd;
+    }
+    c[DIM - 1] = (int64_t)u;
+    return;
+  }
 #pragma unroll
   for (int a = 0; a < DIM - 1; ++a) {
     const int64_t m = g.n[a] - 3;
@@ -200,6 +214,41 @@ __device__ __forceinline__ void cell_coords(int64_t idx, const arb_grid &g, int6
 }
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }
+
+// float -> double on the integer pipe (exact for normal numbers and zeros;
+// subnormals, infinities and NaN take the conversion instruction).
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)u << 32));
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) |
+                               ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)b);
+}
+
+// Split a double into float32 hi = RN(v) and lo = RN(v - hi) with integer
+// operations (bit-identical to the float64-pipe conversions) for
+// 2^-45 <= |v| < 2^127; other magnitudes fall back to the conversions.
+__device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int E = (int)((b >> 52) & 0x7ff);
+  if (E < 978 || E > 1023 + 126) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
+    return;
+  }
+  const unsigned long long m = b & 0xfffffffffffffULL;
+  const unsigned top = (unsigned)(m >> 29);          // 23 kept mantissa bits
+  const unsigned r = (unsigned)(m & 0x1fffffffULL);   // 29 dropped bits
+  const bool up = (r > 0x10000000u) || (r == 0x10000000u && (top & 1u));
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  hi = __uint_as_float(sign | ((((unsigned)(E - 1023 + 127)) << 23) + top + (up ? 1u : 0u)));
+  const int rs = up ? (int)r - 0x20000000 : (int)r;   // v - hi in units of 2^(E-1075)
+  const float l = __int2float_rn(rs) * __uint_as_float(((unsigned)(E - 948)) << 23);
+  lo = sign ? -l : l;
+}
 
 // Warp-aggregated append of an out-of-volume row index.
 __device__ __forceinline__ void append_oob(const arb_query_out &o, int64_t row, bool pred) {

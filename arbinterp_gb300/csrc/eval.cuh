@@ -219,15 +219,15 @@ __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, 
 #pragma unroll
   for (int f = 0; f < F; ++f) {
     if constexpr (MIXED)
-      val[f] = (double)(rhi[f] + (rlo[f] + acc[f]));
+      val[f] = f2d_exact(rhi[f] + (rlo[f] + acc[f]));
     else
       val[f] = (double)acc[f];
   }
   if (GRAD) {
     if constexpr (MIXED) {
-      grad[0] = (double)(gx * kp.inv_hf[0]);
-      grad[1] = (double)(gy * kp.inv_hf[1]);
-      grad[2] = (double)(gz * kp.inv_hf[2]);
+      grad[0] = f2d_exact(gx * kp.inv_hf[0]);
+      grad[1] = f2d_exact(gy * kp.inv_hf[1]);
+      grad[2] = f2d_exact(gz * kp.inv_hf[2]);
     } else {
       grad[0] = (double)gx * kp.inv_h[0];
       grad[1] = (double)gy * kp.inv_h[1];
@@ -357,7 +357,7 @@ __device__ __forceinline__ void eval_otf4(const arb_grid &g, const KParams &kp, 
     const T C = hb[3][0] * Cz[0] + hb[3][1] * Cz[1];
     const T total = V + C;
     if constexpr (MIXED)
-      val[f] = (double)(rhi + (rlo + total));
+      val[f] = f2d_exact(rhi + (rlo + total));
     else
       val[f] = (double)total;
     if (gradf) {
@@ -368,7 +368,7 @@ __device__ __forceinline__ void eval_otf4(const arb_grid &g, const KParams &kp, 
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
         if constexpr (MIXED)
-          grad[a] = (double)(G[a] * kp.inv_hf[a]);
+          grad[a] = f2d_exact(G[a] * kp.inv_hf[a]);
         else
           grad[a] = (double)G[a] * kp.inv_h[a];
       }
@@ -453,12 +453,15 @@ __device__ __forceinline__ void eval_tab(const arb_grid &g, const KParams &kp, i
         G[2] = Gz[2];
       }
     }
-    val[f] = (double)V;
+    if constexpr (MIXED)
+      val[f] = f2d_exact(V);
+    else
+      val[f] = V;
     if (gradf) {
 #pragma unroll
       for (int d = 0; d < DIM; ++d) {
         if constexpr (MIXED)
-          grad[d] = (double)(G[d] * kp.inv_hf[d]);
+          grad[d] = f2d_exact(G[d] * kp.inv_hf[d]);
         else
           grad[d] = (double)G[d] * kp.inv_h[d];
       }

@@ -150,8 +150,21 @@ __global__ void __launch_bounds__(256) ingest_index_kernel(const TF *field, int6
     const TF *row = field + i * ncol;
     int64_t dest = 0;
     bool ok = true;
+    // Rows of a warp usually share all but their fastest-varying coordinate:
+    // when a coordinate is equal across the warp, one lane searches for it.
+    const unsigned act = __activemask();
+    const int leader = __ffs(act) - 1;
+    const int lane = threadIdx.x & 31;
     for (int a = dim - 1; a >= 0; --a) {
-      const int64_t r = find_key(skeys + off[a], nn[a], ord_key((double)row[a]));
+      const unsigned long long key = ord_key((double)row[a]);
+      const unsigned long long k0 = __shfl_sync(act, key, leader);
+      int64_t r;
+      if (__all_sync(act, key == k0)) {
+        r = lane == leader ? find_key(skeys + off[a], nn[a], key) : 0;
+        r = __shfl_sync(act, r, leader);
+      } else {
+        r = find_key(skeys + off[a], nn[a], key);
+      }
       ok &= (r >= 0);
       dest = dest * nn[a] + (r < 0 ? 0 : r);
     }
@@ -222,8 +235,7 @@ __global__ void __launch_bounds__(256) ingest_gather_kernel(const TF *field, int
       float hi[4], lo[4];
 #pragma unroll
       for (int f = 0; f < F; ++f) {
-        hi[f] = __double2float_rn(out[f]);
-        lo[f] = __double2float_rn(out[f] - (double)hi[f]);
+        split_f32(out[f], hi[f], lo[f]);
       }
       if (F == 4) {
         reinterpret_cast<float4 *>(grid32)[dest * 2] = make_float4(hi[0], lo[0], hi[1 % F], lo[1 % F]);

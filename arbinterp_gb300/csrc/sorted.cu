@@ -258,16 +258,16 @@ __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KPar
   }
   if (sub == 0) {
     if (o.comps) {
-      o.comps[i * 3 + 0] = (double)(ref.x + (ref.y + V0));
-      o.comps[i * 3 + 1] = (double)(ref.z + (ref.w + V1));
+      o.comps[i * 3 + 0] = f2d_exact(ref.x + (ref.y + V0));
+      o.comps[i * 3 + 1] = f2d_exact(ref.z + (ref.w + V1));
     }
   } else if (sub == 1) {
-    if (o.comps) o.comps[i * 3 + 2] = (double)(ref.x + (ref.y + V0));
-    if (o.norms) o.norms[i] = (double)(ref.z + (ref.w + V1));
+    if (o.comps) o.comps[i * 3 + 2] = f2d_exact(ref.x + (ref.y + V0));
+    if (o.norms) o.norms[i] = f2d_exact(ref.z + (ref.w + V1));
     if (o.grads) {
-      o.grads[i * 3 + 0] = (double)(Gx * kp.inv_hf[0]);
-      o.grads[i * 3 + 1] = (double)(Gy * kp.inv_hf[1]);
-      o.grads[i * 3 + 2] = (double)(Gz * kp.inv_hf[2]);
+      o.grads[i * 3 + 0] = f2d_exact(Gx * kp.inv_hf[0]);
+      o.grads[i * 3 + 1] = f2d_exact(Gy * kp.inv_hf[1]);
+      o.grads[i * 3 + 2] = f2d_exact(Gz * kp.inv_hf[2]);
     }
   }
   }
