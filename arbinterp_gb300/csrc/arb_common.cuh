@@ -215,6 +215,37 @@ __device__ __forceinline__ void cell_coords(int64_t idx, const arb_grid &g, int6
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }
 
+// ---- mixed-precision grid (grid32) layout -----------------------------------
+//   F = 1: [npts] float2 (hi, lo)               value + gradient field
+//   F = 3: [npts] float4 (hi_x, hi_y, hi_z, 0)   components: values only
+//   F = 4: [npts] float4 (hi_x, hi_y, hi_z, hi_n), then [npts] float lo_n
+// hi = RN(v), lo = RN(v - hi).  Only the field whose gradient is returned
+// keeps lo; a value interpolated from float32-rounded samples is within
+// ~2 eps32 max|f| of the float64 one (Catmull-Rom weights sum to 1 with
+// absolute sum <= 1.25 per axis), whereas a gradient needs the residual.
+template <int F>
+__host__ __device__ constexpr int g32_floats_per_point() { return F == 1 ? 2 : (F == 3 ? 4 : 5); }
+
+__device__ __forceinline__ int64_t grid_points(const arb_grid &g) {
+  int64_t n = g.n[0] * g.n[1] * g.n[2];
+  if (g.dim == 4) n *= g.n[3];
+  return n;
+}
+
+// hi / lo of field f at point p (lo = 0 for fields stored without residual).
+template <int F>
+__device__ __forceinline__ void g32_load(const float *g32, int64_t npts, int64_t p, int f, float &hi,
+                                         float &lo) {
+  if (F == 1) {
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(g32) + p);
+    hi = v.x;
+    lo = v.y;
+  } else {
+    hi = __ldg(g32 + p * 4 + f);
+    lo = (F == 4 && f == 3) ? __ldg(g32 + npts * 4 + p) : 0.f;
+  }
+}
+
 // float -> double on the integer pipe (exact for normal numbers and zeros;
 // subnormals, infinities and NaN take the conversion instruction).
 __device__ __forceinline__ double f2d_exact(float f) {

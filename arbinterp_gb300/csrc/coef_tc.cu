@@ -65,16 +65,16 @@ __device__ __forceinline__ uint32_t bf16_bits(float x) {
 
 }  // namespace
 
+template <int F>
 __global__ void __launch_bounds__(128, 4) coef3_tc_kernel(arb_grid g, int64_t cell0, int64_t ncells,
                                                           float *table, int32_t *status) {
   extern __shared__ unsigned char smem_raw[];
   TcSmem &sm = *reinterpret_cast<TcSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int F = g.nfield;
   const int64_t rows = ncells * F;
+  const int64_t npts = grid_points(g);
   const int64_t ntiles = (rows + TM - 1) / TM;
   const int64_t nx = g.n[0], ny = g.n[1];
-  const float2 *g32 = reinterpret_cast<const float2 *>(g.grid32);
 
   // B operand: B[n][k] = A[n][k] = A1[ex][ox] A1[ey][oy] A1[ez][oz]
   for (int e = tid; e < 64 * 64; e += blockDim.x) {
@@ -110,9 +110,7 @@ __global__ void __launch_bounds__(128, 4) coef3_tc_kernel(arb_grid g, int64_t ce
       int64_t c[3];
       cell_coords<3>(cell, g, c);
       const int64_t pref = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
-      const float2 rv = __ldg(g32 + pref * F + f);
-      rhi = rv.x;
-      rlo = rv.y;
+      g32_load<F>(g.grid32, npts, pref, f, rhi, rlo);
 #pragma unroll
       for (int ch = 0; ch < 8; ++ch) {  // 8 points = x-row pair (oy = 2ch&3 ..)
         uint32_t ph[4], pm[4], pl[4];
@@ -124,8 +122,9 @@ __global__ void __launch_bounds__(128, 4) coef3_tc_kernel(arb_grid g, int64_t ce
             const int k = ch * 8 + u * 2 + w;          // point index ox + 4 oy + 16 oz
             const int ox = k & 3, oy = (k >> 2) & 3, oz = k >> 4;
             const int64_t p = ((c[2] + oz) * ny + (c[1] + oy)) * nx + (c[0] + ox);
-            const float2 v = __ldg(g32 + p * F + f);
-            const float d = (v.x - rhi) + (v.y - rlo);
+            float vh, vl;
+            g32_load<F>(g.grid32, npts, p, f, vh, vl);
+            const float d = (vh - rhi) + (vl - rlo);
             const __nv_bfloat16 h = __float2bfloat16_rn(d);
             const float r1 = d - __bfloat162float(h);
             const __nv_bfloat16 m = __float2bfloat16_rn(r1);
@@ -218,20 +217,29 @@ int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *tabl
   const size_t smem = sizeof(TcSmem) + 1024;
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(coef3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(coef3_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(coef3_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(coef3_tc_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
       return ARB_ERR_CUDA;
     attr = true;
   }
   const int64_t rows = ncells * g->nfield;
   const int64_t tiles = (rows + TM - 1) / TM;
   static int per_sm = 0;
-  if (!per_sm && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coef3_tc_kernel, 128, smem) != cudaSuccess)
+  if (!per_sm && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coef3_tc_kernel<4>, 128, smem) != cudaSuccess)
     return ARB_ERR_CUDA;
   if (per_sm < 1) per_sm = 1;
   int64_t grid = (int64_t)num_sms() * per_sm;
   if (grid > tiles) grid = tiles;
-  coef3_tc_kernel<<<(unsigned)grid, 128, smem, s>>>(*g, cell0, ncells, table, status);
+  switch (g->nfield) {
+    case 1: coef3_tc_kernel<1><<<(unsigned)grid, 128, smem, s>>>(*g, cell0, ncells, table, status); break;
+    case 3: coef3_tc_kernel<3><<<(unsigned)grid, 128, smem, s>>>(*g, cell0, ncells, table, status); break;
+    case 4: coef3_tc_kernel<4><<<(unsigned)grid, 128, smem, s>>>(*g, cell0, ncells, table, status); break;
+    default: return ARB_ERR_INVALID;
+  }
   return launch_status();
 }
 

@@ -118,36 +118,35 @@ __device__ __forceinline__ void load_row64(const double *grid, int64_t p, double
 // Deltas against the reference point: (hi - rhi) + (lo - rlo) is accurate to
 // float32 rounding of the DIFFERENCE, so gradients keep full relative
 // precision even where |f| >> h |grad f|.
+// (grid32 layout: see g32_load in arb_common.cuh.)
 template <int F>
-__device__ __forceinline__ void load_row32(const float *grid, int64_t p, const float *rhi,
+__device__ __forceinline__ void load_row32(const float *grid, int64_t npts, int64_t p, const float *rhi,
                                            const float *rlo, float v[4][F]) {
-  const float2 *r = reinterpret_cast<const float2 *>(grid) + p * F;
-  if (F == 4) {
-    const float4 *r4 = reinterpret_cast<const float4 *>(r);
+  if (F == 1) {
+    const float2 *r = reinterpret_cast<const float2 *>(grid) + p;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const float4 a = __ldg(r4 + 2 * i), b = __ldg(r4 + 2 * i + 1);
+      const float2 a = __ldg(r + i);
       v[i][0] = (a.x - rhi[0]) + (a.y - rlo[0]);
-      v[i][1 % F] = (a.z - rhi[1 % F]) + (a.w - rlo[1 % F]);
-      v[i][2 % F] = (b.x - rhi[2 % F]) + (b.y - rlo[2 % F]);
-      v[i][3 % F] = (b.z - rhi[3 % F]) + (b.w - rlo[3 % F]);
     }
   } else {
+    const float4 *r4 = reinterpret_cast<const float4 *>(grid) + p;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int f = 0; f < F; ++f) {
-        const float2 a = __ldg(r + i * F + f);
-        v[i][f] = (a.x - rhi[f]) + (a.y - rlo[f]);
-      }
+    for (int i = 0; i < 4; ++i) {
+      const float4 a = __ldg(r4 + i);
+      v[i][0] = a.x - rhi[0];
+      v[i][1 % F] = a.y - rhi[1 % F];
+      v[i][2 % F] = a.z - rhi[2 % F];
+      if (F == 4) v[i][3 % F] = (a.w - rhi[3 % F]) + (__ldg(grid + npts * 4 + p + i) - rlo[3 % F]);
+    }
   }
 }
 
 template <int F, bool MIXED, typename T>
-__device__ __forceinline__ void load_row(const arb_grid &g, int64_t p, const float *rhi,
+__device__ __forceinline__ void load_row(const arb_grid &g, int64_t npts, int64_t p, const float *rhi,
                                          const float *rlo, T v[4][F]) {
   if constexpr (MIXED)
-    load_row32<F>(g.grid32, p, rhi, rlo, v);
+    load_row32<F>(g.grid32, npts, p, rhi, rlo, v);
   else
     load_row64<F>(g.grid64, p, v);
 }
@@ -172,16 +171,12 @@ __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, 
     cr_dweights<T>((T)frac[2], dz);
   }
   float rhi[F], rlo[F];
+  const int64_t npts = grid_points(g);
   if constexpr (MIXED) {
     // reference point: the cell's own corner, block offset (1, 1, 1)
     const int64_t pr = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
-    const float2 *r = reinterpret_cast<const float2 *>(g.grid32) + pr * F;
 #pragma unroll
-    for (int f = 0; f < F; ++f) {
-      const float2 a = __ldg(r + f);
-      rhi[f] = a.x;
-      rlo[f] = a.y;
-    }
+    for (int f = 0; f < F; ++f) g32_load<F>(g.grid32, npts, pr, f, rhi[f], rlo[f]);
   }
   T acc[F], gx = 0, gy = 0, gz = 0;
 #pragma unroll
@@ -194,7 +189,7 @@ __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, 
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       T v[4][F];
-      load_row<F, MIXED, T>(g, ((c[2] + k) * ny + (c[1] + j)) * nx + c[0], rhi, rlo, v);
+      load_row<F, MIXED, T>(g, npts, ((c[2] + k) * ny + (c[1] + j)) * nx + c[0], rhi, rlo, v);
       T ax[F];
 #pragma unroll
       for (int f = 0; f < F; ++f)
@@ -258,17 +253,13 @@ __device__ __forceinline__ void eval_otf4(const arb_grid &g, const KParams &kp, 
     cr_dweights<T>((T)frac[a], dw[a]);
     hermite_slope<T>((T)frac[a], hb[a], dhb[a]);
   }
-  const float2 *g32 = reinterpret_cast<const float2 *>(g.grid32);
+  const int64_t npts = grid_points(g);
   const int64_t pref = (((c[3] + 1) * nz + (c[2] + 1)) * ny + (c[1] + 1)) * nx + (c[0] + 1);
 #pragma unroll 1
   for (int f = 0; f < F; ++f) {
     const bool gradf = (F != 3) && (f == F - 1);
     float rhi = 0.f, rlo = 0.f;
-    if constexpr (MIXED) {
-      const float2 a = __ldg(g32 + pref * F + f);
-      rhi = a.x;
-      rlo = a.y;
-    }
+    if constexpr (MIXED) g32_load<F>(g.grid32, npts, pref, f, rhi, rlo);
     T V = 0, Vg[4] = {0, 0, 0, 0};
     T S[16];
 #pragma unroll
@@ -290,8 +281,9 @@ __device__ __forceinline__ void eval_otf4(const arb_grid &g, const KParams &kp, 
 #pragma unroll
           for (int ii = 0; ii < 4; ++ii) {
             if constexpr (MIXED) {
-              const float2 a = __ldg(g32 + (p + ii) * F + f);
-              r[ii] = (a.x - rhi) + (a.y - rlo);
+              float h_, l_;
+              g32_load<F>(g.grid32, npts, p + ii, f, h_, l_);
+              r[ii] = (h_ - rhi) + (l_ - rlo);
             } else {
               r[ii] = __ldg(g.grid64 + (p + ii) * F + f);
             }

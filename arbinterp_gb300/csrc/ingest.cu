@@ -237,13 +237,14 @@ __global__ void __launch_bounds__(256) ingest_gather_kernel(const TF *field, int
       for (int f = 0; f < F; ++f) {
         split_f32(out[f], hi[f], lo[f]);
       }
+      // layout: see g32_load (arb_common.cuh)
       if (F == 4) {
-        reinterpret_cast<float4 *>(grid32)[dest * 2] = make_float4(hi[0], lo[0], hi[1 % F], lo[1 % F]);
-        reinterpret_cast<float4 *>(grid32)[dest * 2 + 1] = make_float4(hi[2 % F], lo[2 % F], hi[3 % F], lo[3 % F]);
+        reinterpret_cast<float4 *>(grid32)[dest] = make_float4(hi[0], hi[1 % F], hi[2 % F], hi[3 % F]);
+        grid32[npts * 4 + dest] = lo[3 % F];
+      } else if (F == 3) {
+        reinterpret_cast<float4 *>(grid32)[dest] = make_float4(hi[0], hi[1 % F], hi[2 % F], 0.f);
       } else {
-#pragma unroll
-        for (int f = 0; f < F; ++f)
-          reinterpret_cast<float2 *>(grid32)[dest * F + f] = make_float2(hi[f], lo[f]);
+        reinterpret_cast<float2 *>(grid32)[dest] = make_float2(hi[0], lo[0]);
       }
     }
     if (KIND == ARB_KIND_SCALAR && raw_out) raw_out[dest] = out[0];

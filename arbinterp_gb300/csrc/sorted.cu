@@ -192,84 +192,96 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
   write_vals<DIM, F>(o, i, val, grad);
 }
 
-// 3D, four fields ('both' mode), mixed precision: 8 lanes per query.  One
-// grid row (4 points x 4 fields x (hi, lo) float32 = 128 bytes) is read by 8
-// lanes with one 16-byte load each, so a warp load touches 4 rows instead of
-// 32 scattered lines.  Lane s of a query group holds point s>>1 and fields
-// 2(s&1), 2(s&1)+1; it contracts its 16 rows over y and z, then the 4 lanes
-// of a field pair reduce over x with two butterfly shuffles.
-// Each block walks COOP_CHUNK consecutive sorted queries (about one spatial
-// bin) so the bin's grid footprint stays in that SM's L1.
+// 3D, four fields ('both' mode), mixed precision: 4 lanes per query, lane
+// s owning grid point s of every x-row.  A row is 4 points x float4
+// (hi_x, hi_y, hi_z, hi_n) = 64 bytes plus 4 x float lo_n, so the 4 lanes of
+// a query read it with one 16-byte and one 4-byte load each.  Each lane
+// contracts its 16 rows over y and z (components from their float32 values
+// as deltas to the cell corner; |B| from (hi, lo) deltas so its gradient keeps
+// full precision), then the 4 lanes reduce over x with two butterfly
+// shuffles.  Each block walks COOP_CHUNK consecutive sorted queries (about
+// one spatial bin) so the bin's grid footprint stays in that SM's L1.
 constexpr int COOP_CHUNK = 256;
 
 __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KParams kp, int64_t nq,
                                                                 arb_query_out o, SortedWork w) {
   const int lane = threadIdx.x & 31;
-  const int sub = lane & 7, p = sub >> 1, fp = sub & 1;
+  const int p = lane & 3;
   const int64_t t0 = (int64_t)blockIdx.x * COOP_CHUNK;
   const int64_t t1 = min(t0 + COOP_CHUNK, nq);
-  for (int64_t t = t0 + (threadIdx.x >> 3); t < t1; t += blockDim.x >> 3) {  // groups stay converged
-  const int64_t code = w.s_code[t];
-  const int64_t i = w.s_row[t];
-  if (code < 0 || code == g.nc) {
-    if (sub == 0) write_const<3, 4>(o, i, (code < 0 || g.sentinel_nan) ? qnan() : 0.0);
-    continue;
-  }
-  const float *fr = reinterpret_cast<const float *>(w.s_frac) + t * 3;
-  const float fx = fr[0], fy = fr[1], fz = fr[2];
-  float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
-  cr_weights<float>(fx, wx);
-  cr_dweights<float>(fx, dx);
-  cr_weights<float>(fy, wy);
-  cr_dweights<float>(fy, dy);
-  cr_weights<float>(fz, wz);
-  cr_dweights<float>(fz, dz);
-  int64_t c[3];
-  cell_coords<3>(code, g, c);
   const int64_t nx = g.n[0], ny = g.n[1];
+  const int64_t npts = grid_points(g);
   const float4 *g4 = reinterpret_cast<const float4 *>(g.grid32);
-  const int64_t pref = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
-  const float4 ref = __ldg(g4 + pref * 2 + fp);
-  float S0 = 0.f, S1 = 0.f, Sy = 0.f, Sz = 0.f;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int64_t pt = ((c[2] + k) * ny + (c[1] + j)) * nx + c[0] + p;
-      const float4 v = __ldg(g4 + pt * 2 + fp);
-      const float d0 = (v.x - ref.x) + (v.y - ref.y);
-      const float d1 = (v.z - ref.z) + (v.w - ref.w);
-      const float wyz = wy[j] * wz[k];
-      S0 += wyz * d0;
-      S1 += wyz * d1;
-      Sy += (dy[j] * wz[k]) * d1;
-      Sz += (wy[j] * dz[k]) * d1;
+  const float *glo = g.grid32 + npts * 4;
+  const unsigned mask = 0xfu << (lane & 28);
+  for (int64_t t = t0 + (threadIdx.x >> 2); t < t1; t += blockDim.x >> 2) {  // groups stay converged
+    const int64_t code = w.s_code[t];
+    const int64_t i = w.s_row[t];
+    if (code < 0 || code == g.nc) {
+      if (p == 0) write_const<3, 4>(o, i, (code < 0 || g.sentinel_nan) ? qnan() : 0.0);
+      continue;
     }
-  }
-  float V0 = wx[p] * S0, V1 = wx[p] * S1, Gx = dx[p] * S1, Gy = wx[p] * Sy, Gz = wx[p] * Sz;
-  const unsigned mask = 0xffu << (lane & 24);
+    const float *fr = reinterpret_cast<const float *>(w.s_frac) + t * 3;
+    const float fx = fr[0], fy = fr[1], fz = fr[2];
+    float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
+    cr_weights<float>(fx, wx);
+    cr_dweights<float>(fx, dx);
+    cr_weights<float>(fy, wy);
+    cr_dweights<float>(fy, dy);
+    cr_weights<float>(fz, wz);
+    cr_dweights<float>(fz, dz);
+    int64_t c[3];
+    cell_coords<3>(code, g, c);
+    const int64_t pref = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
+    const float4 ref = __ldg(g4 + pref);
+    const float rlo = __ldg(glo + pref);
+    float Sx = 0.f, Sy_ = 0.f, Sz_ = 0.f, Sn = 0.f, Gy = 0.f, Gz = 0.f;
 #pragma unroll
-  for (int off = 2; off <= 4; off <<= 1) {
-    V0 += __shfl_xor_sync(mask, V0, off);
-    V1 += __shfl_xor_sync(mask, V1, off);
-    Gx += __shfl_xor_sync(mask, Gx, off);
-    Gy += __shfl_xor_sync(mask, Gy, off);
-    Gz += __shfl_xor_sync(mask, Gz, off);
-  }
-  if (sub == 0) {
-    if (o.comps) {
-      o.comps[i * 3 + 0] = f2d_exact(ref.x + (ref.y + V0));
-      o.comps[i * 3 + 1] = f2d_exact(ref.z + (ref.w + V1));
+    for (int k = 0; k < 4; ++k) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t pt = ((c[2] + k) * ny + (c[1] + j)) * nx + c[0] + p;
+        const float4 v = __ldg(g4 + pt);
+        const float lo = __ldg(glo + pt);
+        const float dn = (v.w - ref.w) + (lo - rlo);
+        const float wyz = wy[j] * wz[k];
+        Sx += wyz * (v.x - ref.x);
+        Sy_ += wyz * (v.y - ref.y);
+        Sz_ += wyz * (v.z - ref.z);
+        Sn += wyz * dn;
+        Gy += (dy[j] * wz[k]) * dn;
+        Gz += (wy[j] * dz[k]) * dn;
+      }
     }
-  } else if (sub == 1) {
-    if (o.comps) o.comps[i * 3 + 2] = f2d_exact(ref.x + (ref.y + V0));
-    if (o.norms) o.norms[i] = f2d_exact(ref.z + (ref.w + V1));
-    if (o.grads) {
-      o.grads[i * 3 + 0] = f2d_exact(Gx * kp.inv_hf[0]);
-      o.grads[i * 3 + 1] = f2d_exact(Gy * kp.inv_hf[1]);
-      o.grads[i * 3 + 2] = f2d_exact(Gz * kp.inv_hf[2]);
+    float Vx = wx[p] * Sx, Vy = wx[p] * Sy_, Vz = wx[p] * Sz_, Vn = wx[p] * Sn;
+    float Gx = dx[p] * Sn;
+    Gy *= wx[p];
+    Gz *= wx[p];
+#pragma unroll
+    for (int off = 1; off <= 2; off <<= 1) {
+      Vx += __shfl_xor_sync(mask, Vx, off);
+      Vy += __shfl_xor_sync(mask, Vy, off);
+      Vz += __shfl_xor_sync(mask, Vz, off);
+      Vn += __shfl_xor_sync(mask, Vn, off);
+      Gx += __shfl_xor_sync(mask, Gx, off);
+      Gy += __shfl_xor_sync(mask, Gy, off);
+      Gz += __shfl_xor_sync(mask, Gz, off);
     }
-  }
+    if (p == 0) {
+      if (o.comps) {
+        o.comps[i * 3 + 0] = f2d_exact(ref.x + Vx);
+        o.comps[i * 3 + 1] = f2d_exact(ref.y + Vy);
+        o.comps[i * 3 + 2] = f2d_exact(ref.z + Vz);
+      }
+    } else if (p == 1) {
+      if (o.norms) o.norms[i] = f2d_exact(ref.w + (rlo + Vn));
+    } else if (p == 2) {
+      if (o.grads) {
+        o.grads[i * 3 + 0] = f2d_exact(Gx * kp.inv_hf[0]);
+        o.grads[i * 3 + 1] = f2d_exact(Gy * kp.inv_hf[1]);
+        o.grads[i * 3 + 2] = f2d_exact(Gz * kp.inv_hf[2]);
+      }
+    }
   }
 }
 

@@ -161,7 +161,10 @@ class _Interpolant:
         self._npts = npts
         kind, F = self._kind, self._F
         grid64 = torch.empty(npts * F, dtype=torch.float64, device=dev)
-        grid32 = torch.empty(npts * F * 2, dtype=torch.float32, device=dev) if self.precision == "mixed" else None
+        # mixed-precision grid: F=1 (hi, lo); F=3 float4 of hi; F=4 float4 of hi + lo of |B|
+        g32_floats = {1: 2, 3: 4, 4: 5}[F]
+        grid32 = (torch.empty(npts * g32_floats, dtype=torch.float32, device=dev)
+                  if self.precision == "mixed" else None)
         raw = torch.empty(npts * 3, dtype=torch.float64, device=dev) if kind == _lib.KIND_NORM else None
         claim = torch.empty(npts, dtype=torch.int32, device=dev)
         n_c = (ctypes.c_int64 * 4)(*(n + [1] * (4 - dim)))

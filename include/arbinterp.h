@@ -12,7 +12,11 @@
  *
  * Data layout in device memory (see arb_grid):
  *   grid64  [npts][F] float64, points z-major with x fastest (t slowest in 4D)
- *   grid32  [npts][F][2] float32 (hi, lo) with hi + lo == value to ~2^-48
+ *   grid32  float32 split, hi = RN(v), lo = RN(v - hi):
+ *             F = 1: [npts] (hi, lo)
+ *             F = 3: [npts] (hi_x, hi_y, hi_z, 0)        (values only)
+ *             F = 4: [npts] (hi_x, hi_y, hi_z, hi_n), then [npts] lo_n
+ *           only the field whose gradient is returned keeps its residual
  *   table   [nc][F][M] coefficients (M = 64 in 3D, 256 in 4D), float64 or
  *           float32, monomial index ex + 4 ey + 16 ez (+ 64 et)
  * F (fields) is 1 for scalar and norm modes, 3 for vector mode and 4 for
@@ -69,7 +73,7 @@ typedef struct arb_grid {
   double hi[4];         /* xIntMax.. : second-to-last grid coordinate       */
   double h[4];          /* spacing from the first two axis samples          */
   const double *grid64; /* [npts][F]                                        */
-  const float *grid32;  /* [npts][F][2] or NULL                             */
+  const float *grid32;  /* mixed-precision split (layout above) or NULL   */
   const void *table;    /* [nc][F][M] or NULL                               */
   int32_t table_prec;   /* enum arb_precision of table (FP64: double)      */
   int32_t reserved;
@@ -93,8 +97,9 @@ typedef struct arb_query_out {
 /* Scratch bytes arb_ingest_axes needs in `work`. */
 size_t arb_ingest_axes_work_bytes(int32_t dim);
 
-/* Finds each axis' sample values (points on the axis lines through the
- * lexicographically smallest point), sorted ascending.  Writes
+/* Finds each axis' sample values (points on the axis lines through row 0;
+ * for a full tensor grid these equal the reference's lines through its
+ * first sorted row), sorted ascending.  Writes
  * axis_out[a * axis_cap + i] and axis_count[a] (device).  axis_out holds
  * 2 * dim * axis_cap doubles: the second half stages the unsorted lists.
  * field is [npts][ncol] float64 (field_is_f32 == 0) or float32. */
