@@ -53,7 +53,32 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--kernel-only", action="store_true", help="time only the query kernel (profiling)")
+    p.add_argument("--profile", default=None, choices=["step", "small", "small-table", "small-fp64"],
+                   help="run a fixed workload for an ncu capture and exit (no timing, no JSON): "
+                        "'step' = two full bench steps; 'small*' = 160^3 dipole field, 2.02e6 queries")
     return p.parse_args()
+
+
+def run_profile(args):
+    """Workloads for ncu captures (profiles/ cites these command lines)."""
+    import torch
+    from arbinterp_gb300 import tricubic, synth
+    dev = torch.device("cuda")
+    if args.profile == "step":
+        field, q, lo, hi, h = make_workload(dev)
+        for _ in range(2):
+            tricubic(field, "quiet", mode="both", precision=args.precision, strategy=args.strategy).Query(q)
+    else:
+        prec = "fp64" if args.profile == "small-fp64" else "mixed"
+        strategy = "table" if args.profile == "small-table" else "otf"
+        field = synth.dipole_field3(n=(160, 160, 160), seed=1, device=dev)
+        o = tricubic(field, "quiet", mode="both", precision=prec, strategy=strategy)
+        q = synth.uniform_queries([o.xIntMin, o.yIntMin, o.zIntMin], [o.xIntMax, o.yIntMax, o.zIntMax],
+                                  2_000_000, 20_000, [o.hx, o.hy, o.hz], seed=3, device=dev)
+        for _ in range(2):
+            o.Query(q)
+    torch.cuda.synchronize()
+    print("profile workload done")
 
 
 # ---------------------------------------------------------------- clocks
@@ -250,6 +275,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile(args)
     import numpy as np
     import torch
     import torch.distributed as dist
