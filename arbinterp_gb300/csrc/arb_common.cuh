@@ -60,6 +60,7 @@ __device__ __forceinline__ void hermite_slope(T t, T hb[2], T dhb[2]) {
 // be the IEEE one so floors (hence cell indices) are bit-exact.
 struct CoordStep {
   int64_t idx;       // flat cell index, as the reference computes it
+  int64_t fl[4];     // per-axis floors (valid when !oob && !nan)
   bool oob;          // some coordinate outside [lo, hi]  -> row written NaN
   bool nan;          // some coordinate NaN (row not rewritten, outputs NaN)
 };
@@ -96,6 +97,8 @@ __device__ __forceinline__ CoordStep coord_step(const double *qrow, const arb_gr
     frac[a] = iu - k;
     fl[a] = (int64_t)k;
   }
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) s.fl[a] = fl[a];
   if (s.oob || s.nan) {
     s.idx = g.nc;
     return s;
@@ -175,6 +178,8 @@ __device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const F
     fl[a] = kk;
     frac[a] = fr;
   }
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) s.fl[a] = fl[a];
   if (s.oob || s.nan) {
     s.idx = g.nc;
     return s;
@@ -211,6 +216,54 @@ __device__ __forceinline__ void cell_coords(int64_t idx, const arb_grid &g, int6
     idx /= m;
   }
   c[DIM - 1] = idx;
+}
+
+// ---- packed cell coordinates (bin-ordered query records) -------------------
+// 21 bits per axis in 3D, 15 in 4D; bit 63 marks a row that needs no
+// evaluation (low bits 0: NaN row; 1: in-volume row whose flat index equals
+// nc, the reference's sentinel column).
+constexpr unsigned long long CELL_SPECIAL = 1ULL << 63;
+template <int DIM>
+__host__ __device__ constexpr int cell_bits() { return DIM == 3 ? 21 : 15; }
+
+template <int DIM>
+__device__ __forceinline__ unsigned long long pack_cell(const int64_t c[DIM]) {
+  unsigned long long w = 0;
+#pragma unroll
+  for (int a = DIM - 1; a >= 0; --a) w = (w << cell_bits<DIM>()) | (unsigned long long)c[a];
+  return w;
+}
+template <int DIM>
+__device__ __forceinline__ void unpack_cell(unsigned long long w, int64_t c[DIM]) {
+  const unsigned long long m = (1ULL << cell_bits<DIM>()) - 1;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    c[a] = (int64_t)(w & m);
+    w >>= cell_bits<DIM>();
+  }
+}
+// Flat cell index from coordinates (no division).
+template <int DIM>
+__device__ __forceinline__ int64_t flat_cell(const int64_t c[DIM], const arb_grid &g) {
+  int64_t idx = c[DIM - 1];
+#pragma unroll
+  for (int a = DIM - 2; a >= 0; --a) idx = idx * (g.n[a] - 3) + c[a];
+  return idx;
+}
+// Cell coordinates of an in-volume step: the floors themselves, unless one
+// sits on an upper face (floor == cells on that axis), where the reference's
+// flat index aliases onto another cell and is decoded.
+template <int DIM>
+__device__ __forceinline__ void cell_from_step(const CoordStep &s, const arb_grid &g, int64_t c[DIM]) {
+  bool face = false;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) face |= s.fl[a] >= g.n[a] - 3;
+  if (face) {
+    cell_coords<DIM>(s.idx, g, c);
+  } else {
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) c[a] = s.fl[a];
+  }
 }
 
 __device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000LL); }

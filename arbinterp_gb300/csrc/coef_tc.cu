@@ -217,13 +217,15 @@ int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *tabl
   const size_t smem = sizeof(TcSmem) + 1024;
   static bool attr = false;
   if (!attr) {
-    if (cudaFuncSetAttribute(coef3_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(coef3_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(coef3_tc_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-      return ARB_ERR_CUDA;
+    // prefer the largest shared-memory carveout so several CTAs share an SM
+    // (their gathers overlap each other's MMAs and epilogues)
+    const void *ks[3] = {(const void *)coef3_tc_kernel<1>, (const void *)coef3_tc_kernel<3>,
+                         (const void *)coef3_tc_kernel<4>};
+    for (const void *k : ks) {
+      if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+          cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+        return ARB_ERR_CUDA;
+    }
     attr = true;
   }
   const int64_t rows = ncells * g->nfield;

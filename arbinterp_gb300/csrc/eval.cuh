@@ -153,13 +153,11 @@ __device__ __forceinline__ void load_row(const arb_grid &g, int64_t npts, int64_
 
 // ---- 3D on-the-fly ---------------------------------------------------------
 template <int F, bool MIXED>
-__device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, int64_t idx,
+__device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, const int64_t c[3],
                                           const typename std::conditional<MIXED, float, double>::type frac[3],
                                           double val[F], double grad[3]) {
   using T = typename std::conditional<MIXED, float, double>::type;
   constexpr bool GRAD = (F != 3);
-  int64_t c[3];
-  cell_coords<3>(idx, g, c);
   const int64_t nx = g.n[0], ny = g.n[1];
   T wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
   cr_weights<T>((T)frac[0], wx);
@@ -239,12 +237,11 @@ __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, 
 // reference's A minus kron(A1,A1,A1,A1) (D row 240 zero, rows 241..255
 // shifted by one corner).
 template <int F, bool MIXED>
-__device__ __forceinline__ void eval_otf4(const arb_grid &g, const KParams &kp, int64_t idx,
+__device__ __forceinline__ void eval_otf4(const arb_grid &g, const KParams &kp, const int64_t c[4],
                                           const typename std::conditional<MIXED, float, double>::type frac[4],
                                           double val[F], double grad[4]) {
   using T = typename std::conditional<MIXED, float, double>::type;
-  int64_t c[4];
-  cell_coords<4>(idx, g, c);
+
   const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
   T w[4][4], dw[4][4], hb[4][2], dhb[4][2];
 #pragma unroll
@@ -395,11 +392,12 @@ __device__ __forceinline__ void load4(const T *p, T a[4]) {
 }
 
 template <int DIM, int F, bool MIXED>
-__device__ __forceinline__ void eval_tab(const arb_grid &g, const KParams &kp, int64_t idx,
+__device__ __forceinline__ void eval_tab(const arb_grid &g, const KParams &kp, const int64_t c[DIM],
                                          const typename std::conditional<MIXED, float, double>::type x[DIM],
                                          double val[F], double grad[DIM]) {
   using T = typename std::conditional<MIXED, float, double>::type;
   constexpr int M = DIM == 3 ? 64 : 256;
+  const int64_t idx = flat_cell<DIM>(c, g);
   const T *tab = reinterpret_cast<const T *>(g.table) + idx * (int64_t)F * M;
 #pragma unroll 1
   for (int f = 0; f < F; ++f) {

@@ -31,7 +31,9 @@ __global__ void __launch_bounds__(256) otf3_kernel(arb_grid g, KParams kp, doubl
   if (!query_prologue<3, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac_, idx)) return;
   const T fr[3] = {frac_[0], frac_[1], frac_[2]};
   double val[F], grad[3];
-  eval_otf3<F, MIXED>(g, kp, idx, fr, val, grad);
+  int64_t c[3];
+  cell_coords<3>(idx, g, c);
+  eval_otf3<F, MIXED>(g, kp, c, fr, val, grad);
   write_vals<3, F>(o, i, val, grad);
 }
 
@@ -47,7 +49,9 @@ __global__ void __launch_bounds__(128) otf4_kernel(arb_grid g, KParams kp, doubl
   if (!query_prologue<4, F, !MIXED>(g, kp, q, i, qs, wb, o, status, frac_, idx)) return;
   const T fr[4] = {frac_[0], frac_[1], frac_[2], frac_[3]};
   double val[F], grad[4] = {0, 0, 0, 0};
-  eval_otf4<F, MIXED>(g, kp, idx, fr, val, grad);
+  int64_t c[4];
+  cell_coords<4>(idx, g, c);
+  eval_otf4<F, MIXED>(g, kp, c, fr, val, grad);
   write_vals<4, F>(o, i, val, grad);
 }
 
@@ -62,7 +66,9 @@ __global__ void __launch_bounds__(256) tab_kernel(arb_grid g, KParams kp, double
   int64_t idx;
   if (!query_prologue<DIM, F, !MIXED>(g, kp, q, i, qs, wb, o, status, x, idx)) return;
   double val[F], grad[DIM];
-  eval_tab<DIM, F, MIXED>(g, kp, idx, x, val, grad);
+  int64_t c[DIM];
+  cell_coords<DIM>(idx, g, c);
+  eval_tab<DIM, F, MIXED>(g, kp, c, x, val, grad);
   write_vals<DIM, F>(o, i, val, grad);
 }
 

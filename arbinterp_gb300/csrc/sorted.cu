@@ -8,26 +8,27 @@
 //
 //   locate   : float64 cell index + fractional offset (exactly the
 //              reference's iu = (q - IntMin)/h, floor, flat index), the
-//              out-of-volume bookkeeping of rQuery (NaN rows, queryInds), and
-//              bin id + rank within the bin (atomic histogram)
+//              out-of-volume bookkeeping of rQuery (NaN rows, queryInds), the
+//              packed cell coordinates, and bin id + rank within the bin
+//              (atomic histogram)
 //   scan     : exclusive prefix sum of the bin histogram
-//   scatter  : records (code, row, frac) into bin order
+//   scatter  : records (packed cell, row, frac) into bin order
 //   evaluate : on-the-fly or table evaluation in bin order, outputs written
 //              to the query's original row
 // The float64 index step runs once per query; the evaluation pass does no
-// float64 arithmetic in mixed precision.
+// float64 arithmetic and no integer division in mixed precision.
 #include "eval.cuh"
 
 namespace arb {
 
 struct SortedWork {
-  uint32_t *hist;    // nbins + 1 (exclusive offsets after the scan)
-  uint2 *binrank;    // nq
-  int64_t *code;     // nq: cell index, nc = sentinel, -1 = NaN row
-  void *frac;        // nq * DIM values of T
-  int64_t *s_code;   // nq, bin order
-  int64_t *s_row;    // nq
-  void *s_frac;      // nq * DIM
+  uint32_t *hist;              // nbins + 1 (exclusive offsets after the scan)
+  uint2 *binrank;              // nq
+  unsigned long long *cell;    // nq: packed cell (or CELL_SPECIAL | code)
+  void *frac;                  // nq * DIM values of T
+  unsigned long long *s_cell;  // nq, bin order
+  uint32_t *s_row;             // nq
+  void *s_frac;                // nq * DIM
 };
 
 struct BinGeom {
@@ -67,10 +68,10 @@ static size_t carve(SortedWork *w, void *base, const arb_grid *g, int precision,
   SortedWork t;
   t.hist = (uint32_t *)take(sizeof(uint32_t) * (bg.nbins + 1));
   t.binrank = (uint2 *)take(sizeof(uint2) * nq);
-  t.code = (int64_t *)take(sizeof(int64_t) * nq);
+  t.cell = (unsigned long long *)take(sizeof(unsigned long long) * nq);
   t.frac = take(tsz * g->dim * nq);
-  t.s_code = (int64_t *)take(sizeof(int64_t) * nq);
-  t.s_row = (int64_t *)take(sizeof(int64_t) * nq);
+  t.s_cell = (unsigned long long *)take(sizeof(unsigned long long) * nq);
+  t.s_row = (uint32_t *)take(sizeof(uint32_t) * nq);
   t.s_frac = take(tsz * g->dim * nq);
   if (w) *w = t;
   return off;
@@ -96,26 +97,26 @@ __global__ void __launch_bounds__(256) locate_kernel(arb_grid g, KParams kp, Bin
   if (s.oob && wb)
     for (int64_t c = 0; c < qs; ++c) qr[c] = qnan();
   if (o.inds) o.inds[i] = s.idx;
-  int64_t code;
+  unsigned long long cw;
   int64_t bin = bg.nbins;
   if (s.oob || s.nan) {
-    code = -1;
+    cw = CELL_SPECIAL;
   } else if (s.idx > g.nc) {
     set_status(status, ARB_ERR_CELL_INDEX);
-    code = -1;
+    cw = CELL_SPECIAL;
   } else if (s.idx == g.nc) {
-    code = g.nc;
+    cw = CELL_SPECIAL | 1ULL;
   } else {
-    code = s.idx;
     int64_t c[DIM];
-    cell_coords<DIM>(s.idx, g, c);
+    cell_from_step<DIM>(s, g, c);
+    cw = pack_cell<DIM>(c);
     bin = c[DIM - 1] >> bg.shift;
 #pragma unroll
     for (int a = DIM - 2; a >= 0; --a) bin = bin * bg.nb[a] + (c[a] >> bg.shift);
   }
   const uint32_t rank = atomicAdd(&w.hist[bin], 1u);
   w.binrank[i] = make_uint2((uint32_t)bin, rank);
-  w.code[i] = code;
+  w.cell[i] = cw;
   T *fr = reinterpret_cast<T *>(w.frac) + i * DIM;
 #pragma unroll
   for (int a = 0; a < DIM; ++a) fr[a] = frac[a];
@@ -150,8 +151,8 @@ __global__ void __launch_bounds__(256) scatter_kernel(int64_t nq, SortedWork w) 
   if (i >= nq) return;
   const uint2 br = w.binrank[i];
   const int64_t pos = (int64_t)w.hist[br.x] + br.y;
-  w.s_code[pos] = w.code[i];
-  w.s_row[pos] = i;
+  w.s_cell[pos] = w.cell[i];
+  w.s_row[pos] = (uint32_t)i;
   const T *src = reinterpret_cast<const T *>(w.frac) + i * DIM;
   T *dst = reinterpret_cast<T *>(w.s_frac) + pos * DIM;
 #pragma unroll
@@ -165,16 +166,14 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
   using T = typename std::conditional<MIXED, float, double>::type;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nq) return;
-  const int64_t code = w.s_code[t];
+  const unsigned long long cw = w.s_cell[t];
   const int64_t i = w.s_row[t];
-  if (code < 0) {
-    write_const<DIM, F>(o, i, qnan());
+  if (cw & CELL_SPECIAL) {
+    write_const<DIM, F>(o, i, (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
     return;
   }
-  if (code == g.nc) {
-    write_const<DIM, F>(o, i, g.sentinel_nan ? qnan() : 0.0);
-    return;
-  }
+  int64_t c[DIM];
+  unpack_cell<DIM>(cw, c);
   T fr[DIM];
   const T *src = reinterpret_cast<const T *>(w.s_frac) + t * DIM;
 #pragma unroll
@@ -183,11 +182,11 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
 #pragma unroll
   for (int a = 0; a < DIM; ++a) grad[a] = 0.0;
   if constexpr (TABLE) {
-    eval_tab<DIM, F, MIXED>(g, kp, code, fr, val, grad);
+    eval_tab<DIM, F, MIXED>(g, kp, c, fr, val, grad);
   } else if constexpr (DIM == 3) {
-    eval_otf3<F, MIXED>(g, kp, code, fr, val, grad);
+    eval_otf3<F, MIXED>(g, kp, c, fr, val, grad);
   } else {
-    eval_otf4<F, MIXED>(g, kp, code, fr, val, grad);
+    eval_otf4<F, MIXED>(g, kp, c, fr, val, grad);
   }
   write_vals<DIM, F>(o, i, val, grad);
 }
@@ -215,12 +214,14 @@ __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KPar
   const float *glo = g.grid32 + npts * 4;
   const unsigned mask = 0xfu << (lane & 28);
   for (int64_t t = t0 + (threadIdx.x >> 2); t < t1; t += blockDim.x >> 2) {  // groups stay converged
-    const int64_t code = w.s_code[t];
+    const unsigned long long cw = w.s_cell[t];
     const int64_t i = w.s_row[t];
-    if (code < 0 || code == g.nc) {
-      if (p == 0) write_const<3, 4>(o, i, (code < 0 || g.sentinel_nan) ? qnan() : 0.0);
+    if (cw & CELL_SPECIAL) {
+      if (p == 0) write_const<3, 4>(o, i, (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
       continue;
     }
+    int64_t c[3];
+    unpack_cell<3>(cw, c);
     const float *fr = reinterpret_cast<const float *>(w.s_frac) + t * 3;
     const float fx = fr[0], fy = fr[1], fz = fr[2];
     float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
@@ -230,8 +231,6 @@ __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KPar
     cr_dweights<float>(fy, dy);
     cr_weights<float>(fz, wz);
     cr_dweights<float>(fz, dz);
-    int64_t c[3];
-    cell_coords<3>(code, g, c);
     const int64_t pref = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
     const float4 ref = __ldg(g4 + pref);
     const float rlo = __ldg(glo + pref);
@@ -327,6 +326,9 @@ extern "C" int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32
   if (nq == 0) return ARB_OK;
   if (!work || !status) return ARB_ERR_INVALID;
   if (nq >= (int64_t)1 << 32) return ARB_ERR_UNSUPPORTED;
+  const int bits = g->dim == 3 ? cell_bits<3>() : cell_bits<4>();
+  for (int a = 0; a < g->dim; ++a)
+    if (g->n[a] - 3 >= ((int64_t)1 << bits)) return ARB_ERR_UNSUPPORTED;  // cells per axis
   const bool mixed = precision == ARB_PREC_MIXED;
   if (use_table) {
     if (!g->table || g->table_prec != precision) return ARB_ERR_INVALID;
