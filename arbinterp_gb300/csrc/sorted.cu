@@ -17,6 +17,8 @@
 //              to the query's original row
 // The float64 index step runs once per query; the evaluation pass does no
 // float64 arithmetic and no integer division in mixed precision.
+#include <mutex>
+
 #include "eval.cuh"
 
 namespace arb {
@@ -312,6 +314,37 @@ static void launch_sorted(const arb_grid *g, const KParams &kp, const BinGeom &b
 
 using namespace arb;
 
+// ---- allocation-free variant --------------------------------------------------
+// Scratch of arb_query_eval_sorted_noalloc: a file-scope device array that
+// every GPU which loads this library holds until the process exits.  Host code
+// must not pass the symbol itself to a kernel (on the host it is only a
+// stand-in); its device address is looked up once per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[ARB_NOALLOC_SCRATCH_BYTES];
+
+static void *noalloc_scratch(int *rc) {
+  static std::mutex mu;
+  static void *ptrs[64] = {};
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    *rc = ARB_ERR_CUDA;
+    return nullptr;
+  }
+  if (dev < 0 || dev >= 64) {
+    *rc = ARB_ERR_UNSUPPORTED;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!ptrs[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+      *rc = ARB_ERR_CUDA;
+      return nullptr;
+    }
+    ptrs[dev] = p;
+  }
+  return ptrs[dev];
+}
+
 extern "C" size_t arb_query_sorted_work_bytes(const arb_grid *g, int32_t precision, int64_t nq) {
   if (!g || nq < 0 || (g->dim != 3 && g->dim != 4)) return 0;
   return carve(nullptr, nullptr, g, precision, nq);
@@ -349,4 +382,20 @@ extern "C" int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32
     else launch_sorted<4, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
   }
   return launch_status();
+}
+
+extern "C" int arb_query_eval_sorted_noalloc(const arb_grid *g, int32_t precision, int32_t use_table,
+                                             double *q, int64_t nq, int64_t q_stride, int32_t q_writeback,
+                                             const arb_query_out *out, int32_t *status,
+                                             arb_stream_t stream) {
+  if (!g || nq < 0) return ARB_ERR_INVALID;
+  if (nq == 0) return ARB_OK;
+  const size_t need = arb_query_sorted_work_bytes(g, precision, nq);
+  if (need == 0) return ARB_ERR_INVALID;
+  if (need > (size_t)ARB_NOALLOC_SCRATCH_BYTES) return ARB_ERR_CAPACITY;
+  int rc = ARB_OK;
+  void *ws = noalloc_scratch(&rc);
+  if (!ws) return rc;
+  return arb_query_eval_sorted(g, precision, use_table, q, nq, q_stride, q_writeback, out, ws, need,
+                               status, stream);
 }

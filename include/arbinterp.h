@@ -168,6 +168,34 @@ int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32_t use_tabl
                           const arb_query_out *out, void *work, size_t work_bytes,
                           int32_t *status, arb_stream_t stream);
 
+/* ---- allocation-free cell-grouped evaluation.  No counterpart in the
+ *      reference (which has no device memory at all).
+ *
+ *      For callers that cannot allocate device memory while they run: hosts
+ *      that own every device byte through their own pool (simulation or
+ *      rendering engines), plugin hosts that forbid allocation inside
+ *      callbacks, and long-running services that must not grow or fragment
+ *      device memory mid-run.  Same contract as arb_query_eval_sorted, but the
+ *      scratch is a fixed array inside the library: ARB_NOALLOC_SCRATCH_BYTES
+ *      on every GPU that loads the library, held until the process exits.
+ *      Calls whose scratch need (arb_query_sorted_work_bytes) exceeds it
+ *      return ARB_ERR_CAPACITY without touching the GPU — about 2e5 query
+ *      rows per call in float64 and 3e5 in mixed precision on a 256^3 grid;
+ *      split larger query sets into several calls.
+ *
+ *      The first call on a device looks up the array's device address (once
+ *      per device, with that device current); make that first call before
+ *      any stream capture.  Nothing is allocated: no cudaMalloc, no
+ *      cudaFree, no allocating library call.  Every call shares the one
+ *      array and leaves its contents behind; each call clears what must start
+ *      at zero.  Calls that overlap on the GPU (other streams, other host
+ *      threads) race on the array and must be serialised by the caller. */
+#define ARB_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+int arb_query_eval_sorted_noalloc(const arb_grid *g, int32_t precision, int32_t use_table,
+                                  double *q, int64_t nq, int64_t q_stride, int32_t q_writeback,
+                                  const arb_query_out *out, int32_t *status, arb_stream_t stream);
+
 /* Reads (and clears) the device status word after the stream's work is
  * done; returns ARB_OK, an arb_status bit set, or ARB_ERR_CUDA. */
 int arb_status_fetch(int32_t *status, arb_stream_t stream);
