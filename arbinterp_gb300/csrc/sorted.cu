@@ -287,15 +287,20 @@ __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KPar
 }
 
 template <int DIM, bool MIXED>
-static void launch_sorted(const arb_grid *g, const KParams &kp, const BinGeom &bg, double *q, int64_t nq,
-                          int64_t qs, int wb, const arb_query_out *out, int32_t *status,
-                          const SortedWork &w, bool table, cudaStream_t s) {
+static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, double *q, int64_t nq,
+                       int64_t qs, int wb, const arb_query_out *out, int32_t *status, const SortedWork &w,
+                       cudaStream_t s) {
   using T = typename std::conditional<MIXED, float, double>::type;
   const int TB = 256;
   const unsigned B = (unsigned)((nq + TB - 1) / TB);
   locate_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, wb, *out, status, w);
   scan_kernel<<<1, 1024, 0, s>>>(w.hist, bg.nbins + 1);
   scatter_kernel<DIM, T><<<B, TB, 0, s>>>(nq, w);
+}
+
+template <int DIM, bool MIXED>
+static void launch_eval(const arb_grid *g, const KParams &kp, int64_t nq, const arb_query_out *out,
+                        const SortedWork &w, bool table, cudaStream_t s) {
   const int TE = DIM == 3 ? 256 : 128;
   const unsigned BE = (unsigned)((nq + TE - 1) / TE);
 #define ES(FF, TAB) eval_sorted_kernel<DIM, FF, MIXED, TAB><<<BE, TE, 0, s>>>(*g, kp, nq, *out, w)
@@ -375,11 +380,80 @@ extern "C" int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32
   if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nbins + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
   const KParams kp = make_kparams(g);
   if (g->dim == 3) {
-    if (mixed) launch_sorted<3, true>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
-    else launch_sorted<3, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
+    if (mixed) {
+      launch_bin<3, true>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, s);
+      launch_eval<3, true>(g, kp, nq, out, w, use_table, s);
+    } else {
+      launch_bin<3, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, s);
+      launch_eval<3, false>(g, kp, nq, out, w, use_table, s);
+    }
   } else {
-    if (mixed) launch_sorted<4, true>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
-    else launch_sorted<4, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, use_table, s);
+    if (mixed) {
+      launch_bin<4, true>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, s);
+      launch_eval<4, true>(g, kp, nq, out, w, use_table, s);
+    } else {
+      launch_bin<4, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, s);
+      launch_eval<4, false>(g, kp, nq, out, w, use_table, s);
+    }
+  }
+  return launch_status();
+}
+
+// Binning only: the first half of arb_query_eval_sorted.  The workspace then
+// holds the bin-ordered records, which depend on the query points and the
+// grid geometry but not on the field values.
+extern "C" int arb_query_bin(const arb_grid *g, int32_t precision, double *q, int64_t nq, int64_t q_stride,
+                             int32_t q_writeback, const arb_query_out *out, void *work, size_t work_bytes,
+                             int32_t *status, arb_stream_t stream) {
+  int rc = check_query_args(g, q, nq, q_stride, out);
+  if (rc) return rc;
+  if (nq == 0) return ARB_OK;
+  if (!work || !status) return ARB_ERR_INVALID;
+  if (nq >= (int64_t)1 << 32) return ARB_ERR_UNSUPPORTED;
+  const int bits = g->dim == 3 ? cell_bits<3>() : cell_bits<4>();
+  for (int a = 0; a < g->dim; ++a)
+    if (g->n[a] - 3 >= ((int64_t)1 << bits)) return ARB_ERR_UNSUPPORTED;
+  SortedWork w;
+  if (carve(&w, work, g, precision, nq) > work_bytes) return ARB_ERR_INVALID;
+  const BinGeom bg = bin_geom(g);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nbins + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
+  const KParams kp = make_kparams(g);
+  const bool mixed = precision == ARB_PREC_MIXED;
+  if (g->dim == 3) {
+    if (mixed) launch_bin<3, true>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, s);
+    else launch_bin<3, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, s);
+  } else {
+    if (mixed) launch_bin<4, true>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, s);
+    else launch_bin<4, false>(g, kp, bg, q, nq, q_stride, q_writeback, out, status, w, s);
+  }
+  return launch_status();
+}
+
+// Evaluation only, from a workspace filled by arb_query_bin for the same
+// query rows and a grid of the same geometry (values may differ).
+extern "C" int arb_query_eval_binned(const arb_grid *g, int32_t precision, int32_t use_table, int64_t nq,
+                                     const arb_query_out *out, void *work, size_t work_bytes,
+                                     arb_stream_t stream) {
+  if (!g || !out || nq < 0 || (g->dim != 3 && g->dim != 4)) return ARB_ERR_INVALID;
+  if (nq == 0) return ARB_OK;
+  if (!work) return ARB_ERR_INVALID;
+  const bool mixed = precision == ARB_PREC_MIXED;
+  if (use_table) {
+    if (!g->table || g->table_prec != precision) return ARB_ERR_INVALID;
+  } else if (mixed ? !g->grid32 : !g->grid64) {
+    return ARB_ERR_INVALID;
+  }
+  SortedWork w;
+  if (carve(&w, work, g, precision, nq) > work_bytes) return ARB_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  const KParams kp = make_kparams(g);
+  if (g->dim == 3) {
+    if (mixed) launch_eval<3, true>(g, kp, nq, out, w, use_table, s);
+    else launch_eval<3, false>(g, kp, nq, out, w, use_table, s);
+  } else {
+    if (mixed) launch_eval<4, true>(g, kp, nq, out, w, use_table, s);
+    else launch_eval<4, false>(g, kp, nq, out, w, use_table, s);
   }
   return launch_status();
 }

@@ -321,19 +321,35 @@ def main():
     dt = tmax(dt)
     value = world * nq * args.steps / dt
 
-    # per-launch time of the query kernel alone (the dominant kernel)
+    # The dominant kernel is the evaluation pass over the bin-ordered records
+    # (46% of the step in the ncu launch list).  Bin the queries once, then
+    # time the evaluation launch alone on the launching stream.
+    from arbinterp_gb300 import _lib as LB
+    L = LB.lib()
     o = tricubic(field, "quiet", mode="both", precision=prec, strategy=strat)
     use_tab = o._use_table()
-    kt = cuda_time(lambda: o._run(q, nq, 3, False, False), 5, 2) / 5
-    F = 4
-    grid_bytes = o._npts * F * (8 if prec == "mixed" else 8)
-    io_bytes = nq * (3 * 8 + 7 * 8 + 8)
-    if use_tab:
-        algo = nq * F * 64 * (4 if prec == "mixed" else 8) + io_bytes
-        kname = "tab_kernel<3,4>"
-    else:
-        algo = grid_bytes + io_bytes
-        kname = "otf3_kernel<4,%s>" % ("true" if prec == "mixed" else "false")
+    pc = LB.PREC_MIXED if prec == "mixed" else LB.PREC_FP64
+    need = int(L.arb_query_sorted_work_bytes(o._g, pc, nq))
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    f64 = dict(dtype=torch.float64, device=dev)
+    oc, on, og = torch.empty((nq, 3), **f64), torch.empty((nq, 1), **f64), torch.empty((nq, 3), **f64)
+    oi = torch.empty(nq, dtype=torch.int64, device=dev)
+    st = torch.zeros(1, dtype=torch.int32, device=dev)
+    qo = LB.ArbQueryOut(oc.data_ptr(), on.data_ptr(), og.data_ptr(), oi.data_ptr(), None, None)
+    sp = torch.cuda.current_stream().cuda_stream
+    LB.check(L.arb_query_bin(o._g, pc, q.clone().data_ptr(), nq, 3, 0, qo, ws.data_ptr(), need,
+                             st.data_ptr(), sp), "arb_query_bin")
+    kt = cuda_time(lambda: L.arb_query_eval_binned(o._g, pc, int(use_tab), nq, qo, ws.data_ptr(), need, sp),
+                   5, 2) / 5
+    rec = 8 + 4 + 3 * (4 if prec == "mixed" else 8)          # packed cell, row, fraction
+    grid_bytes = o._npts * (20 if prec == "mixed" else 32)    # grid read once (compulsory)
+    algo = nq * (rec + 7 * 8) + (nq * 4 * 64 * (4 if prec == "mixed" else 8) if use_tab else grid_bytes)
+    kname = ("eval_sorted_kernel<3,4,table>" if use_tab else
+             ("eval_sorted_coop4_kernel" if prec == "mixed" else "eval_sorted_kernel<3,4,fp64>"))
+    # DRAM traffic per launch, scaled from the small-case ncu capture
+    # (profiles/query_ingest_kernels__tricubic160_both_mixed.md: 523.8 MB for
+    # 2.02e6 queries on a 160^3 grid whose mixed grid is 81.9 MB)
+    traffic = (nq * (523.79e6 - 81.92e6) / 2.02e6 + grid_bytes) if (prec == "mixed" and not use_tab) else None
     peak, peak_src = measured_peaks()
     achieved = algo / kt / 1e9
 
@@ -419,7 +435,7 @@ def main():
                        "precision": prec, "strategy": "table" if use_tab else "otf",
                        "l2": "inputs larger than L2 (field 805 MB, queries 242 MB); no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": kname,
+                         "frac": achieved / peak, "traffic": traffic, "kernel": kname,
                          "kernel_ms": 1000 * kt, "algorithmic_bytes": algo, "peak_source": peak_src},
             "clocks": clk.summary(),
             "gpu_launches": launches_per_step * args.steps,

@@ -168,6 +168,20 @@ int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32_t use_tabl
                           const arb_query_out *out, void *work, size_t work_bytes,
                           int32_t *status, arb_stream_t stream);
 
+/* ---- the two halves of arb_query_eval_sorted (same reference methods).
+ *      arb_query_bin: index step, out-of-volume bookkeeping (inds, oob rows,
+ *      q write-back, status) and the bin-ordered records in `work`.
+ *      arb_query_eval_binned: evaluation from those records into
+ *      out->comps/norms/grads.  The records depend on the query points and
+ *      the grid geometry only, so the same points can be re-evaluated after
+ *      the field values change (same geometry) without binning again. */
+int arb_query_bin(const arb_grid *g, int32_t precision, double *q, int64_t nq, int64_t q_stride,
+                  int32_t q_writeback, const arb_query_out *out, void *work, size_t work_bytes,
+                  int32_t *status, arb_stream_t stream);
+
+int arb_query_eval_binned(const arb_grid *g, int32_t precision, int32_t use_table, int64_t nq,
+                          const arb_query_out *out, void *work, size_t work_bytes, arb_stream_t stream);
+
 /* ---- allocation-free cell-grouped evaluation.  No counterpart in the
  *      reference (which has no device memory at all).
  *

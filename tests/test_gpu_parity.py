@@ -293,3 +293,38 @@ def test_tensor_core_table_matches_fp64(mode):
     for cell in (0, 7, one.nc - 1):
         assert np.abs(a[:, cell] - ref[:, cell]).max() <= 1e-6 * np.abs(ref[:, :o64.nc]).max()
     assert not a[:, 3].any()      # unsolved cells stay zero
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_bin_once_evaluate_twice(prec):
+    """arb_query_bin + arb_query_eval_binned equal the one-call sorted path,
+    and the records are reusable on a second field of the same geometry."""
+    import torch
+    tricubic, _ = _mods()
+    from arbinterp_gb300 import synth, _lib
+    L = _lib.lib()
+    fa = synth.dipole_field3(n=(30, 34, 28), seed=21).numpy()
+    fb = fa.copy()
+    fb[:, 3:] = synth.dipole_field3(n=(30, 34, 28), seed=22).numpy()[:, 3:]
+    oa = tricubic(fa, "quiet", mode="both", precision=prec, sort_threshold=0)
+    ob = tricubic(fb, "quiet", mode="both", precision=prec, sort_threshold=0)
+    q = synth.uniform_queries([oa.xIntMin, oa.yIntMin, oa.zIntMin], [oa.xIntMax, oa.yIntMax, oa.zIntMax],
+                              40000, 400, [oa.hx, oa.hy, oa.hz], seed=23, device="cuda")
+    n = q.shape[0]
+    pc = _lib.PREC_FP64 if prec == "fp64" else _lib.PREC_MIXED
+    need = int(L.arb_query_sorted_work_bytes(oa._g, pc, n))
+    ws = torch.empty(need, dtype=torch.uint8, device="cuda")
+    f64 = dict(dtype=torch.float64, device="cuda")
+    c, nn, g = torch.empty((n, 3), **f64), torch.empty((n, 1), **f64), torch.empty((n, 3), **f64)
+    inds = torch.empty(n, dtype=torch.int64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    out = _lib.ArbQueryOut(c.data_ptr(), nn.data_ptr(), g.data_ptr(), inds.data_ptr(), None, None)
+    s = torch.cuda.current_stream().cuda_stream
+    assert L.arb_query_bin(oa._g, pc, q.clone().data_ptr(), n, 3, 0, out, ws.data_ptr(), need,
+                           st.data_ptr(), s) == 0
+    for o in (oa, ob):
+        assert L.arb_query_eval_binned(o._g, pc, 0, n, out, ws.data_ptr(), need, s) == 0
+        want = o.Query(q.clone())
+        for got, ref in zip((c, nn, g), want):
+            assert torch.equal(torch.isnan(got), torch.isnan(ref))
+            assert torch.equal(torch.nan_to_num(got), torch.nan_to_num(ref))
