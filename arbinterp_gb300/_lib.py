@@ -32,7 +32,7 @@ class ArbGrid(C.Structure):
         ("n", C.c_int64 * 4), ("nc", C.c_int64),
         ("lo", C.c_double * 4), ("hi", C.c_double * 4), ("h", C.c_double * 4),
         ("grid64", C.c_void_p), ("grid32", C.c_void_p), ("table", C.c_void_p),
-        ("table_prec", C.c_int32), ("reserved", C.c_int32),
+        ("table_prec", C.c_int32), ("bin_shift", C.c_int32),
     ]
 
 

@@ -41,7 +41,7 @@ struct BinGeom {
 
 static inline BinGeom bin_geom(const arb_grid *g) {
   BinGeom b;
-  b.shift = g->dim == 3 ? 3 : 2;
+  b.shift = (g->bin_shift > 0 && g->bin_shift <= 8) ? g->bin_shift : (g->dim == 3 ? 3 : 2);
   b.nbins = 1;
   for (int a = 0; a < 4; ++a) {
     if (a < g->dim) {

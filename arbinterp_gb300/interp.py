@@ -34,6 +34,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from . import autotune
 from . import matrices
 from ._lib import ArbGrid, ArbQueryOut, lib, check
 
@@ -115,6 +116,7 @@ class _Interpolant:
         self._solved = None          # host bool mask of solved cells (partial solves)
         self._last_inds = None
         self._last_ind = None
+        self.last_plan = None
 
     # ------------------------------------------------------------------ ingest
     def _ingest(self, field):
@@ -248,18 +250,26 @@ class _Interpolant:
         return self._solved is not None and bool(self._solved.all())
 
     # ------------------------------------------------------------------ queries
-    def _use_table(self):
+    def _plan(self, qd, n, qs):
+        """Strategy for this batch: forced by `strategy`, else the autotuner."""
         if self.strategy == "table":
             if not self._table_complete:
                 self.allCoeffs()
-            return True
+            return {"table": True, "binned": n >= self.sort_threshold, "bin_shift": 0}
         if self.strategy == "otf":
-            return False
-        return self._table_complete
+            return {"table": False, "binned": n >= self.sort_threshold, "bin_shift": 0}
+        return autotune.choose(self, qd, n, qs)
 
-    def _run(self, qd, n, qs, writeback, want_oob):
-        """Launch the evaluation kernel on device rows qd; returns device outputs."""
-        L = lib()
+    def _use_table(self):
+        return self.strategy == "table" or (self.strategy == "auto" and self._table_complete)
+
+    def _drop_table(self):
+        self._table = None
+        self._table_prec = None
+        self._solved = None
+        self._g.table = None
+
+    def _outputs(self, n, want_oob):
         dev = self.device
         dim, kind = self._dim, self._kind
         f64 = dict(dtype=torch.float64, device=dev)
@@ -269,15 +279,23 @@ class _Interpolant:
         inds = torch.empty(n, dtype=torch.int64, device=dev)
         oob = torch.empty(n, dtype=torch.int64, device=dev) if want_oob else None
         cnt = torch.zeros(1, dtype=torch.int64, device=dev) if want_oob else None
+        return comps, norms, grads, inds, oob, cnt
+
+    def _launch(self, qd, n, qs, writeback, want_oob, plan):
+        """Launch one evaluation of device rows qd with a given plan."""
+        L = lib()
+        res = self._outputs(n, want_oob)
+        comps, norms, grads, inds, oob, cnt = res
         out = ArbQueryOut(_ptr(comps), _ptr(norms), _ptr(grads), _ptr(inds), _ptr(oob), _ptr(cnt))
         s = _stream()
-        table = self._use_table()
+        table = bool(plan["table"])
         prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_MIXED
-        if n >= self.sort_threshold:
+        if plan["binned"]:
             # group queries by spatial bin first (cell-coherent gathers)
+            self._g.bin_shift = int(plan.get("bin_shift", 0))
             need = int(L.arb_query_sorted_work_bytes(self._g, prec, n))
             if self._ws is None or self._ws.numel() < need:
-                self._ws = torch.empty(need, dtype=torch.uint8, device=dev)
+                self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
             rc = L.arb_query_eval_sorted(self._g, prec, int(table), qd.data_ptr(), n, qs, int(writeback),
                                          out, self._ws.data_ptr(), need, self._status.data_ptr(), s)
         elif table:
@@ -287,7 +305,13 @@ class _Interpolant:
             rc = L.arb_query_eval_otf(self._g, prec, qd.data_ptr(), n, qs, int(writeback), out,
                                       self._status.data_ptr(), s)
         check(rc, "query evaluation")
-        return comps, norms, grads, inds, oob, cnt
+        return res
+
+    def _run(self, qd, n, qs, writeback, want_oob):
+        """Evaluate device rows qd with the planned strategy; returns device outputs."""
+        plan = self._plan(qd, n, qs)
+        self.last_plan = plan
+        return self._launch(qd, n, qs, writeback, want_oob, plan)
 
     def _fetch_status(self):
         return lib().arb_status_fetch(self._status.data_ptr(), _stream())

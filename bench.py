@@ -327,7 +327,9 @@ def main():
     from arbinterp_gb300 import _lib as LB
     L = LB.lib()
     o = tricubic(field, "quiet", mode="both", precision=prec, strategy=strat)
-    use_tab = o._use_table()
+    o.Query(q.clone())                                   # the plan the timed steps use
+    use_tab = bool(o.last_plan["table"])
+    o._g.bin_shift = int(o.last_plan.get("bin_shift", 0))
     pc = LB.PREC_MIXED if prec == "mixed" else LB.PREC_FP64
     need = int(L.arb_query_sorted_work_bytes(o._g, pc, nq))
     ws = torch.empty(need, dtype=torch.uint8, device=dev)
@@ -433,6 +435,7 @@ def main():
             "config": {"workload": "tricubic 256^3 dipole vector field (16 dipoles outside the box), mode both, "
                                    "construct + 1.01e7 queries (1% outside the volume)",
                        "precision": prec, "strategy": "table" if use_tab else "otf",
+                       "plan": o.last_plan,
                        "l2": "inputs larger than L2 (field 805 MB, queries 242 MB); no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": kname,

@@ -76,7 +76,7 @@ typedef struct arb_grid {
   const float *grid32;  /* mixed-precision split (layout above) or NULL   */
   const void *table;    /* [nc][F][M] or NULL                               */
   int32_t table_prec;   /* enum arb_precision of table (FP64: double)      */
-  int32_t reserved;
+  int32_t bin_shift;    /* log2 cells per bin edge for grouped queries; 0 = default (3D: 3, 4D: 2) */
 } arb_grid;
 
 /* Query outputs.  Any pointer may be NULL when not wanted.  Row-major like

@@ -328,3 +328,38 @@ def test_bin_once_evaluate_twice(prec):
         for got, ref in zip((c, nn, g), want):
             assert torch.equal(torch.isnan(got), torch.isnan(ref))
             assert torch.equal(torch.nan_to_num(got), torch.nan_to_num(ref))
+
+
+def test_autotuner_plans_and_caches(tmp_path, monkeypatch):
+    """The autotuner times strategies / bin sizes on the caller's rows, caches
+    the winner on disk, and every candidate gives identical results."""
+    import json
+    import torch
+    monkeypatch.setenv("ARBINTERP_TUNE_DIR", str(tmp_path))
+    tricubic, _ = _mods()
+    from arbinterp_gb300 import synth, autotune
+    autotune._MEM.clear()
+    f = synth.dipole_field3(n=(48, 40, 44), seed=31).numpy()
+    o = tricubic(f, "quiet", mode="both", precision="mixed")
+    q = synth.uniform_queries([o.xIntMin, o.yIntMin, o.zIntMin], [o.xIntMax, o.yIntMax, o.zIntMax],
+                              300000, 3000, [o.hx, o.hy, o.hz], seed=32, device="cuda")
+    got = o.Query(q.clone())
+    plan = o.last_plan
+    assert plan is not None and "ms" in plan
+    cache = json.load(open(tmp_path / "autotune.json"))
+    assert list(cache.values())[0]["bin_shift"] == plan["bin_shift"]
+    ref = tricubic(f, "quiet", mode="both", precision="mixed", strategy="otf", sort_threshold=1 << 40)
+    want = ref.Query(q.clone())
+    for a, b in zip(got, want):
+        assert torch.equal(torch.isnan(a), torch.isnan(b))
+        assert (torch.nan_to_num(a) - torch.nan_to_num(b)).abs().max() <= 1e-6 * torch.nan_to_num(b).abs().max()
+    n = q.shape[0]
+    for cand in autotune._candidates(o):
+        res = o._launch(q.clone(), n, 3, False, False, cand)
+        for a, b in zip(res[:3], want):
+            assert torch.equal(torch.isnan(a), torch.isnan(b))
+            assert (torch.nan_to_num(a) - torch.nan_to_num(b)).abs().max() <= 1e-6 * torch.nan_to_num(b).abs().max()
+    autotune._MEM.clear()
+    o2 = tricubic(f, "quiet", mode="both", precision="mixed")
+    o2.Query(q.clone())
+    assert o2.last_plan == plan
