@@ -168,6 +168,27 @@ int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32_t use_tabl
                           const arb_query_out *out, void *work, size_t work_bytes,
                           int32_t *status, arb_stream_t stream);
 
+/* ---- adjoint of the 3D scalar interpolant.  No counterpart in the
+ *      reference (it has no backward pass); it is the transpose of the
+ *      forward map of rQuery2 (src/ARBInterp/ARBInterp.py:399-454): values
+ *      and gradients are linear in the grid samples through A = inv(B) D.
+ *      Given upstream dL/dvalue dval[nq] and/or dL/dgrad dgrad[nq][3]
+ *      (either may be NULL), accumulates dL/df into grid_grad[npts] (float64
+ *      for ARB_PREC_FP64, float32 for ARB_PREC_MIXED; zero it first) with
+ *      atomics, and writes dL/dq into q_grad[nq][3] (may be NULL).  Rows
+ *      outside the volume, NaN rows and sentinel rows contribute nothing
+ *      and get dL/dq = 0.  g must be 3D with F = 1 (scalar or norm mode). */
+int arb_adjoint(const arb_grid *g, int32_t precision, const double *q, int64_t nq, int64_t q_stride,
+                const double *dval, const double *dgrad, void *grid_grad, double *q_grad,
+                int32_t *status, arb_stream_t stream);
+
+/* Replaces the sample values of a scalar (F = 1) interpolant: values[npts]
+ * in grid order (z-major, x fastest), float32 (values_f32) or float64;
+ * rewrites grid64 and, when given, the float32 split grid32.  The geometry
+ * and any coefficient table are unchanged (solve again if one is used). */
+int arb_grid_set_values(const arb_grid *g, const void *values, int32_t values_f32, double *grid64,
+                        float *grid32, arb_stream_t stream);
+
 /* ---- the two halves of arb_query_eval_sorted (same reference methods).
  *      arb_query_bin: index step, out-of-volume bookkeeping (inds, oob rows,
  *      q write-back, status) and the bin-ordered records in `work`.

@@ -317,6 +317,44 @@ class _OracleBase:
             out["grads"] = np.stack(g, axis=1)
         return out
 
+    def adjoint(self, q, dval, dgrad=None):
+        """Float64 reference gradient of a loss w.r.t. the grid samples of the
+        interpolated scalar field (grid order), given dL/dvalue (n,) and
+        optionally dL/dgrad (n, dim).  The reference has no backward pass;
+        this is the transpose of its forward map: value = p(x) . (A f_block)
+        and grad_a = (dp_a(x) . (A f_block)) / h_a (ARB:399-454), so
+        dL/df_block = (dval p + sum_a dgrad_a dp_a / h_a) A."""
+        d = self.dim
+        q = np.asarray(q, dtype=np.float64)
+        bad = np.zeros(len(q), bool)
+        for a in range(d):
+            bad |= (q[:, a] < self.lo[a]) | (q[:, a] > self.hi[a]) | np.isnan(q[:, a])
+        iu = [(q[:, a] - self.lo[a]) / self.h[a] for a in range(d)]
+        fl = [np.floor(u) for u in iu]
+        ind = fl[0].copy()
+        mul = 1
+        for a in range(1, d):
+            mul = mul * self.ncell[a - 1]
+            ind = ind + fl[a] * mul
+        ok = ~bad
+        ind = np.where(ok, ind, 0).astype(np.int64)
+        ok &= ind < self.nc
+        frac = [u - f for u, f in zip(iu, fl)]
+        P = [_powers(np.where(ok, t, 0.0)) for t in frac]
+        dP = [_dpowers(np.where(ok, t, 0.0)) for t in frac]
+        coef = dval[:, None] * self._outer(P)
+        if dgrad is not None:
+            for a in range(d):
+                Pa = list(P)
+                Pa[a] = dP[a]
+                coef = coef + (dgrad[:, a] / self.h[a])[:, None] * self._outer(Pa)
+        w = coef @ self.A                          # (n, M) weights on the block samples
+        w[~ok] = 0.0
+        gg = np.zeros(len(self.inputfield))
+        blocks = self.basePointInds[ind][:, None] + self.block_offsets[None, :]
+        np.add.at(gg, blocks[ok], w[ok])
+        return gg
+
     def _outer(self, P):
         # monomial index ex + 4 ey + 16 ez (+ 64 et), x fastest
         m = P[0]

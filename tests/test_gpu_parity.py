@@ -365,3 +365,62 @@ def test_autotuner_plans_and_caches(tmp_path, monkeypatch):
     o2 = tricubic(f, "quiet", mode="both", precision="mixed")
     o2.Query(q.clone())
     assert o2.last_plan == plan
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_adjoint_gradients(prec):
+    """Backward kernel: dL/d(grid values) against the float64 reference
+    adjoint (dense A^T scatter of the reference's monomial form) and against
+    central finite differences; dL/d(query) against finite differences."""
+    import torch
+    from arbinterp_gb300 import synth
+    from arbinterp_gb300.autograd import TricubicField
+    from oracle.arb_oracle import OracleTricubic
+    dt = torch.float64 if prec == "fp64" else torch.float32
+    f = synth.gaussian_field3(n=(18, 16, 20), h=(0.1, 0.12, 0.08), seed=41).numpy()
+    if prec == "mixed":
+        f = f.astype(np.float32)
+    fld = TricubicField(f, precision=prec)
+    ref = OracleTricubic(f.astype(np.float64))
+    vals = fld.initial_values().to(dt).cuda().requires_grad_()
+    lo, hi = np.array(ref.lo), np.array(ref.hi)
+    rng = np.random.default_rng(42)
+    qn = lo + (hi - lo) * rng.uniform(0.01, 0.99, (3000, 3))
+    q = torch.tensor(qn, device="cuda", dtype=torch.float64, requires_grad=True)
+    target = torch.tensor(rng.standard_normal(3000) * 0.1, device="cuda", dtype=dt)
+    value, grad = fld(vals, q)
+    loss = ((value - target) ** 2).sum() + 0.01 * (grad ** 2).sum()
+    loss.backward()
+    dv = (2 * (value - target)).detach().double().cpu().numpy()
+    dg = (0.02 * grad).detach().double().cpu().numpy()
+    gg_ref = ref.adjoint(qn, dv, dg)
+    gg = vals.grad.double().cpu().numpy()
+    tol = 1e-12 if prec == "fp64" else 2e-5
+    assert np.abs(gg - gg_ref).max() <= tol * np.abs(gg_ref).max()
+
+    # central finite differences in float64 through the float64 forward
+    fd = TricubicField(f.astype(np.float64), precision="fp64")
+    v64 = fd.initial_values().cuda()
+    q64 = q.detach().clone()
+    t64 = target.double()
+
+    def L64(v, qq):
+        a, b = fd(v, qq)
+        return float((((a - t64) ** 2).sum() + 0.01 * (b ** 2).sum()).item())
+
+    for p in rng.choice(v64.numel(), 40, replace=False):
+        e = 1e-4
+        vp, vm = v64.clone(), v64.clone()
+        vp[p] += e
+        vm[p] -= e
+        fdv = (L64(vp, q64) - L64(vm, q64)) / (2 * e)
+        assert abs(fdv - gg[p]) <= 1e-6 * max(1.0, np.abs(gg).max()) + 3e-5 * abs(fdv), (p, fdv, gg[p])
+    qg = q.grad.cpu().numpy()
+    for r in rng.choice(3000, 20, replace=False):
+        for a in range(3):
+            e = 1e-6 * ref.h[a]
+            qp, qm = q64.clone(), q64.clone()
+            qp[r, a] += e
+            qm[r, a] -= e
+            fdq = (L64(v64, qp) - L64(v64, qm)) / (2 * e)
+            assert abs(fdq - qg[r, a]) <= 1e-4 * max(1.0, abs(fdq)), (r, a, fdq, qg[r, a])
