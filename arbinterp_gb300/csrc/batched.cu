@@ -1,0 +1,134 @@
+// Batched persistent evaluation: many 3D interpolants (fields) and their
+// query sets in one launch.  No counterpart in the reference (one object per
+// field, ARB:8-621); per field it computes exactly what rQuery1/2/3 do
+// (ARB:344-521).
+//
+// The query sets are concatenated; each is cut into tiles of `tile_rows`
+// rows, and tiles are numbered field by field (tile_off is the prefix sum of
+// tiles per field).  One CTA per SM slot loops: it takes the next tile from a
+// global atomic counter, loads that field's descriptor into shared memory
+// and evaluates the tile's rows, on the fly from the grid or from the
+// field's coefficient table when the descriptor carries one.  Dynamic
+// scheduling keeps uneven fields (1e3 .. 1e6 rows, 16^3 .. 128^3 grids)
+// balanced, and fields are processed roughly in order so each field's grid
+// stays L2-resident while its tiles run.
+#include "eval.cuh"
+
+namespace arb {
+
+__device__ KParams make_kparams_dev(const arb_grid &g) {
+  KParams kp;
+  for (int a = 0; a < 4; ++a) {
+    const double h = a < g.dim ? g.h[a] : 1.0;
+    const double lo = a < g.dim ? g.lo[a] : 0.0, hi = a < g.dim ? g.hi[a] : 0.0;
+    kp.inv_h[a] = 1.0 / h;
+    kp.inv_hf[a] = (float)(1.0 / h);
+    kp.ax[a].lo_key = ord_key_bits((unsigned long long)__double_as_longlong(lo));
+    kp.ax[a].hi_key = ord_key_bits((unsigned long long)__double_as_longlong(hi));
+    kp.ax[a].lo = lo;
+    kp.ax[a].h = h;
+    kp.ax[a].inv_h = 1.0 / h;
+  }
+  return kp;
+}
+
+template <int F, bool MIXED>
+__device__ __forceinline__ void batched_rows(const arb_grid &g, const KParams &kp, double *q, int64_t q0,
+                                             int64_t q1, int64_t qs, int wb, const arb_query_out &o,
+                                             int32_t *status) {
+  using T = typename std::conditional<MIXED, float, double>::type;
+  for (int64_t i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
+    T fr[3];
+    int64_t idx;
+    if (!query_prologue<3, F, !MIXED>(g, kp, q, i, qs, wb, o, status, fr, idx)) continue;
+    int64_t c[3];
+    cell_coords<3>(idx, g, c);
+    double val[F], grad[3] = {0, 0, 0};
+    if (g.table)
+      eval_tab<3, F, MIXED>(g, kp, c, fr, val, grad);
+    else
+      eval_otf3<F, MIXED>(g, kp, c, fr, val, grad);
+    write_vals<3, F>(o, i, val, grad);
+  }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) batched_kernel(const arb_grid *grids, int32_t nfields,
+                                                      const int64_t *q_off, const int64_t *tile_off,
+                                                      int64_t ntiles, int32_t tile_rows, double *q,
+                                                      int64_t qs, int wb, arb_query_out o,
+                                                      unsigned long long *counter, int32_t *status) {
+  __shared__ arb_grid sg;
+  __shared__ KParams skp;
+  __shared__ int64_t stile;
+  __shared__ int32_t sfield;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int64_t tile = (int64_t)atomicAdd(counter, 1ULL);
+      stile = tile;
+      if (tile < ntiles) {
+        int32_t lo = 0, hi = nfields - 1;  // last field with tile_off[f] <= tile
+        while (lo < hi) {
+          const int32_t mid = (lo + hi + 1) >> 1;
+          if (tile_off[mid] <= tile)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        sfield = lo;
+        sg = grids[lo];
+        skp = make_kparams_dev(sg);
+      }
+    }
+    __syncthreads();
+    const int64_t tile = stile;
+    if (tile >= ntiles) break;
+    const int32_t f = sfield;
+    const int64_t q0 = q_off[f] + (tile - tile_off[f]) * tile_rows;
+    const int64_t q1 = min(q0 + (int64_t)tile_rows, q_off[f + 1]);
+    switch (sg.nfield) {
+      case 1: batched_rows<1, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
+      case 3: batched_rows<3, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
+      default: batched_rows<4, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
+    }
+    __syncthreads();  // the descriptor in shared memory is replaced next round
+  }
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 148;
+  }
+  return n;
+}
+
+}  // namespace arb
+
+using namespace arb;
+
+extern "C" int arb_batched_launch(const arb_grid *grids, int32_t nfields, const int64_t *q_off,
+                                  const int64_t *tile_off, int64_t ntiles, int32_t tile_rows,
+                                  int32_t precision, double *q, int64_t q_stride, int32_t q_writeback,
+                                  const arb_query_out *out, unsigned long long *counter, int32_t *status,
+                                  arb_stream_t stream) {
+  if (!grids || nfields <= 0 || !q_off || !tile_off || !out || !counter || tile_rows <= 0 || q_stride < 3)
+    return ARB_ERR_INVALID;
+  if (out->oob_rows && !out->oob_count) return ARB_ERR_INVALID;
+  if (ntiles == 0) return ARB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s) != cudaSuccess) return ARB_ERR_CUDA;
+  const int per_sm = 8;
+  int64_t grid = (int64_t)sm_count() * per_sm;
+  if (grid > ntiles) grid = ntiles;
+  if (precision == ARB_PREC_MIXED)
+    batched_kernel<true><<<(unsigned)grid, 256, 0, s>>>(grids, nfields, q_off, tile_off, ntiles, tile_rows, q,
+                                                        q_stride, q_writeback, *out, counter, status);
+  else
+    batched_kernel<false><<<(unsigned)grid, 256, 0, s>>>(grids, nfields, q_off, tile_off, ntiles, tile_rows, q,
+                                                         q_stride, q_writeback, *out, counter, status);
+  return launch_status();
+}

@@ -189,6 +189,22 @@ int arb_adjoint(const arb_grid *g, int32_t precision, const double *q, int64_t n
 int arb_grid_set_values(const arb_grid *g, const void *values, int32_t values_f32, double *grid64,
                         float *grid32, arb_stream_t stream);
 
+/* ---- batched persistent evaluation of many 3D interpolants in one launch.
+ *      Per field it computes what rQuery1/2/3 do
+ *      (src/ARBInterp/ARBInterp.py:344-521); the batching itself has no
+ *      counterpart in the reference (one Python object per field).
+ *      grids: DEVICE array of nfields descriptors (a descriptor with a table
+ *      is evaluated from its table, otherwise on the fly; all use
+ *      `precision`).  Queries of all fields are concatenated in q (q_stride
+ *      doubles per row); field f owns rows [q_off[f], q_off[f+1]) and tiles
+ *      [tile_off[f], tile_off[f+1]) of tile_rows rows (device arrays of
+ *      nfields+1).  Outputs are concatenated the same way.  counter is one
+ *      device word of scratch (reset here).  Capturable in a CUDA graph. */
+int arb_batched_launch(const arb_grid *grids, int32_t nfields, const int64_t *q_off,
+                       const int64_t *tile_off, int64_t ntiles, int32_t tile_rows, int32_t precision,
+                       double *q, int64_t q_stride, int32_t q_writeback, const arb_query_out *out,
+                       unsigned long long *counter, int32_t *status, arb_stream_t stream);
+
 /* ---- the two halves of arb_query_eval_sorted (same reference methods).
  *      arb_query_bin: index step, out-of-volume bookkeeping (inds, oob rows,
  *      q write-back, status) and the bin-ordered records in `work`.

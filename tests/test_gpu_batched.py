@@ -1,0 +1,80 @@
+"""Batched persistent evaluation (arb_batched_launch) and its CUDA graph:
+every field's rows match the single-field path; per-field strategy and tile
+size come from the batch tuner."""
+import numpy as np
+import pytest
+
+from conftest import normwise
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _batch(seed=0, nfields=7):
+    import torch
+    from arbinterp_gb300 import synth
+    rng = np.random.default_rng(seed)
+    fields, qs, counts = [], [], []
+    for i in range(nfields):
+        e = int(rng.integers(6, 24))
+        h = tuple(rng.uniform(0.05, 0.2, 3))
+        f = synth.gaussian_field3(n=(e, e + 1, e + 2), h=h, seed=100 + i).numpy()
+        n = int(rng.choice([5, 300, 5000, 40000]))
+        from oracle.arb_oracle import OracleTricubic
+        o = OracleTricubic(f)
+        q = synth.uniform_queries(o.lo, o.hi, n, max(1, n // 50), o.h, seed=200 + i)
+        fields.append(f)
+        qs.append(q)
+        counts.append(q.shape[0])
+    return fields, torch.cat(qs).cuda(), counts
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batched_matches_single_field(prec, tmp_path, monkeypatch):
+    import torch
+    monkeypatch.setenv("ARBINTERP_TUNE_DIR", str(tmp_path))
+    from arbinterp_gb300 import tricubic
+    from arbinterp_gb300.batched import BatchedTricubic
+    fields, q, counts = _batch()
+    b = BatchedTricubic(fields, precision=prec)
+    norms, grads = b.query(q.clone(), counts)
+    assert b.tile_rows in (256, 512, 1024, 2048)
+    off = np.concatenate([[0], np.cumsum(counts)])
+    tol = 1e-12 if prec == "fp64" else 1e-6
+    for k, f in enumerate(fields):
+        ref = tricubic(f, "quiet")                       # float64 single-field path
+        rn, rg = ref.Query(q[off[k]:off[k + 1]].clone())
+        gn, gg = norms[off[k]:off[k + 1]], grads[off[k]:off[k + 1]]
+        assert torch.equal(torch.isnan(gn), torch.isnan(rn))
+        a, r = gn.cpu().numpy(), rn.cpu().numpy()
+        assert (normwise(a, r) <= tol).all(), (k, normwise(a, r))
+        assert (normwise(gg.cpu().numpy(), rg.cpu().numpy()) <= tol).all()
+
+
+def test_batched_graph_replay(tmp_path, monkeypatch):
+    import torch
+    monkeypatch.setenv("ARBINTERP_TUNE_DIR", str(tmp_path))
+    from arbinterp_gb300.batched import BatchedTricubic
+    fields, q, counts = _batch(seed=1)
+    b = BatchedTricubic(fields, precision="mixed")
+    qbuf = q.clone()
+    graph, (gn, gg) = b.capture(qbuf, counts)
+    graph.replay()
+    torch.cuda.synchronize()
+    want_n, want_g = b.query(q.clone(), counts)
+    assert torch.equal(torch.nan_to_num(gn), torch.nan_to_num(want_n))
+    # new query contents, same shape: replay re-evaluates them
+    _, q2, counts2 = _batch(seed=1)
+    perm = torch.randperm(q2.shape[0], device="cuda")
+    qbuf.copy_(q2)
+    graph.replay()
+    torch.cuda.synchronize()
+    w2n, _ = b.query(q2.clone(), counts)
+    assert torch.equal(torch.nan_to_num(gn), torch.nan_to_num(w2n))
+    del perm
