@@ -258,10 +258,9 @@ def test_fd_planes_match_D_matrix():
 
 @pytest.mark.parametrize("mode", ["both", "vector", "norm"])
 def test_tensor_core_table_matches_fp64(mode):
-    """Mixed-precision table (split-BF16 tcgen05 GEMM, float32 rows) against
-    the float64 table: every coefficient within 1e-6 of its column's scale,
-    alpha_000 within float32 rounding of the value; single-cell solves
-    (partial tiles, cell offsets) included."""
+    """Mixed-precision table (FP16 fixed-point tcgen05 GEMM, float32 rows)
+    against the float64 table; single-cell solves (partial tiles, cell
+    offsets) included."""
     tricubic, _ = _mods()
     from arbinterp_gb300 import synth
     f = synth.dipole_field3(n=(23, 19, 21), seed=8).numpy()
@@ -280,10 +279,10 @@ def test_tensor_core_table_matches_fp64(mode):
         # value error, sum_i ex_i |d alpha_i| the (cell-unit) x-gradient error
         val_err = d.sum(axis=0).max() / np.abs(a64[0]).max()
         grad_err = (ex[:, None] * d).sum(axis=0).max() / (ex[:, None] * np.abs(a64)).sum(axis=0).max()
-        # float32 accumulation: |d alpha_n| <= 216 eps32 max|f - f_ref| per
-        # coefficient (216 = largest row abs-sum of A); summed over the 64
-        # coefficients this triangle bound is ~1e-5 on this coarse, fast-
-        # varying grid.  The 1e-6 bar applies to query outputs (other tests).
+        # triangle bounds over the 64 float32-rounded coefficients (float32
+        # deltas, vector components without a lo word): ~1.5e-5 on this
+        # coarse, fast-varying grid even for exactly computed coefficients;
+        # the GEMM itself adds no accumulation error (next test)
         assert val_err <= 3e-5 and grad_err <= 3e-5, (name, val_err, grad_err)
     one = tricubic(f, "quiet", mode=mode, precision="mixed")
     for cell in (0, 7, one.nc - 1):
@@ -293,6 +292,42 @@ def test_tensor_core_table_matches_fp64(mode):
     for cell in (0, 7, one.nc - 1):
         assert np.abs(a[:, cell] - ref[:, cell]).max() <= 1e-6 * np.abs(ref[:, :o64.nc]).max()
     assert not a[:, 3].any()      # unsolved cells stay zero
+
+
+@pytest.mark.parametrize("mode", ["both", "vector", "norm", None])
+def test_tensor_core_table_exact_from_deltas(mode):
+    """The tcgen05 solve adds no accumulation error: every float32
+    coefficient equals alpha = A d computed exactly from the kernel's float32
+    deltas d = (hi - hi_ref) + (lo - lo_ref), up to its own float32 rounding
+    and the fixed-point truncation of d (2^-33 of the row's power-of-two
+    scale, times the largest row abs-sum 216 of A).  Coarse, fast-varying
+    dipole field; scalar field too."""
+    tricubic, _ = _mods()
+    from arbinterp_gb300 import synth
+    from oracle.arb_oracle import OracleTricubic
+    f = synth.dipole_field3(n=(23, 19, 21), seed=8).numpy()
+    if mode is None:
+        f = np.hstack([f[:, :3], f[:, 3:4] * f[:, 4:5] + 3.0])
+    kw = {} if mode is None else {"mode": mode}
+    omx = tricubic(f, "quiet", precision="mixed", **kw)
+    omx.allCoeffs()
+    o = OracleTricubic(f, **kw)
+    blocks = o.basePointInds[:, None] + o.block_offsets[None, :]
+    corner = 1 + 4 + 16
+    for key in o.fields:
+        v = o.fields[key]
+        hi = v.astype(np.float32)
+        lo = (v - hi).astype(np.float32) if key == "n" else np.zeros_like(hi)
+        rhi, rlo = hi[blocks[:, corner]], lo[blocks[:, corner]]
+        d = (hi[blocks] - rhi[:, None]) + (lo[blocks] - rlo[:, None])      # float32, as the kernel
+        want = d.astype(np.float64) @ o.A.T
+        want[:, 0] = (rhi + (rlo + np.float32(0))).astype(np.float64)
+        got = getattr(omx, "alpha" + key)[:, :o.nc].T.astype(np.float64)
+        amax = np.abs(d).max(axis=1).astype(np.float64)
+        scale = 2.0 ** np.ceil(np.log2(np.maximum(amax, 1e-300)) + 1e-12)
+        bound = 2.0 ** -23 * np.abs(want) + (2.0 ** -24 + 216 * 2.0 ** -33) * 2 * scale[:, None]
+        err = np.abs(got - want)
+        assert (err <= bound).all(), (key, (err / np.maximum(bound, 1e-300)).max())
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
