@@ -10,30 +10,36 @@
 // cell's own corner value, d = f - f_ref, formed in float32 from the (hi, lo)
 // grid split (alpha_000 is the only coefficient of magnitude |f|; the others
 // scale with the field's variation).  Each row is scaled by a power of two
-// S = 2^E >= max|d| and u = d / S is cut into three integers
-//   u = h0 2^-10 + h1 2^-21 + h2 2^-32,   |h0| <= 2048, |h1|, |h2| <= 1024,
-// each exact in FP16.  The B operand is 8 A, integers of at most 7 bits, also
-// exact in FP16.  Every product h * 8A is an integer below 2^18 and a sum of
-// 64 of them stays below 2^24, so each part's accumulation is EXACT in the
-// float32 accumulator; the three parts go to three TMEM accumulators and are
-// combined once in the epilogue,
-//   alpha = 2^(E-13) (acc0 + 2^-11 (acc1 + 2^-11 acc2)).
-// The only roundings are u's truncation at 2^-33 S and the final float32
-// rounding of alpha, so the table matches alpha computed exactly from the
-// float32 deltas and rounded to float32.  (A single accumulator over
+// S = 2^E > max|d|, t = 2^10 d / S, and t is cut into three FP16 parts
+//   t = h0 + h1 + 2^-22 h2,   h0 integer (|h0| <= 1024),
+//   h1 a multiple of 2^-11 (|h1| <= 1/2),  |h2| <= 1024,
+// h0 and h1 exact normal FP16 numbers.  The B operand is 8 A, integers of at
+// most 7 bits, exact in FP16.  Every product h0 * 8A is an integer and every
+// h1 * 8A a multiple of 2^-11, and their 64-term sums stay below 2^23 units,
+// so those two accumulations are EXACT in the float32 accumulator; the third
+// part carries only the last 2^-22 of t.  The parts accumulate into three
+// TMEM accumulators and are combined once in the epilogue,
+//   alpha = 2^(E-13) (acc0 + (acc1 + 2^-22 acc2)),
+// so the table matches alpha computed exactly from the float32 deltas up to
+// its own float32 rounding (plus ~2^-26 S).  A single accumulator over
 // float32-split operands loses up to ~10x more to cancellation between
-// partial sums on coarse, fast-varying grids.)
+// partial sums on coarse, fast-varying grids.
 //
 // CTA = 256 threads (8 warps), tile = 128 rows.  Thread t owns row t & 127
 // (TMEM lane t & 127); its half (t >> 7) gathers block points 32h..32h+31
-// and, in the epilogue, coefficients 32h..32h+31 of that row.  Twelve
-// 128x64x16 MMAs per tile (3 parts x 4 K-chunks) are issued by one thread;
-// accumulators use 3 x 64 of the 256 allocated TMEM columns.  Output rows are
-// staged in padded shared memory and written with bulk async stores, which
-// drain while the next tile is gathered.  Two CTAs per SM (shared memory
-// above a third of the SM's keeps the 256-column TMEM allocations within the
-// SM's 512 columns).
+// (block layers oz = 2h, 2h+1) and, in the epilogue, coefficients
+// 32h..32h+31 of that row.  Twelve 128x64x16 MMAs per tile (3 parts x 4
+// K-chunks) are issued by one thread; the accumulators use 3 x 64 of the 256
+// allocated TMEM columns.  The tile's 128 output rows are one contiguous
+// 32 KB range of the table: they are staged in shared memory in the 128-byte
+// swizzled layout (conflict-free row-per-thread writes) and written by two
+// TMA tensor stores, which drain while the next tile is gathered.  Two CTAs
+// per SM (shared memory above a third of the SM's keeps the 256-column TMEM
+// allocations within the SM's 512 columns).
+#include <cuda.h>
 #include <cuda_fp16.h>
+
+#include <mutex>
 
 #include "arb_common.cuh"
 #include "tc_ptx.cuh"
@@ -45,21 +51,22 @@ namespace {
 constexpr int TM = 128;                  // tile rows
 constexpr int NT = 256;                  // threads per CTA
 constexpr int KP = 64;                   // block points
-constexpr int PARTS = 3;                 // FP16 fixed-point parts per value
+constexpr int PARTS = 3;                 // FP16 parts per value
 constexpr int KT = KP * PARTS;           // 192
 constexpr int A_SBO = (KT / 8) * 128;    // bytes between 8-row core-matrix groups
 constexpr int A_BYTES = (TM / 8) * A_SBO;
 constexpr int B_SBO = (KP / 8) * 128;
 constexpr int B_BYTES = (64 / 8) * B_SBO;
-constexpr int STAGE_STRIDE = 256 + 16;   // padded output row (conflict-free stores)
+constexpr int BOX_BYTES = TM * 128;      // one half-row box: 128 rows x 32 floats
 constexpr int TMEM_COLS = 256;
 constexpr uint32_t WAIT_LIMIT = 1u << 22;
-constexpr float kRound = 12582912.0f;    // 1.5 * 2^23: x + kRound - kRound = rint(x) for |x| < 2^22
+constexpr float kRound0 = 12582912.0f;   // 1.5 * 2^23: (x + c) - c rounds x to an integer (|x| < 2^22)
+constexpr float kRound1 = 6144.0f;       // 1.5 * 2^12: (x + c) - c rounds x to a multiple of 2^-11
 
 struct TcSmem {
-  unsigned char a[A_BYTES];
-  unsigned char b[B_BYTES];
-  unsigned char stage[TM * STAGE_STRIDE];
+  unsigned char a[A_BYTES];              // A tile, no-swizzle K-major (offset 0)
+  unsigned char b[B_BYTES];              // B = 8 A (offset 48 KB)
+  unsigned char stage[2][BOX_BYTES];     // output rows, 128-byte swizzled (offset 56 KB, 1 KB aligned)
   float amax[2][TM];
   uint64_t mbar;
   uint32_t tmem_base;
@@ -75,8 +82,6 @@ __device__ __forceinline__ uint32_t kmaj(int row, int k, int sbo) {
   return (uint32_t)((row >> 3) * sbo + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
-__device__ __forceinline__ float rint_f(float x) { return __fadd_rn(__fadd_rn(x, kRound), -kRound); }
-
 __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
   const __half2 h = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<const uint32_t *>(&h);
@@ -88,11 +93,39 @@ __device__ __forceinline__ int scale_exp(float amax) {
   return min(max(eb - 126, -100), 126);
 }
 
+// t -> (h0, h1, h2) with t = h0 + h1 + 2^-22 h2 (see the file comment)
+__device__ __forceinline__ void split3(float t, float &h0, float &h1, float &h2) {
+  h0 = __fadd_rn(__fadd_rn(t, kRound0), -kRound0);
+  const float r = __fadd_rn(t, -h0);
+  h1 = __fadd_rn(__fadd_rn(r, kRound1), -kRound1);
+  h2 = __fmul_rn(__fadd_rn(r, -h1), 4194304.0f);
+}
+
+// four points along x of one block line: component f of grid32 (+ lo)
+template <int F>
+__device__ __forceinline__ void load_line(const float *hp, const float *lp, bool has_lo, float rhi, float rlo,
+                                          float *d, float &amax) {
+#pragma unroll
+  for (int ox = 0; ox < 4; ++ox) {
+    float vh, vl = 0.f;
+    if (F == 1) {
+      const float2 v = __ldg(reinterpret_cast<const float2 *>(hp) + ox);
+      vh = v.x;
+      vl = v.y;
+    } else {
+      vh = __ldg(hp + 4 * ox);
+      if (has_lo) vl = __ldg(lp + ox);
+    }
+    d[ox] = (vh - rhi) + (vl - rlo);
+    amax = fmaxf(amax, fabsf(d[ox]));
+  }
+}
+
 }  // namespace
 
 template <int F>
-__global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(arb_grid g, int64_t cell0, int64_t ncells,
-                                                         float *table, int32_t *status) {
+__global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__ CUtensorMap tmap, arb_grid g,
+                                                         int64_t cell0, int64_t ncells, int32_t *status) {
   extern __shared__ unsigned char smem_raw[];
   TcSmem &sm = *reinterpret_cast<TcSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -100,7 +133,8 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(arb_grid g, int64_t cel
   const int64_t rows = ncells * F;
   const int64_t npts = grid_points(g);
   const int64_t ntiles = (rows + TM - 1) / TM;
-  const int64_t nx = g.n[0], ny = g.n[1];
+  const int64_t nx = g.n[0], sy = g.n[0], sz = g.n[0] * g.n[1];   // point strides
+  constexpr int PW = F == 1 ? 2 : 4;                                  // floats per point in grid32
 
   // B operand: B[n][k] = 8 A[n][k] = 8 A1[ex][ox] A1[ey][oy] A1[ez][oz]
   for (int e = tid; e < 64 * 64; e += NT) {
@@ -124,29 +158,43 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(arb_grid g, int64_t cel
   const uint32_t idesc = tc::idesc_f16(0u, 128u, 64u);
   const uint32_t a_base = tc::smem_u32(sm.a), b_base = tc::smem_u32(sm.b);
   const uint32_t t_row = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * 32);
+  unsigned char *st_row = sm.stage[half] + row * 128;
   uint32_t parity = 0;
   bool timed_out = false;
 
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t r = tile * TM + row;
     float rhi = 0.f, rlo = 0.f, d[32], amax = 0.f;
-    // ---- gather half of the 4x4x4 block as deltas to the corner -------------
+    // ---- gather block layers oz = 2h, 2h+1 as deltas to the corner ---------
     if (r < rows) {
       const int64_t cell = cell0 + r / F;
-      const int f = (int)(r % F);
+      const int f = F == 1 ? 0 : (int)(r % F);
+      const bool has_lo = F == 1 || (F == 4 && f == 3);
       int64_t c[3];
       cell_coords<3>(cell, g, c);
-      const int64_t pref = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
-      g32_load<F>(g.grid32, npts, pref, f, rhi, rlo);
+      const int64_t p0 = (c[2] * g.n[1] + c[1]) * nx + c[0];          // block origin (ox = oy = oz = 0)
+      const float *hb = g.grid32 + p0 * PW + f;
+      const float *lb = g.grid32 + npts * 4 + p0;                     // lo of |B| (F = 4)
+      const int64_t corner = sz + sy + 1;
+      if (F == 1) {
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(hb + corner * PW));
+        rhi = v.x;
+        rlo = v.y;
+      } else {
+        rhi = __ldg(hb + corner * PW);
+        if (has_lo) rlo = __ldg(lb + corner);
+      }
+      const float *hp = hb + (2 * half) * sz * PW, *lp = lb + (2 * half) * sz;
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const int k = half * 32 + j;  // point index ox + 4 oy + 16 oz
-        const int ox = k & 3, oy = (k >> 2) & 3, oz = k >> 4;
-        const int64_t p = ((c[2] + oz) * ny + (c[1] + oy)) * nx + (c[0] + ox);
-        float vh, vl;
-        g32_load<F>(g.grid32, npts, p, f, vh, vl);
-        d[j] = (vh - rhi) + (vl - rlo);
-        amax = fmaxf(amax, fabsf(d[j]));
+      for (int oz = 0; oz < 2; ++oz) {
+#pragma unroll
+        for (int oy = 0; oy < 4; ++oy) {
+          load_line<F>(hp, lp, has_lo, rhi, rlo, d + oz * 16 + oy * 4, amax);
+          hp += sy * PW;
+          lp += sy;
+        }
+        hp += (sz - 4 * sy) * PW;
+        lp += sz - 4 * sy;
       }
     } else {
 #pragma unroll
@@ -155,25 +203,19 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(arb_grid g, int64_t cel
     sm.amax[half][row] = amax;
     __syncthreads();
     const int E = scale_exp(fmaxf(amax, sm.amax[half ^ 1][row]));
-    const float inv_s = __uint_as_float((uint32_t)(127 - E) << 23);
-    // ---- exact three-part FP16 fixed-point split into the A tile ----------
+    const float c10 = __uint_as_float((uint32_t)(137 - E) << 23);    // 2^(10 - E)
+    // ---- three-part FP16 split into the A tile ------------------------------
 #pragma unroll
     for (int ch = 0; ch < 4; ++ch) {
       uint32_t w0[4], w1[4], w2[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        float h0[2], h1[2], h2[2];
-#pragma unroll
-        for (int w = 0; w < 2; ++w) {
-          const float t0 = d[ch * 8 + v * 2 + w] * inv_s * 1024.f;
-          h0[w] = rint_f(t0);
-          const float t1 = (t0 - h0[w]) * 2048.f;
-          h1[w] = rint_f(t1);
-          h2[w] = rint_f((t1 - h1[w]) * 2048.f);
-        }
-        w0[v] = pack_h2(h0[0], h0[1]);
-        w1[v] = pack_h2(h1[0], h1[1]);
-        w2[v] = pack_h2(h2[0], h2[1]);
+        float a0, a1, a2, b0, b1, b2;
+        split3(__fmul_rn(d[ch * 8 + v * 2], c10), a0, a1, a2);
+        split3(__fmul_rn(d[ch * 8 + v * 2 + 1], c10), b0, b1, b2);
+        w0[v] = pack_h2(a0, b0);
+        w1[v] = pack_h2(a1, b1);
+        w2[v] = pack_h2(a2, b2);
       }
       const int k = half * 32 + ch * 8;
       *reinterpret_cast<uint4 *>(sm.a + kmaj(row, k, A_SBO)) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
@@ -182,6 +224,7 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(arb_grid g, int64_t cel
     }
     tc::fence_proxy_async_smem();
     tc::tc_fence_before();
+    if (tid == 0) tc::bulk_wait_read0();  // the previous tile's stores have read the staging buffer
     __syncthreads();
     // ---- 12 MMAs of 128 x 64 x 16: part p accumulates into columns 64p -----
     if (tid == 0) {
@@ -205,7 +248,7 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(arb_grid g, int64_t cel
       timed_out = true;
       break;
     }
-    // ---- epilogue: combine the exact part sums, stage, bulk-store ----------
+    // ---- epilogue: combine the part sums, stage swizzled, TMA-store --------
     float a[32], t[32];
     tc::tmem_ld16(t_row + 128u, t);
     tc::tmem_ld16(t_row + 144u, t + 16);
@@ -213,27 +256,28 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(arb_grid g, int64_t cel
     tc::tmem_ld16(t_row + 80u, a + 16);
     tc::tmem_wait_ld();
 #pragma unroll
-    for (int j = 0; j < 32; ++j) t[j] = __fmaf_rn(t[j], 0x1p-11f, a[j]);
+    for (int j = 0; j < 32; ++j) t[j] = __fmaf_rn(t[j], 0x1p-22f, a[j]);
     tc::tmem_ld16(t_row, a);
     tc::tmem_ld16(t_row + 16u, a + 16);
     tc::tmem_wait_ld();
-    const float so = __uint_as_float((uint32_t)(E - 13 + 127) << 23);
+    const float so = __uint_as_float((uint32_t)(E - 13 + 127) << 23);   // 2^(E - 13)
 #pragma unroll
-    for (int j = 0; j < 32; ++j) a[j] = __fmaf_rn(t[j], 0x1p-11f, a[j]) * so;
+    for (int j = 0; j < 32; ++j) a[j] = __fmul_rn(__fadd_rn(a[j], t[j]), so);
     if (half == 0) a[0] = rhi + (rlo + a[0]);
-    tc::bulk_wait_read0();  // this slot's previous store has read its source
-    unsigned char *st = sm.stage + row * STAGE_STRIDE + half * 128;
 #pragma unroll
     for (int q = 0; q < 8; ++q)
-      *reinterpret_cast<float4 *>(st + 16 * q) = make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
+      *reinterpret_cast<float4 *>(st_row + 16 * (q ^ (row & 7))) =
+          make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
     tc::fence_proxy_async_smem();
-    if (r < rows) {
-      tc::bulk_store(table + r * 64 + half * 32, st, 128u);
+    tc::tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc::tma_store_2d(&tmap, sm.stage[0], 0, (int32_t)(tile * TM));
+      tc::tma_store_2d(&tmap, sm.stage[1], 32, (int32_t)(tile * TM));
       tc::bulk_commit();
     }
-    tc::tc_fence_before();
   }
-  tc::bulk_wait0();
+  if (tid == 0) tc::bulk_wait0();
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
@@ -255,38 +299,81 @@ static int num_sms() {
   return n;
 }
 
-// Host launcher used by arb_coef_solve for 3D mixed precision.
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiled encode_fn() {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  });
+  return fn;
+}
+
+// Host launcher used by arb_coef_solve for 3D mixed precision.  The table is
+// written as a 2D tensor [rows][64] float32 (rows = ncells x nfield) through
+// 128-row x 32-float boxes in the 128-byte swizzled layout.
 int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *table, int32_t *status,
                    cudaStream_t s) {
-  if (!g->grid32) return ARB_ERR_INVALID;
+  if (!g->grid32 || ((uintptr_t)table & 15u)) return ARB_ERR_INVALID;
+  const EncodeTiled encode = encode_fn();
+  if (!encode) return ARB_ERR_CUDA;
   const size_t smem = sizeof(TcSmem) + 1024;
-  static_assert(3 * (sizeof(TcSmem) + 1024) > 228 * 1024, "a third CTA per SM would oversubscribe TMEM");
-  static bool attr = false;
-  if (!attr) {
+  static_assert(3 * (sizeof(TcSmem) + 1024 + 1024) > 228 * 1024, "a third CTA per SM would oversubscribe TMEM");
+  static_assert(offsetof(TcSmem, stage) % 1024 == 0, "swizzled boxes need 1 KB alignment");
+  static int per_sm = 0;
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [&] {
     const void *ks[3] = {(const void *)coef3_tc_kernel<1>, (const void *)coef3_tc_kernel<3>,
                          (const void *)coef3_tc_kernel<4>};
     for (const void *k : ks) {
-      if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-          cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
-        return ARB_ERR_CUDA;
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      if (e != cudaSuccess) attr_err = e;
     }
-    attr = true;
+    int dev = 0, smem_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    per_sm = (int)(smem_sm / (int64_t)(smem + 1024));
+    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
+  });
+  if (attr_err != cudaSuccess) return ARB_ERR_CUDA;
+  const int F = g->nfield;
+  if (F != 1 && F != 3 && F != 4) return ARB_ERR_INVALID;
+  // one tensor map covers at most 2^31 rows; larger solves go in chunks
+  const int64_t max_cells = ((int64_t)1 << 31) / F;
+  for (int64_t done = 0; done < ncells; done += max_cells) {
+    const int64_t nc = ncells - done < max_cells ? ncells - done : max_cells;
+    const int64_t rows = nc * F;
+    CUtensorMap tmap;
+    const cuuint64_t dims[2] = {64, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {64 * sizeof(float)};
+    const cuuint32_t box[2] = {32, TM};
+    const cuuint32_t estr[2] = {1, 1};
+    if (encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, table + done * F * 64, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return ARB_ERR_CUDA;
+    const int64_t tiles = (rows + TM - 1) / TM;
+    int64_t grid = (int64_t)num_sms() * per_sm;
+    if (grid > tiles) grid = tiles;
+    switch (F) {
+      case 1: coef3_tc_kernel<1><<<(unsigned)grid, NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
+      case 3: coef3_tc_kernel<3><<<(unsigned)grid, NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
+      default: coef3_tc_kernel<4><<<(unsigned)grid, NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
+    }
+    const int rc = launch_status();
+    if (rc != ARB_OK) return rc;
   }
-  const int64_t rows = ncells * g->nfield;
-  const int64_t tiles = (rows + TM - 1) / TM;
-  static int per_sm = 0;
-  if (!per_sm && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coef3_tc_kernel<4>, NT, smem) != cudaSuccess)
-    return ARB_ERR_CUDA;
-  per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
-  int64_t grid = (int64_t)num_sms() * per_sm;
-  if (grid > tiles) grid = tiles;
-  switch (g->nfield) {
-    case 1: coef3_tc_kernel<1><<<(unsigned)grid, NT, smem, s>>>(*g, cell0, ncells, table, status); break;
-    case 3: coef3_tc_kernel<3><<<(unsigned)grid, NT, smem, s>>>(*g, cell0, ncells, table, status); break;
-    case 4: coef3_tc_kernel<4><<<(unsigned)grid, NT, smem, s>>>(*g, cell0, ncells, table, status); break;
-    default: return ARB_ERR_INVALID;
-  }
-  return launch_status();
+  return ARB_OK;
 }
 
 }  // namespace arb

@@ -124,6 +124,15 @@ __device__ __forceinline__ void bulk_store(void *gdst, const void *ssrc, uint32_
                "r"(smem_u32(ssrc)), "r"(bytes)
                : "memory");
 }
+// 2D tiled tensor store shared -> global through a tensor map (a
+// __grid_constant__ kernel parameter); x is the inner coordinate in
+// elements, y the row.  Rows beyond the map's extent are not written.
+__device__ __forceinline__ void tma_store_2d(const void *tmap, const void *ssrc, int32_t x, int32_t y) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(tmap)),
+               "r"(x), "r"(y), "r"(smem_u32(ssrc))
+               : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read0() {
   asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");

@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--kernel-only", action="store_true", help="time only the query kernel (profiling)")
-    p.add_argument("--profile", default=None, choices=["step", "small", "small-table", "small-fp64"],
+    p.add_argument("--profile", default=None, choices=["step", "small", "small-table", "small-fp64", "small-coef"],
                    help="run a fixed workload for an ncu capture and exit (no timing, no JSON): "
                         "'step' = two full bench steps; 'small*' = 160^3 dipole field, 2.02e6 queries")
     return p.parse_args()
@@ -68,6 +68,12 @@ def run_profile(args):
         field, q, lo, hi, h = make_workload(dev)
         for _ in range(2):
             tricubic(field, "quiet", mode="both", precision=args.precision, strategy=args.strategy).Query(q)
+    elif args.profile == "small-coef":
+        # 96^3 'both' field: 804k cells x 4 fields x 64 float32 coefficients = 0.82 GB table
+        field = synth.dipole_field3(n=(96, 96, 96), seed=1, device=dev)
+        o = tricubic(field, "quiet", mode="both", precision=args.precision, strategy="table")
+        for _ in range(2):
+            o.allCoeffs()
     else:
         prec = "fp64" if args.profile == "small-fp64" else "mixed"
         strategy = "table" if args.profile == "small-table" else "otf"
