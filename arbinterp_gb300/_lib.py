@@ -53,6 +53,8 @@ SIGNATURES = {
     "arb_ingest_axes": (C.c_int, [_P, _I32, _I64, _I32, _I32, _I64, _P, _P, _P, C.c_size_t, _P, _P]),
     "arb_ingest_scatter": (C.c_int, [_P, _I32, _I64, _I32, _I32, _P, _I64, C.POINTER(C.c_int64), _I32,
                                      _P, _P, _P, _P, _P, _P]),
+    "arb_ingest_ordered": (C.c_int, [_P, _I32, _I64, _I32, _I32, _I32, _I64, _P, _P, _P, _P, _P, _P, C.c_size_t,
+                                     _P, _P]),
     "arb_fd_planes": (C.c_int, [C.POINTER(ArbGrid), _P, _P]),
     "arb_coef_solve": (C.c_int, [C.POINTER(ArbGrid), _I32, _I64, _I64, _P, _P, _P]),
     "arb_query_eval": (C.c_int, [C.POINTER(ArbGrid), _P, _I64, _I64, _I32, C.POINTER(ArbQueryOut), _P, _P]),

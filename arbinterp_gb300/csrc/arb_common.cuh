@@ -116,10 +116,38 @@ __host__ __device__ __forceinline__ unsigned long long ord_key_bits(unsigned lon
   return (b >> 63) ? ~b : (b | 0x8000000000000000ULL);
 }
 
+__device__ __forceinline__ void split_f32(double v, float &hi, float &lo);
+
 struct FastAxis {
   unsigned long long lo_key, hi_key;  // ord keys of IntMin / IntMax
   double lo, h, inv_h;
+  float loh, lol, ih, il;             // float32 pairs of IntMin and 1/h
+  int df;                             // the float32 double-float step applies on this axis
 };
+
+// Float32 pairs of IntMin and 1/h, and whether the double-float step of
+// coord_step_fast applies: the interpolation range spans at most 2^20 cells
+// from the origin ((|IntMin| + |IntMax|) / h <= 2^20) and the values lie where
+// float32 pairs hold them (0 or [2^-80, 2^100] in magnitude).
+__host__ __device__ inline void fast_axis_pairs(FastAxis &f, double lo, double hi, double h) {
+  const double ih = 1.0 / h;
+#ifdef __CUDA_ARCH__
+  split_f32(lo, f.loh, f.lol);
+  split_f32(ih, f.ih, f.il);
+#else
+  f.loh = (float)lo;
+  f.lol = (float)(lo - (double)f.loh);
+  f.ih = (float)ih;
+  f.il = (float)(ih - (double)f.ih);
+#endif
+  auto in_range = [](double v) {
+    const double m = v < 0 ? -v : v;
+    return m == 0.0 || (m >= 0x1p-80 && m <= 0x1p100);
+  };
+  const double alo = lo < 0 ? -lo : lo, ahi = hi < 0 ? -hi : hi;
+  f.df = (h > 0.0 && in_range(lo) && in_range(hi) && in_range(ih) && ih > 0.0 && (alo + ahi) * ih <= 0x1p20) ? 1
+                                                                                                         : 0;
+}
 
 // Mixed-precision coordinate step: the cell index is bit-exact (it equals
 // floor((q - IntMin) / h) with IEEE division, as the reference computes it)
@@ -149,6 +177,39 @@ __device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const F
       frac[a] = 0.f;
       continue;
     }
+    if (ax[a].df) {
+      // (q - IntMin) / h in float32 double-float arithmetic: q and IntMin
+      // as float pairs (residual 2^-48 relative), an exact two-sum of the
+      // high parts, times the pair of 1/h.  Error <= 2^-25 in cell units
+      // (span <= 2^20 cells); the reference's own float64 roundings move iu
+      // by <= 2^-31.  So the floor is the reference's whenever the fraction
+      // is 2^-20 or more away from a cell face; otherwise the float64 steps
+      // below decide.
+      float qh, ql;
+      split_f32(q, qh, ql);
+      const float sh = __fsub_rn(qh, ax[a].loh);
+      const float bv = __fsub_rn(sh, qh);
+      const float se = __fadd_rn(__fsub_rn(qh, __fsub_rn(sh, bv)), __fsub_rn(-ax[a].loh, bv));
+      const float st = __fadd_rn(se, __fsub_rn(ql, ax[a].lol));
+      const float ph = __fmul_rn(sh, ax[a].ih);
+      const float pe = __fmaf_rn(sh, ax[a].ih, -ph);
+      const float pl = __fmaf_rn(sh, ax[a].il, __fmaf_rn(st, ax[a].ih, pe));
+      float kf = __fsub_rn(__fadd_rn(ph, 8388608.f), 8388608.f);  // nearest integer (0 <= ph < 2^21)
+      if (kf > ph) kf = __fsub_rn(kf, 1.f);
+      float fr = __fadd_rn(__fsub_rn(ph, kf), pl);
+      if (fr < 0.f) {
+        kf = __fsub_rn(kf, 1.f);
+        fr = __fadd_rn(fr, 1.f);
+      } else if (fr >= 1.f) {
+        kf = __fadd_rn(kf, 1.f);
+        fr = __fsub_rn(fr, 1.f);
+      }
+      if (kf >= 0.f && fr >= 0x1p-20f && fr <= 1.f - 0x1p-20f) {
+        fl[a] = (int64_t)(__float_as_int(__fadd_rn(kf, 8388608.f)) - 0x4b000000);
+        frac[a] = fr;
+        continue;
+      }
+    }
     const double d = q - ax[a].lo;
     double iu = d * ax[a].inv_h;
     const unsigned long long b = (unsigned long long)__double_as_longlong(iu);
@@ -165,7 +226,9 @@ __device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const F
       redo = (fb < 8ULL) || (fb > one - 8ULL);
       // top 24 bits of the fraction, converted exactly, times 2^-24
       const unsigned f24 = (unsigned)(nf >= 24 ? (fb >> (nf - 24)) : (fb << (24 - nf)));
-      fr = __uint2float_rz(f24) * 5.9604644775390625e-08f;
+      // f24 * 2^-24 exactly, without an int->float conversion instruction
+      const float f23 = __fsub_rn(__uint_as_float(0x4b000000u | (f24 >> 1)), 8388608.f);
+      fr = __fmaf_rn(f23, 2.f, (f24 & 1u) ? 1.f : 0.f) * 5.9604644775390625e-08f;
     } else if (e < -1) {
       fr = __double2float_rn(iu);  // iu < 0.5: floor is 0
     }

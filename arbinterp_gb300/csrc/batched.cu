@@ -28,6 +28,7 @@ __device__ KParams make_kparams_dev(const arb_grid &g) {
     kp.ax[a].lo = lo;
     kp.ax[a].h = h;
     kp.ax[a].inv_h = 1.0 / h;
+    fast_axis_pairs(kp.ax[a], lo, hi, h);
   }
   return kp;
 }

@@ -151,6 +151,127 @@ __device__ __forceinline__ void load_row(const arb_grid &g, int64_t npts, int64_
     load_row64<F>(g.grid64, p, v);
 }
 
+// ---- 3D on-the-fly, float32 with gradient ----------------------------------
+// Each gradient component is a difference along its own axis; formed from
+// deltas to the cell corner it would inherit the float32 rounding of the
+// OTHER axes' variation (error ~ eps * sum_b h_b |f_b| / (h_a |f_a|), over
+// 1e-6 on coarse anisotropic grids).  So the gradient field is differenced
+// along each axis first, from the (hi, lo) grid words:
+//   d/dx: x-local deltas f[k][j][i] - f[k][j][1] per x-line,
+//   d/dy: y-local deltas f[k][j][i] - f[k][1][i] (line j = 1 of the layer),
+//   d/dz: z-local deltas f[k][j][i] - f[1][j][i] (layer k = 1),
+// then smoothed over the other two axes (positive-dominated weights, no
+// cancellation).  Values use corner deltas as before.  Layers and lines are
+// visited in the order 1, 0, 2, 3 so the local references are loaded first.
+template <int F>
+__device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KParams &kp, const int64_t c[3],
+                                                     const float frac[3], double val[F], double grad[3]) {
+  constexpr int G = F - 1;  // the field whose gradient is returned (scalar or |B|)
+  const int64_t nx = g.n[0], ny = g.n[1];
+  const int64_t npts = grid_points(g);
+  float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
+  cr_weights<float>(frac[0], wx);
+  cr_weights<float>(frac[1], wy);
+  cr_weights<float>(frac[2], wz);
+  cr_dweights<float>(frac[0], dx);
+  cr_dweights<float>(frac[1], dy);
+  cr_dweights<float>(frac[2], dz);
+  float rhi[F], rlo[F];
+  const int64_t pr = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
+#pragma unroll
+  for (int f = 0; f < F; ++f) g32_load<F>(g.grid32, npts, pr, f, rhi[f], rlo[f]);
+  float zh[4][4], zl[4][4], yh[4], yl[4];
+  float acc[F], gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+  for (int f = 0; f < F; ++f) acc[f] = 0.f;
+  constexpr int ORD[4] = {1, 0, 2, 3};
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk) {
+    const int k = ORD[kk];
+    float ay[F], ayx = 0.f, ayy = 0.f;
+#pragma unroll
+    for (int f = 0; f < F; ++f) ay[f] = 0.f;
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = ORD[jj];
+      const int64_t p = ((c[2] + k) * ny + (c[1] + j)) * nx + c[0];
+      float h[4], l[4], vv[4][3];
+      if (F == 1) {
+        const float2 *r = reinterpret_cast<const float2 *>(g.grid32) + p;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float2 a = __ldg(r + i);
+          h[i] = a.x;
+          l[i] = a.y;
+        }
+      } else {
+        const float4 *r4 = reinterpret_cast<const float4 *>(g.grid32) + p;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float4 a = __ldg(r4 + i);
+          vv[i][0] = a.x - rhi[0];
+          vv[i][1] = a.y - rhi[1 % F];
+          vv[i][2] = a.z - rhi[2 % F];
+          h[i] = a.w;
+          l[i] = __ldg(g.grid32 + npts * 4 + p + i);
+        }
+      }
+      if (k == 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          zh[j][i] = h[i];
+          zl[j][i] = l[i];
+        }
+      }
+      if (j == 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          yh[i] = h[i];
+          yl[i] = l[i];
+        }
+      }
+      // values: corner deltas
+      float d[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) d[i] = (h[i] - rhi[G]) + (l[i] - rlo[G]);
+      ay[G] += wy[j] * (wx[0] * d[0] + wx[1] * d[1] + wx[2] * d[2] + wx[3] * d[3]);
+      if (F == 4) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+          ay[f] += wy[j] * (wx[0] * vv[0][f] + wx[1] * vv[1][f] + wx[2] * vv[2][f] + wx[3] * vv[3][f]);
+      }
+      // d/dx from x-local deltas
+      const float e0 = (h[0] - h[1]) + (l[0] - l[1]);
+      const float e2 = (h[2] - h[1]) + (l[2] - l[1]);
+      const float e3 = (h[3] - h[1]) + (l[3] - l[1]);
+      ayx += wy[j] * (dx[0] * e0 + dx[2] * e2 + dx[3] * e3);
+      // d/dy from y-local deltas
+      if (j != 1) {
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) s += wx[i] * ((h[i] - yh[i]) + (l[i] - yl[i]));
+        ayy += dy[j] * s;
+      }
+      // d/dz from z-local deltas
+      if (k != 1) {
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) s += wx[i] * ((h[i] - zh[j][i]) + (l[i] - zl[j][i]));
+        gz += (dz[k] * wy[j]) * s;
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < F; ++f) acc[f] += wz[k] * ay[f];
+    gx += wz[k] * ayx;
+    gy += wz[k] * ayy;
+  }
+#pragma unroll
+  for (int f = 0; f < F; ++f) val[f] = f2d_exact(rhi[f] + (rlo[f] + acc[f]));
+  grad[0] = f2d_exact(gx * kp.inv_hf[0]);
+  grad[1] = f2d_exact(gy * kp.inv_hf[1]);
+  grad[2] = f2d_exact(gz * kp.inv_hf[2]);
+}
+
 // ---- 3D on-the-fly ---------------------------------------------------------
 template <int F, bool MIXED>
 __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, const int64_t c[3],
@@ -158,6 +279,10 @@ __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, 
                                           double val[F], double grad[3]) {
   using T = typename std::conditional<MIXED, float, double>::type;
   constexpr bool GRAD = (F != 3);
+  if constexpr (MIXED && GRAD) {
+    eval_otf3_mixed_grad<F>(g, kp, c, frac, val, grad);
+    return;
+  }
   const int64_t nx = g.n[0], ny = g.n[1];
   T wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
   cr_weights<T>((T)frac[0], wx);
@@ -475,6 +600,7 @@ static inline KParams make_kparams(const arb_grid *g) {
     kp.ax[a].lo = lo;
     kp.ax[a].h = h;
     kp.ax[a].inv_h = 1.0 / h;
+    fast_axis_pairs(kp.ax[a], lo, hi, h);
   }
   return kp;
 }

@@ -10,6 +10,8 @@
 // pass with coalesced writes, with no global sort.  Rows that are not a full tensor
 // grid (missing or duplicate points, a coordinate not on its axis) set
 // ARB_ERR_IRREGULAR_GRID instead of silently producing garbage.
+#include <climits>
+
 #include "arb_common.cuh"
 
 namespace arb {
@@ -176,6 +178,135 @@ __global__ void __launch_bounds__(256) ingest_index_kernel(const TF *field, int6
   }
 }
 
+// field value as float64 without the float64 pipe
+template <typename TF>
+__device__ __forceinline__ double to_f64(TF v) {
+  if constexpr (sizeof(TF) == 8)
+    return (double)v;
+  else
+    return f2d_exact(v);
+}
+
+// ||(bx, by, bz)|| for float64 components as a float32 pair hi + lo, in
+// float32 arithmetic only: the components are rescaled by the power of two
+// of the largest (exact, on the exponent bits), then double-float: error-free
+// squares via FMA, two-sum accumulation, one Newton correction of the float32
+// square root.  Accurate to ~2^-46 relative, below the pair's own
+// resolution.  Returns false (caller takes the float64 norm) for a largest
+// component outside [2^-90, 2^90], zeros, infinities and NaN.
+__device__ __forceinline__ bool norm_f32pair(double bx, double by, double bz, float &hi, float &lo) {
+  const long long bb[3] = {__double_as_longlong(bx), __double_as_longlong(by), __double_as_longlong(bz)};
+  int ex[3], em = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ex[a] = (int)((bb[a] >> 52) & 0x7ff);
+    em = max(em, ex[a]);
+  }
+  if (em < 1023 - 90 || em > 1023 + 90) return false;
+  const int sc = em - 1023;
+  float h[3], l[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (ex[a] - sc >= 1) {
+      split_f32(__longlong_as_double(bb[a] - ((long long)sc << 52)), h[a], l[a]);
+    } else {
+      h[a] = 0.f;  // below 2^-1022 of the largest: no contribution
+      l[a] = 0.f;
+    }
+  }
+  float s = 0.f, e = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float p = __fmul_rn(h[a], h[a]);
+    const float pe = __fmaf_rn(h[a], h[a], -p);           // exact error of the square
+    const float t = __fadd_rn(s, p);                       // two-sum s + p
+    const float bp = __fsub_rn(t, s);
+    const float te = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    e = __fadd_rn(e, __fadd_rn(te, __fmaf_rn(2.f * h[a], l[a], pe)));
+    s = t;
+  }
+  const float S = __fadd_rn(s, e), Slo = __fsub_rn(e, __fsub_rn(S, s));   // renormalise
+  const float r = __fsqrt_rn(S);                           // S in [1, 12)
+  const float res = __fadd_rn(__fmaf_rn(-r, r, S), Slo);   // S + Slo - r^2
+  const float rc = __fmul_rn(res, __fdividef(0.5f, r));
+  const float h0 = __fadd_rn(r, rc);
+  const float f = __int_as_float((sc + 127) << 23);        // 2^sc, exact rescale
+  hi = h0 * f;
+  lo = __fsub_rn(rc, __fsub_rn(h0, r)) * f;
+  return true;
+}
+
+// Per-mode interpolated fields of one row written to grid slot `dest`:
+// grid64, grid32 (hi/lo split, layout of g32_load in arb_common.cuh) and the
+// raw value columns.  With grid32 (mixed precision) and float64 components
+// the norm comes from norm_f32pair (float32 pipe); otherwise it is the
+// float64 norm NumPy computes.
+template <typename TF, int KIND>
+__device__ __forceinline__ void write_slot(const TF *row, int64_t dest, int64_t npts, int dim, double *grid64,
+                                           float *grid32, double *raw_out) {
+  constexpr int F = (KIND == ARB_KIND_VECTOR) ? 3 : (KIND == ARB_KIND_BOTH ? 4 : 1);
+  double out[4];
+  float nhi = 0.f, nlo = 0.f;
+  bool nsplit = false;
+  if (KIND == ARB_KIND_SCALAR) {
+    out[0] = to_f64(row[dim]);
+  } else {
+    const TF bx = row[dim], by = row[dim + 1], bz = row[dim + 2];
+    out[0] = to_f64(bx);
+    out[1] = to_f64(by);
+    out[2] = to_f64(bz);
+    if (KIND == ARB_KIND_NORM || KIND == ARB_KIND_BOTH) {
+      // ||B|| at the grid point in the field's own precision, as NumPy's
+      // norm evaluates it: sqrt((bx*bx + by*by) + bz*bz).
+      double nrm;
+      if (sizeof(TF) == 8 && grid32 && norm_f32pair(out[0], out[1], out[2], nhi, nlo)) {
+        nrm = f2d_exact(nhi) + f2d_exact(nlo);
+        nsplit = true;
+      } else if (sizeof(TF) == 8) {
+        nrm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn((double)bx, (double)bx), __dmul_rn((double)by, (double)by)),
+                                   __dmul_rn((double)bz, (double)bz)));
+      } else {
+        nrm = f2d_exact(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn((float)bx, (float)bx), __fmul_rn((float)by, (float)by)),
+                                             __fmul_rn((float)bz, (float)bz))));
+      }
+      if (KIND == ARB_KIND_NORM)
+        out[0] = nrm;
+      else
+        out[3] = nrm;
+    }
+    if (raw_out) {
+      raw_out[dest * 3 + 0] = (double)bx;
+      raw_out[dest * 3 + 1] = (double)by;
+      raw_out[dest * 3 + 2] = (double)bz;
+    }
+  }
+  if (F == 4) {
+    reinterpret_cast<double2 *>(grid64)[dest * 2] = make_double2(out[0], out[1 % F]);
+    reinterpret_cast<double2 *>(grid64)[dest * 2 + 1] = make_double2(out[2 % F], out[3 % F]);
+  } else {
+#pragma unroll
+    for (int f = 0; f < F; ++f) grid64[dest * F + f] = out[f];
+  }
+  if (grid32) {
+    float hi[4], lo[4];
+#pragma unroll
+    for (int f = 0; f < F; ++f) split_f32(out[f], hi[f], lo[f]);
+    if (nsplit) {
+      hi[F - 1] = nhi;
+      lo[F - 1] = nlo;
+    }
+    if (F == 4) {
+      reinterpret_cast<float4 *>(grid32)[dest] = make_float4(hi[0], hi[1 % F], hi[2 % F], hi[3 % F]);
+      grid32[npts * 4 + dest] = lo[3 % F];
+    } else if (F == 3) {
+      reinterpret_cast<float4 *>(grid32)[dest] = make_float4(hi[0], hi[1 % F], hi[2 % F], 0.f);
+    } else {
+      reinterpret_cast<float2 *>(grid32)[dest] = make_float2(hi[0], lo[0]);
+    }
+  }
+  if (KIND == ARB_KIND_SCALAR && raw_out) raw_out[dest] = out[0];
+}
+
 // Pass 2 (grid order): each slot reads its row and writes the per-mode
 // interpolated fields with coalesced stores.
 template <typename TF, int KIND>
@@ -183,7 +314,6 @@ __global__ void __launch_bounds__(256) ingest_gather_kernel(const TF *field, int
                                                             int dim, const uint32_t *inv,
                                                             double *grid64, float *grid32,
                                                             double *raw_out, int32_t *status) {
-  constexpr int F = (KIND == ARB_KIND_VECTOR) ? 3 : (KIND == ARB_KIND_BOTH ? 4 : 1);
   for (int64_t dest = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; dest < npts;
        dest += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t src = inv[dest];
@@ -191,63 +321,159 @@ __global__ void __launch_bounds__(256) ingest_gather_kernel(const TF *field, int
       set_status(status, ARB_ERR_IRREGULAR_GRID);
       continue;
     }
-    const TF *row = field + (int64_t)src * ncol;
-    double out[4];
-    if (KIND == ARB_KIND_SCALAR) {
-      out[0] = (double)row[dim];
-    } else {
-      const TF bx = row[dim], by = row[dim + 1], bz = row[dim + 2];
-      out[0] = (double)bx;
-      out[1] = (double)by;
-      out[2] = (double)bz;
-      if (KIND == ARB_KIND_NORM || KIND == ARB_KIND_BOTH) {
-        // ||B|| at the grid point in the field's own precision, as NumPy's
-        // norm evaluates it: sqrt((bx*bx + by*by) + bz*bz).
-        double nrm;
-        if (sizeof(TF) == 8) {
-          nrm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn((double)bx, (double)bx),
-                                               __dmul_rn((double)by, (double)by)),
-                                     __dmul_rn((double)bz, (double)bz)));
-        } else {
-          nrm = (double)__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn((float)bx, (float)bx),
-                                                       __fmul_rn((float)by, (float)by)),
-                                             __fmul_rn((float)bz, (float)bz)));
-        }
-        if (KIND == ARB_KIND_NORM)
-          out[0] = nrm;
-        else
-          out[3] = nrm;
-      }
-      if (raw_out) {
-        raw_out[dest * 3 + 0] = (double)bx;
-        raw_out[dest * 3 + 1] = (double)by;
-        raw_out[dest * 3 + 2] = (double)bz;
+    write_slot<TF, KIND>(field + (int64_t)src * ncol, dest, npts, dim, grid64, grid32, raw_out);
+  }
+}
+
+// ---- single-pass ingest of rows in meshgrid order ---------------------------
+// Rows in meshgrid order are lexicographic over the axes in some axis order,
+// each axis ascending or descending: row = sum_a stride_a * j_a with j_a the
+// sample's position along the row order (i_a or n_a - 1 - i_a) and the
+// strides the running products of the axis lengths.  NumPy's meshgrid +
+// reshape and the reference's own sort (ARB:530) produce such orders.  The
+// probe reads the axes straight off the lines through row 0 (the lines the
+// axis pass collects); the gather then maps every grid slot to its row
+// arithmetically and checks the row's coordinates against the slot's axis
+// samples, so a field in any other order is detected, never misplaced.
+struct OrderWork {
+  int64_t stride[4];  // signed: negative for an axis descending along the rows
+  int64_t n[4];
+  int32_t ok;
+};
+
+template <typename TF>
+__global__ void __launch_bounds__(256) ordered_probe_kernel(const TF *field, int64_t npts, int ncol, int dim,
+                                                            int64_t cap, double *axis_out, int64_t *axis_count,
+                                                            OrderWork *w, int32_t *status) {
+  __shared__ long long first_stop;
+  const int tid = threadIdx.x;
+  double r0[4];
+  for (int a = 0; a < dim; ++a) r0[a] = (double)field[a];
+  int64_t stride = 1;
+  unsigned used = 0;
+  bool ok = true;
+  for (int step = 0; step < dim && ok; ++step) {
+    if (stride >= npts) {
+      ok = false;
+      break;
+    }
+    // the one axis that changes between row 0 and row `stride`
+    int which = -1, nd = 0;
+    for (int a = 0; a < dim; ++a) {
+      const double v = (double)field[stride * ncol + a];
+      if (!(v == r0[a])) {
+        ++nd;
+        which = a;
       }
     }
-    if (F == 4) {
-      reinterpret_cast<double2 *>(grid64)[dest * 2] = make_double2(out[0], out[1 % F]);
-      reinterpret_cast<double2 *>(grid64)[dest * 2 + 1] = make_double2(out[2 % F], out[3 % F]);
-    } else {
+    if (nd != 1 || ((used >> which) & 1u)) {
+      ok = false;
+      break;
+    }
+    const bool asc = (double)field[stride * ncol + which] > r0[which];
+    // line length: first k >= 1 whose row leaves the line through row 0 or
+    // breaks the strict monotonicity of the axis samples
+    int64_t n = -1;
+    for (int64_t base = 1; base <= cap + 1; base += blockDim.x) {
+      if (tid == 0) first_stop = LLONG_MAX;
+      __syncthreads();
+      const int64_t k = base + tid;
+      bool stop = k * stride >= npts;
+      if (!stop) {
+        const TF *row = field + k * stride * ncol;
+        for (int a = 0; a < dim; ++a)
+          if (a != which && !((double)row[a] == r0[a])) stop = true;
+        const double cur = (double)row[which], prev = (double)field[(k - 1) * stride * ncol + which];
+        if (!(asc ? cur > prev : cur < prev)) stop = true;
+      }
+      if (stop) atomicMin(&first_stop, (long long)k);
+      __syncthreads();
+      const long long fs = first_stop;
+      __syncthreads();
+      if (fs != LLONG_MAX) {
+        n = fs;
+        break;
+      }
+    }
+    if (n < 4 || n > cap) {
+      ok = false;
+      break;
+    }
+    for (int64_t k = tid; k < n; k += blockDim.x)
+      axis_out[which * cap + (asc ? k : n - 1 - k)] = (double)field[k * stride * ncol + which];
+    if (tid == 0) {
+      w->stride[which] = asc ? stride : -stride;
+      w->n[which] = n;
+      axis_count[which] = n;
+    }
+    used |= 1u << which;
+    stride *= n;
+  }
+  if (ok && stride != npts) ok = false;
+  if (tid == 0) {
+    w->ok = ok ? 1 : 0;
+    if (!ok) set_status(status, ARB_ERR_IRREGULAR_GRID);
+  }
+}
+
+// One field row into registers: 16-byte loads when the row is 16-byte
+// aligned (float64 rows of an even column count), scalar loads otherwise.
+template <typename TF, int NC>
+__device__ __forceinline__ void load_field_row(const TF *row, TF v[NC]) {
+  if constexpr (sizeof(TF) == 8 && NC % 2 == 0) {
+    const double2 *r2 = reinterpret_cast<const double2 *>(row);
 #pragma unroll
-      for (int f = 0; f < F; ++f) grid64[dest * F + f] = out[f];
+    for (int k = 0; k < NC / 2; ++k) {
+      const double2 t = __ldg(r2 + k);
+      v[2 * k] = t.x;
+      v[2 * k + 1] = t.y;
     }
-    if (grid32) {
-      float hi[4], lo[4];
+  } else if constexpr (sizeof(TF) == 4 && NC == 4) {
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(row));
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+    v[3] = t.w;
+  } else {
 #pragma unroll
-      for (int f = 0; f < F; ++f) {
-        split_f32(out[f], hi[f], lo[f]);
-      }
-      // layout: see g32_load (arb_common.cuh)
-      if (F == 4) {
-        reinterpret_cast<float4 *>(grid32)[dest] = make_float4(hi[0], hi[1 % F], hi[2 % F], hi[3 % F]);
-        grid32[npts * 4 + dest] = lo[3 % F];
-      } else if (F == 3) {
-        reinterpret_cast<float4 *>(grid32)[dest] = make_float4(hi[0], hi[1 % F], hi[2 % F], 0.f);
-      } else {
-        reinterpret_cast<float2 *>(grid32)[dest] = make_float2(hi[0], lo[0]);
-      }
+    for (int k = 0; k < NC; ++k) v[k] = __ldg(row + k);
+  }
+}
+
+template <typename TF, int KIND, int DIM>
+__global__ void __launch_bounds__(256) ordered_gather_kernel(const TF *field, int64_t npts, int ncol,
+                                                             const double *axes, int64_t cap, const OrderWork *w,
+                                                             double *grid64, float *grid32, double *raw_out,
+                                                             int32_t *status) {
+  if (!w->ok) return;
+  uint32_t nn[DIM];
+  int64_t st[DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    nn[a] = (uint32_t)w->n[a];
+    st[a] = w->stride[a];
+  }
+  for (int64_t dest = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; dest < npts;
+       dest += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t u = (uint32_t)dest;  // npts < 2^32
+    int64_t src = 0;
+    uint32_t idx[DIM];
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) {
+      const uint32_t q = a + 1 < DIM ? u / nn[a] : 0u;
+      idx[a] = u - q * nn[a];
+      u = q;
+      src += st[a] > 0 ? (int64_t)idx[a] * st[a] : (int64_t)(nn[a] - 1u - idx[a]) * (-st[a]);
     }
-    if (KIND == ARB_KIND_SCALAR && raw_out) raw_out[dest] = out[0];
+    constexpr int NC = DIM + (KIND == ARB_KIND_SCALAR ? 1 : 3);
+    TF row[NC];
+    load_field_row<TF, NC>(field + src * NC, row);
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)  // bitwise, as the general path's key lookup
+      ok &= __double_as_longlong(to_f64(row[a])) == __double_as_longlong(__ldg(axes + a * cap + idx[a]));
+    if (!ok) set_status(status, ARB_ERR_IRREGULAR_GRID);
+    write_slot<TF, KIND>(row, dest, npts, DIM, grid64, grid32, raw_out);
   }
 }
 
@@ -263,7 +489,7 @@ using namespace arb;
 
 extern "C" size_t arb_ingest_axes_work_bytes(int32_t dim) {
   (void)dim;
-  return sizeof(AxesWork) + 256;
+  return (sizeof(AxesWork) > sizeof(OrderWork) ? sizeof(AxesWork) : sizeof(OrderWork)) + 256;
 }
 
 extern "C" int arb_ingest_axes(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
@@ -348,6 +574,52 @@ extern "C" int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64
   }
 #undef ARB_GATHER_KIND
 #undef ARB_GATHER
+  return launch_status();
+}
+
+extern "C" int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                                  int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,
+                                  int64_t *axis_count, double *grid64, float *grid32, double *raw_out,
+                                  void *work, size_t work_bytes, int32_t *status, arb_stream_t stream) {
+  if (!field || !axis_out || !axis_count || !grid64 || !work || !status) return ARB_ERR_INVALID;
+  if ((dim != 3 && dim != 4) || npts <= 0 || axis_cap <= 0 || axis_cap > ARB_MAX_AXIS_CAP ||
+      work_bytes < arb_ingest_axes_work_bytes(dim))
+    return ARB_ERR_INVALID;
+  const int nval = ncol - dim;
+  if (kind == ARB_KIND_SCALAR ? nval != 1 : nval != 3) return ARB_ERR_INVALID;
+  if (npts >= (int64_t)0xffffffffLL) return ARB_ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  OrderWork *w = (OrderWork *)work;
+  if (field_is_f32)
+    ordered_probe_kernel<float><<<1, 256, 0, s>>>((const float *)field, npts, ncol, dim, axis_cap, axis_out,
+                                                  axis_count, w, status);
+  else
+    ordered_probe_kernel<double><<<1, 256, 0, s>>>((const double *)field, npts, ncol, dim, axis_cap, axis_out,
+                                                   axis_count, w, status);
+  const int T = 256;
+  const int B = grid_blocks(npts, T);
+#define ARB_OGATHER(TF, K)                                                                              \
+  if (dim == 3)                                                                                         \
+    ordered_gather_kernel<TF, K, 3><<<B, T, 0, s>>>((const TF *)field, npts, ncol, axis_out, axis_cap, w, \
+                                                    grid64, grid32, raw_out, status);                     \
+  else                                                                                                  \
+    ordered_gather_kernel<TF, K, 4><<<B, T, 0, s>>>((const TF *)field, npts, ncol, axis_out, axis_cap, w, \
+                                                    grid64, grid32, raw_out, status)
+#define ARB_OGATHER_KIND(TF)                                         \
+  switch (kind) {                                                    \
+    case ARB_KIND_SCALAR: ARB_OGATHER(TF, ARB_KIND_SCALAR); break;   \
+    case ARB_KIND_VECTOR: ARB_OGATHER(TF, ARB_KIND_VECTOR); break;   \
+    case ARB_KIND_NORM: ARB_OGATHER(TF, ARB_KIND_NORM); break;       \
+    case ARB_KIND_BOTH: ARB_OGATHER(TF, ARB_KIND_BOTH); break;       \
+    default: return ARB_ERR_INVALID;                                 \
+  }
+  if (field_is_f32) {
+    ARB_OGATHER_KIND(float)
+  } else {
+    ARB_OGATHER_KIND(double)
+  }
+#undef ARB_OGATHER_KIND
+#undef ARB_OGATHER
   return launch_status();
 }
 

@@ -286,6 +286,225 @@ __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KPar
   }
 }
 
+// ---- bin-staged evaluation (3D, mixed, 8^3-cell bins) -------------------------
+// One CTA per bin (round-robin over bins): the bin's footprint of 11^3 grid
+// points (8 cells + 3 per axis) is copied into shared memory with cp.async,
+// double-buffered so the next bin's copy overlaps this bin's queries, and
+// every query of the bin gathers its 4x4x4 block from shared memory.  Reading
+// the block from L1 instead costs ~3 L1 wavefronts per (query, x-row) because
+// the 8 queries of a warp touch 16 scattered 64-byte and 16-byte segments;
+// from shared memory it is about one.
+constexpr int BIN_EDGE = 8;
+constexpr int TILE_EDGE = BIN_EDGE + 3;
+constexpr int TILE_PTS = TILE_EDGE * TILE_EDGE * TILE_EDGE;
+
+template <int F>
+struct BinTile;
+template <>
+struct BinTile<4> {          // (hi_x, hi_y, hi_z, hi_n) and lo_n per point
+  float4 hi[TILE_PTS];
+  float lo[TILE_PTS];
+};
+template <>
+struct BinTile<1> {          // (hi, lo) per point
+  float2 v[TILE_PTS];
+};
+
+__device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *sdst, const void *gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// grid-point origin of bin b (x fastest)
+__device__ __forceinline__ void bin_origin(int64_t b, const BinGeom &bg, int64_t o[3]) {
+  o[0] = (b % bg.nb[0]) * BIN_EDGE;
+  const int64_t r = b / bg.nb[0];
+  o[1] = (r % bg.nb[1]) * BIN_EDGE;
+  o[2] = (r / bg.nb[1]) * BIN_EDGE;
+}
+
+// Copy bin b's footprint into `t` (points outside the grid are skipped: no
+// cell of the bin reads them).
+template <int F>
+__device__ __forceinline__ void load_bin_tile(const arb_grid &g, const BinGeom &bg, int64_t b, BinTile<F> &t) {
+  int64_t o[3];
+  bin_origin(b, bg, o);
+  const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  const int64_t npts = nx * ny * nz;
+  for (int e = threadIdx.x; e < TILE_PTS; e += blockDim.x) {
+    const int lx = e % TILE_EDGE, r = e / TILE_EDGE;
+    const int ly = r % TILE_EDGE, lz = r / TILE_EDGE;
+    const int64_t x = o[0] + lx, y = o[1] + ly, z = o[2] + lz;
+    if (x >= nx || y >= ny || z >= nz) continue;
+    const int64_t p = (z * ny + y) * nx + x;
+    if (F == 4) {
+      cp_async16(&reinterpret_cast<BinTile<4> &>(t).hi[e], reinterpret_cast<const float4 *>(g.grid32) + p);
+      cp_async4(&reinterpret_cast<BinTile<4> &>(t).lo[e], g.grid32 + npts * 4 + p);
+    } else {
+      cp_async8(&reinterpret_cast<BinTile<1> &>(t).v[e], reinterpret_cast<const float2 *>(g.grid32) + p);
+    }
+  }
+}
+
+template <int F>
+__global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
+                                                       arb_query_out o, SortedWork w) {
+  extern __shared__ __align__(16) unsigned char bin_smem[];
+  BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(bin_smem);
+  const int lane = threadIdx.x & 31;
+  const int p = lane & 3;
+  const unsigned mask = 0xfu << (lane & 28);
+  const int64_t nbins = bg.nbins;
+  int stage = 0;
+  int64_t b = blockIdx.x;
+  // bins with no query need no copy
+  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb + 1] - (int64_t)w.hist[bb] : 0; };
+  if (count(b) > 0) load_bin_tile<F>(g, bg, b, tiles[0]);
+  cp_async_commit();
+  for (; b < nbins; b += gridDim.x) {
+    const int64_t bn = b + gridDim.x;
+    if (count(bn) > 0) load_bin_tile<F>(g, bg, bn, tiles[stage ^ 1]);
+    cp_async_commit();
+    const int64_t t0 = w.hist[b], t1 = w.hist[b + 1];
+    cp_async_wait1();
+    __syncthreads();
+    if (t1 > t0) {
+      const BinTile<F> &T = tiles[stage];
+      int64_t og[3];
+      bin_origin(b, bg, og);
+      if (F == 4) {
+        // 4 lanes per query, lane p owning x offset p of every block row
+        for (int64_t t = t0 + (threadIdx.x >> 2); t < t1; t += blockDim.x >> 2) {
+          const unsigned long long cw = w.s_cell[t];
+          const int64_t i = w.s_row[t];
+          int64_t c[3];
+          unpack_cell<3>(cw, c);
+          const int lp = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));
+          const float *fr = reinterpret_cast<const float *>(w.s_frac) + t * 3;
+          const float fx = fr[0], fy = fr[1], fz = fr[2];
+          float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
+          cr_weights<float>(fx, wx);
+          cr_dweights<float>(fx, dx);
+          cr_weights<float>(fy, wy);
+          cr_dweights<float>(fy, dy);
+          cr_weights<float>(fz, wz);
+          cr_dweights<float>(fz, dz);
+          const int lref = lp + TILE_EDGE * TILE_EDGE + TILE_EDGE + 1;
+          const float nref = reinterpret_cast<const BinTile<4> &>(T).hi[lref].w;
+          const float rlo = reinterpret_cast<const BinTile<4> &>(T).lo[lref];
+          // Components (values only) accumulate raw float32 values; |B|
+          // accumulates deltas to the corner so its derivatives keep full
+          // relative precision.  y first, then z: d/dz reuses the layer sums.
+          float Sx = 0.f, Sy_ = 0.f, Sz_ = 0.f, Sn = 0.f, Gy = 0.f, Gz = 0.f;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            float ax = 0.f, ay = 0.f, az = 0.f, an = 0.f, gy = 0.f;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int e = lp + (k * TILE_EDGE + j) * TILE_EDGE + p;
+              const float4 v = reinterpret_cast<const BinTile<4> &>(T).hi[e];
+              const float lo = reinterpret_cast<const BinTile<4> &>(T).lo[e];
+              const float dn = (v.w - nref) + (lo - rlo);
+              ax += wy[j] * v.x;
+              ay += wy[j] * v.y;
+              az += wy[j] * v.z;
+              an += wy[j] * dn;
+              gy += dy[j] * dn;
+            }
+            Sx += wz[k] * ax;
+            Sy_ += wz[k] * ay;
+            Sz_ += wz[k] * az;
+            Sn += wz[k] * an;
+            Gy += wz[k] * gy;
+            Gz += dz[k] * an;
+          }
+          float Vx = wx[p] * Sx, Vy = wx[p] * Sy_, Vz = wx[p] * Sz_, Vn = wx[p] * Sn;
+          float Gx = dx[p] * Sn;
+          Gy *= wx[p];
+          Gz *= wx[p];
+#pragma unroll
+          for (int off = 1; off <= 2; off <<= 1) {
+            Vx += __shfl_xor_sync(mask, Vx, off);
+            Vy += __shfl_xor_sync(mask, Vy, off);
+            Vz += __shfl_xor_sync(mask, Vz, off);
+            Vn += __shfl_xor_sync(mask, Vn, off);
+            Gx += __shfl_xor_sync(mask, Gx, off);
+            Gy += __shfl_xor_sync(mask, Gy, off);
+            Gz += __shfl_xor_sync(mask, Gz, off);
+          }
+          if (p == 0) {
+            if (o.comps) {
+              o.comps[i * 3 + 0] = f2d_exact(Vx);
+              o.comps[i * 3 + 1] = f2d_exact(Vy);
+              o.comps[i * 3 + 2] = f2d_exact(Vz);
+            }
+          } else if (p == 1) {
+            if (o.norms) o.norms[i] = f2d_exact(nref + (rlo + Vn));
+          } else if (p == 2) {
+            if (o.grads) {
+              o.grads[i * 3 + 0] = f2d_exact(Gx * kp.inv_hf[0]);
+              o.grads[i * 3 + 1] = f2d_exact(Gy * kp.inv_hf[1]);
+              o.grads[i * 3 + 2] = f2d_exact(Gz * kp.inv_hf[2]);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();  // this stage is refilled two bins later
+    stage ^= 1;
+  }
+  // records that need no evaluation (out of volume, NaN, sentinel column)
+  for (int64_t t = (int64_t)w.hist[nbins] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long cw = w.s_cell[t];
+    write_const<3, F>(o, w.s_row[t], (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
+  }
+}
+
+static int sm_count_sorted() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 148;
+  }
+  return n;
+}
+
+// Launches the bin-staged kernel when it applies (3D, mixed, 'both' fields,
+// 8^3-cell bins); returns false otherwise.
+static bool launch_eval_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
+                            const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
+  if (g->dim != 3 || g->nfield != 4 || bg.shift != 3) return false;
+  const size_t smem = 2 * sizeof(BinTile<4>);
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(eval_bin_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return false;
+    attr = true;
+  }
+  int64_t grid = (int64_t)sm_count_sorted() * 3;  // 3 resident per SM (registers)
+  if (grid > bg.nbins) grid = bg.nbins;
+  if (grid < 1) grid = 1;
+  eval_bin_kernel<4><<<(unsigned)grid, 256, smem, s>>>(*g, kp, bg, nq, *out, w);
+  return true;
+}
+
 template <int DIM, bool MIXED>
 static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, double *q, int64_t nq,
                        int64_t qs, int wb, const arb_query_out *out, int32_t *status, const SortedWork &w,
@@ -301,6 +520,7 @@ static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, 
 template <int DIM, bool MIXED>
 static void launch_eval(const arb_grid *g, const KParams &kp, int64_t nq, const arb_query_out *out,
                         const SortedWork &w, bool table, cudaStream_t s) {
+  if (DIM == 3 && MIXED && !table && launch_eval_bin(g, kp, bin_geom(g), nq, out, w, s)) return;
   const int TE = DIM == 3 ? 256 : 128;
   const unsigned BE = (unsigned)((nq + TE - 1) / TE);
 #define ES(FF, TAB) eval_sorted_kernel<DIM, FF, MIXED, TAB><<<BE, TE, 0, s>>>(*g, kp, nq, *out, w)

@@ -42,6 +42,7 @@ __version__ = "1.8"
 
 _F = {_lib.KIND_SCALAR: 1, _lib.KIND_VECTOR: 3, _lib.KIND_NORM: 1, _lib.KIND_BOTH: 4}
 _AXIS_CAP = 1 << 17
+_ORDERED_INGEST = True      # try the single-pass ingest for rows in meshgrid order first
 
 _BANNERS = {
     "scalar": "--- Scalar field, ignoring switches, interpolating for magnitude and gradient --- \n",
@@ -143,24 +144,6 @@ class _Interpolant:
         work = torch.empty(int(wb), dtype=torch.uint8, device=dev)
         status = torch.zeros(1, dtype=torch.int32, device=dev)
         s = _stream()
-        check(L.arb_ingest_axes(ft.data_ptr(), is32, npts, ncol, dim, cap, axes.data_ptr(),
-                                counts.data_ptr(), work.data_ptr(), wb, status.data_ptr(), s),
-              "arb_ingest_axes")
-        st = L.arb_status_fetch(status.data_ptr(), s)
-        n = [int(v) for v in counts.cpu()]
-        if st & _lib.ARB_ERR_CAPACITY:
-            raise ValueError(f"an axis has more than {cap} grid samples")
-        if st:
-            raise ValueError("field rows are not a regular grid (NaN coordinates or duplicate points)")
-        if any(v < 4 for v in n):
-            raise ValueError("every axis needs at least 4 grid points")
-        if int(np.prod(n)) != npts:
-            raise ValueError(f"field rows do not form a full regular grid: {npts} rows, axes {n}")
-        ax64 = axes[: dim * cap].view(dim, cap)
-        self._axes_dev = [ax64[a, : n[a]].clone() for a in range(dim)]
-        ax = [t.cpu().numpy().astype(self._field_dtype) for t in self._axes_dev]
-        self._n = n
-        self._npts = npts
         kind, F = self._kind, self._F
         grid64 = torch.empty(npts * F, dtype=torch.float64, device=dev)
         # mixed-precision grid: F=1 (hi, lo); F=3 float4 of hi; F=4 float4 of hi + lo of |B|
@@ -168,16 +151,44 @@ class _Interpolant:
         grid32 = (torch.empty(npts * g32_floats, dtype=torch.float32, device=dev)
                   if self.precision == "mixed" else None)
         raw = torch.empty(npts * 3, dtype=torch.float64, device=dev) if kind == _lib.KIND_NORM else None
-        claim = torch.empty(npts, dtype=torch.int32, device=dev)
-        n_c = (ctypes.c_int64 * 4)(*(n + [1] * (4 - dim)))
-        check(L.arb_ingest_scatter(ft.data_ptr(), is32, npts, ncol, dim, ax64.data_ptr(), cap,
-                                   n_c, kind, grid64.data_ptr(), _ptr(grid32), _ptr(raw),
-                                   claim.data_ptr(), status.data_ptr(), s), "arb_ingest_scatter")
-        if self.check:
+        ax64 = axes[: dim * cap].view(dim, cap)
+        done = False
+        if _ORDERED_INGEST and npts < 0xFFFFFFFF:
+            # rows in meshgrid order (the common case): one pass, no sort
+            check(L.arb_ingest_ordered(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
+                                       counts.data_ptr(), grid64.data_ptr(), _ptr(grid32), _ptr(raw),
+                                       work.data_ptr(), wb, status.data_ptr(), s), "arb_ingest_ordered")
+            done = L.arb_status_fetch(status.data_ptr(), s) == 0
+        n = [int(v) for v in counts.cpu()] if done else None
+        if not done:
+            check(L.arb_ingest_axes(ft.data_ptr(), is32, npts, ncol, dim, cap, axes.data_ptr(),
+                                    counts.data_ptr(), work.data_ptr(), wb, status.data_ptr(), s),
+                  "arb_ingest_axes")
             st = L.arb_status_fetch(status.data_ptr(), s)
+            n = [int(v) for v in counts.cpu()]
+            if st & _lib.ARB_ERR_CAPACITY:
+                raise ValueError(f"an axis has more than {cap} grid samples")
             if st:
-                raise ValueError("field rows are not a full regular grid (duplicate or off-axis points)")
-        del claim
+                raise ValueError("field rows are not a regular grid (NaN coordinates or duplicate points)")
+            if any(v < 4 for v in n):
+                raise ValueError("every axis needs at least 4 grid points")
+            if int(np.prod(n)) != npts:
+                raise ValueError(f"field rows do not form a full regular grid: {npts} rows, axes {n}")
+            claim = torch.empty(npts, dtype=torch.int32, device=dev)
+            n_c = (ctypes.c_int64 * 4)(*(n + [1] * (4 - dim)))
+            check(L.arb_ingest_scatter(ft.data_ptr(), is32, npts, ncol, dim, ax64.data_ptr(), cap,
+                                       n_c, kind, grid64.data_ptr(), _ptr(grid32), _ptr(raw),
+                                       claim.data_ptr(), status.data_ptr(), s), "arb_ingest_scatter")
+            if self.check:
+                st = L.arb_status_fetch(status.data_ptr(), s)
+                if st:
+                    raise ValueError("field rows are not a full regular grid (duplicate or off-axis points)")
+            del claim
+        self._axes_dev = [ax64[a, : n[a]].clone() for a in range(dim)]
+        ax = [t.cpu().numpy().astype(self._field_dtype) for t in self._axes_dev]
+        self._n = n
+        self._npts = npts
+        self.ingest_path = "ordered" if done else "general"
         self._grid64, self._grid32, self._raw = grid64, grid32, raw
         self._status = status
         # reference attributes, computed in the field's own dtype (ARB:541-568)

@@ -119,6 +119,23 @@ int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64_t npts, in
                        int32_t kind, double *grid64, float *grid32, double *raw_out,
                        uint32_t *claim, int32_t *status, arb_stream_t stream);
 
+/* Single-pass ingest for rows in meshgrid order: lexicographic over the
+ * axes in any axis order, each axis ascending or descending (what NumPy's
+ * meshgrid + reshape and the reference's own sort, ARB:530, produce).  Reads
+ * the axes off the lines through row 0 into axis_out / axis_count (as
+ * arb_ingest_axes does) and writes every grid slot from the row its
+ * position implies (as arb_ingest_scatter does), checking that row's
+ * coordinates against the slot's axis samples.  For rows in any other order
+ * (or not a full grid) it sets ARB_ERR_IRREGULAR_GRID in *status and leaves
+ * the outputs undefined: the caller then runs arb_ingest_axes +
+ * arb_ingest_scatter, which give the authoritative answer.  work holds
+ * arb_ingest_axes_work_bytes(dim) bytes.  npts < 2^32.  Replaces the same
+ * reference code as the two-step ingest (ARB:528-568, 1264-1320). */
+int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                       int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,
+                       int64_t *axis_count, double *grid64, float *grid32, double *raw_out,
+                       void *work, size_t work_bytes, int32_t *status, arb_stream_t stream);
+
 /* ---- finite-difference planes: replaces the D matrix of makeAMatrix
  *      (src/ARBInterp/ARBInterp.py:129-173, 762-876) applied per grid point.
  *      planes is [2^dim][npts][F] float64: kind r (f, fx, fy, fz, fxy, fxz,

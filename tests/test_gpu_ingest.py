@@ -1,0 +1,114 @@
+"""Single-pass ingest of rows in meshgrid order (arb_ingest_ordered) against
+the general two-step ingest (arb_ingest_axes + arb_ingest_scatter): same
+axes, same grids, same query results, for every axis order and direction;
+rows in any other order fall back to the general path."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _field(dim, order, flip, seed=0, vector=False, dtype=np.float64):
+    """Rows of a regular grid listed lexicographically with axis order
+    `order` (slowest first) and the axes in `flip` descending."""
+    rng = np.random.default_rng(seed)
+    n = [7, 6, 5, 4][:dim]
+    h = rng.uniform(0.05, 0.2, dim)
+    ax = [rng.uniform(-1, 1) + h[a] * np.arange(n[a]) for a in range(dim)]
+    ax = [a[::-1] if i in flip else a for i, a in enumerate(ax)]
+    mesh = np.meshgrid(*[ax[a] for a in order], indexing="ij")
+    cols = [None] * dim
+    for k, a in enumerate(order):
+        cols[a] = mesh[k].ravel()
+    X = np.stack(cols, 1)
+    vals = np.sin(X @ rng.uniform(0.5, 2.0, dim))[:, None] * (rng.uniform(0.5, 2.0, 3 if vector else 1))
+    return np.hstack([X, vals]).astype(dtype)
+
+
+def _both_paths(make, field, monkeypatch):
+    from arbinterp_gb300 import interp
+    a = make(field)
+    monkeypatch.setattr(interp, "_ORDERED_INGEST", False)
+    b = make(field)
+    monkeypatch.setattr(interp, "_ORDERED_INGEST", True)
+    return a, b
+
+
+def _same(a, b, q):
+    import torch
+    assert a._n == b._n
+    for x, y in zip(a._axes_dev, b._axes_dev):
+        assert torch.equal(x, y)
+    assert torch.equal(a._grid64, b._grid64)
+    if a._grid32 is not None:
+        assert torch.equal(a._grid32, b._grid32)
+    if a._raw is not None:
+        assert torch.equal(a._raw, b._raw)
+    ra, rb = a.Query(q.copy()), b.Query(q.copy())
+    ra = ra if isinstance(ra, tuple) else (ra,)
+    rb = rb if isinstance(rb, tuple) else (rb,)
+    for x, y in zip(ra, rb):
+        assert np.array_equal(x, y, equal_nan=True)
+
+
+@pytest.mark.parametrize("order,flip", [((0, 1, 2), ()), ((2, 1, 0), ()), ((1, 2, 0), (1,)),
+                                        ((0, 2, 1), (0, 2)), ((2, 1, 0), (0, 1, 2))])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_tricubic_meshgrid_orders(order, flip, prec, monkeypatch):
+    from arbinterp_gb300 import tricubic
+    f = _field(3, order, flip, vector=True)
+    q = np.random.default_rng(1).uniform(f[:, :3].min(0), f[:, :3].max(0), (500, 3))
+    for mode in ("both", "norm"):
+        a, b = _both_paths(lambda x: tricubic(x, "quiet", mode=mode, precision=prec), f, monkeypatch)
+        assert a.ingest_path == "ordered" and b.ingest_path == "general"
+        _same(a, b, q)
+        assert np.array_equal(a.inputfield, b.inputfield)
+
+
+@pytest.mark.parametrize("order,flip", [((3, 2, 1, 0), ()), ((0, 1, 2, 3), (3,)), ((1, 3, 0, 2), (0,))])
+def test_quadcubic_meshgrid_orders(order, flip, monkeypatch):
+    from arbinterp_gb300 import quadcubic
+    f = _field(4, order, flip)
+    q = np.random.default_rng(2).uniform(f[:, :4].min(0), f[:, :4].max(0), (300, 4))
+    a, b = _both_paths(lambda x: quadcubic(x, "quiet"), f, monkeypatch)
+    assert a.ingest_path == "ordered"
+    _same(a, b, q)
+
+
+def test_float32_field_ordered(monkeypatch):
+    from arbinterp_gb300 import tricubic
+    f = _field(3, (2, 1, 0), (), dtype=np.float32)
+    q = np.random.default_rng(3).uniform(f[:, :3].min(0), f[:, :3].max(0), (200, 3))
+    a, b = _both_paths(lambda x: tricubic(x, "quiet", precision="mixed"), f, monkeypatch)
+    assert a.ingest_path == "ordered"
+    _same(a, b, q)
+
+
+def test_other_orders_fall_back():
+    from arbinterp_gb300 import tricubic
+    f = _field(3, (2, 1, 0), ())
+    q = np.random.default_rng(4).uniform(f[:, :3].min(0), f[:, :3].max(0), (300, 3))
+    ref = tricubic(f, "quiet")
+    rng = np.random.default_rng(5)
+    swapped = f.copy()
+    swapped[[10, 57]] = swapped[[57, 10]]               # meshgrid order but two rows exchanged
+    shuffled = f[rng.permutation(len(f))]
+    for g in (swapped, shuffled):
+        o = tricubic(g, "quiet")
+        assert o.ingest_path == "general"
+        assert np.array_equal(o.Query(q.copy())[0], ref.Query(q.copy())[0], equal_nan=True)
+    off = f.copy()
+    off[33, 1] += 1e-3                                  # a point off its axis
+    with pytest.raises(ValueError):
+        tricubic(off, "quiet")
+    dup = f.copy()
+    dup[5] = dup[6]                                     # duplicate point, one slot empty
+    with pytest.raises(ValueError):
+        tricubic(dup, "quiet")
