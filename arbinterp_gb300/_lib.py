@@ -40,6 +40,7 @@ class ArbQueryOut(C.Structure):
     _fields_ = [
         ("comps", C.c_void_p), ("norms", C.c_void_p), ("grads", C.c_void_p),
         ("inds", C.c_void_p), ("oob_rows", C.c_void_p), ("oob_count", C.c_void_p),
+        ("comps_stride", C.c_int64), ("norms_stride", C.c_int64), ("grads_stride", C.c_int64),
     ]
 
 
@@ -55,6 +56,7 @@ SIGNATURES = {
                                      _P, _P, _P, _P, _P, _P]),
     "arb_ingest_ordered": (C.c_int, [_P, _I32, _I64, _I32, _I32, _I32, _I64, _P, _P, _P, _P, _P, _P, C.c_size_t,
                                      _P, _P]),
+    "arb_ingest_summary": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P]),
     "arb_fd_planes": (C.c_int, [C.POINTER(ArbGrid), _P, _P]),
     "arb_coef_solve": (C.c_int, [C.POINTER(ArbGrid), _I32, _I64, _I64, _P, _P, _P]),
     "arb_query_eval": (C.c_int, [C.POINTER(ArbGrid), _P, _I64, _I64, _I32, C.POINTER(ArbQueryOut), _P, _P]),

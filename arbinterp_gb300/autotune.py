@@ -65,8 +65,13 @@ def default_plan(interp, nq):
     return {"table": interp._table_complete, "binned": nq >= interp.sort_threshold, "bin_shift": 0}
 
 
+_NAMES: dict = {}
+
+
 def plan_key(interp, nq):
-    dev = torch.cuda.get_device_name(interp.device)
+    dev = _NAMES.get(interp.device)
+    if dev is None:
+        dev = _NAMES[interp.device] = torch.cuda.get_device_name(interp.device)
     b = lambda v: int(math.log2(max(v, 1)))  # noqa: E731
     return (f"{dev}|d{interp._dim}|F{interp._F}|{interp.precision}|cells2^{b(interp.nc)}|"
             f"q2^{b(nq)}|table{int(interp._table_complete)}")

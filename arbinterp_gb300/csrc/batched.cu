@@ -121,6 +121,8 @@ extern "C" int arb_batched_launch(const arb_grid *grids, int32_t nfields, const 
   if (out->oob_rows && !out->oob_count) return ARB_ERR_INVALID;
   if (ntiles == 0) return ARB_OK;
   cudaStream_t s = (cudaStream_t)stream;
+  const arb_query_out out_norm = normalize_out(*out, 3);
+  out = &out_norm;
   if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s) != cudaSuccess) return ARB_ERR_CUDA;
   const int per_sm = 8;
   int64_t grid = (int64_t)sm_count() * per_sm;

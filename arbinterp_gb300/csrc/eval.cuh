@@ -16,18 +16,59 @@ struct KParams {
   FastAxis ax[4];
 };
 
+// Output rows.  Strides are normalised on the host (normalize_out), so the
+// kernels always see the row stride of each output.
+__device__ __forceinline__ void st_v4(double *p, double a, double b, double c, double d) {
+  asm volatile("st.global.v4.b64 [%0], {%1,%2,%3,%4};" ::"l"(p), "d"(a), "d"(b), "d"(c), "d"(d) : "memory");
+}
+
+// Interleaved rows (see arb_query_out): whole 32-byte sectors per store.
+template <int DIM, int F>
+__device__ __forceinline__ bool interleaved_rows(const arb_query_out &o) {
+  if (F == 4)
+    return o.comps && o.norms == o.comps + 3 && o.grads == o.comps + 4 && o.comps_stride == 8 &&
+           o.norms_stride == 8 && o.grads_stride == 8 && !((uintptr_t)o.comps & 31);
+  if (F == 1) {
+    constexpr int R = DIM == 3 ? 4 : 8;
+    return o.norms && o.grads == o.norms + 1 && o.norms_stride == R && o.grads_stride == R &&
+           !((uintptr_t)o.norms & 31);
+  }
+  return o.comps && o.comps_stride == 4 && !((uintptr_t)o.comps & 31);
+}
+
+template <int DIM, int F>
+__device__ __forceinline__ void write_rows_v4(const arb_query_out &o, int64_t i, const double *val,
+                                              const double *grad) {
+  if (F == 4) {
+    double *r = o.comps + i * 8;
+    st_v4(r, val[0], val[1], val[2], val[3]);
+    st_v4(r + 4, grad[0], grad[1], grad[2], DIM == 4 ? grad[DIM - 1] : 0.0);
+  } else if (F == 1) {
+    double *r = o.norms + i * (DIM == 3 ? 4 : 8);
+    st_v4(r, val[0], grad[0], grad[1], grad[2]);
+    if (DIM == 4) st_v4(r + 4, grad[DIM - 1], 0.0, 0.0, 0.0);
+  } else {
+    st_v4(o.comps + i * 4, val[0], val[1], val[2], 0.0);
+  }
+}
+
 template <int DIM, int F>
 __device__ __forceinline__ void write_const(const arb_query_out &o, int64_t i, double v) {
+  if (interleaved_rows<DIM, F>(o)) {
+    const double vv[4] = {v, v, v, v}, gg[4] = {v, v, v, v};
+    write_rows_v4<DIM, F>(o, i, vv, gg);
+    return;
+  }
   if (F >= 3 && o.comps) {
-    o.comps[i * 3 + 0] = v;
-    o.comps[i * 3 + 1] = v;
-    o.comps[i * 3 + 2] = v;
+    o.comps[i * o.comps_stride + 0] = v;
+    o.comps[i * o.comps_stride + 1] = v;
+    o.comps[i * o.comps_stride + 2] = v;
   }
   if (F != 3) {
-    if (o.norms) o.norms[i] = v;
+    if (o.norms) o.norms[i * o.norms_stride] = v;
     if (o.grads) {
 #pragma unroll
-      for (int a = 0; a < DIM; ++a) o.grads[i * DIM + a] = v;
+      for (int a = 0; a < DIM; ++a) o.grads[i * o.grads_stride + a] = v;
     }
   }
 }
@@ -35,16 +76,20 @@ __device__ __forceinline__ void write_const(const arb_query_out &o, int64_t i, d
 template <int DIM, int F>
 __device__ __forceinline__ void write_vals(const arb_query_out &o, int64_t i, const double *val,
                                            const double *grad) {
+  if (interleaved_rows<DIM, F>(o)) {
+    write_rows_v4<DIM, F>(o, i, val, grad);
+    return;
+  }
   if (F >= 3 && o.comps) {
-    o.comps[i * 3 + 0] = val[0];
-    o.comps[i * 3 + 1] = val[1];
-    o.comps[i * 3 + 2] = val[2];
+    o.comps[i * o.comps_stride + 0] = val[0];
+    o.comps[i * o.comps_stride + 1] = val[1];
+    o.comps[i * o.comps_stride + 2] = val[2];
   }
   if (F != 3) {
-    if (o.norms) o.norms[i] = val[F - 1];
+    if (o.norms) o.norms[i * o.norms_stride] = val[F - 1];
     if (o.grads) {
 #pragma unroll
-      for (int a = 0; a < DIM; ++a) o.grads[i * DIM + a] = grad[a];
+      for (int a = 0; a < DIM; ++a) o.grads[i * o.grads_stride + a] = grad[a];
     }
   }
 }
@@ -603,6 +648,15 @@ static inline KParams make_kparams(const arb_grid *g) {
     fast_axis_pairs(kp.ax[a], lo, hi, h);
   }
   return kp;
+}
+
+// Output descriptor with every row stride filled in (0 means packed).
+static inline arb_query_out normalize_out(const arb_query_out &in, int dim) {
+  arb_query_out o = in;
+  if (o.comps_stride <= 0) o.comps_stride = 3;
+  if (o.norms_stride <= 0) o.norms_stride = 1;
+  if (o.grads_stride <= 0) o.grads_stride = dim;
+  return o;
 }
 
 static inline int check_query_args(const arb_grid *g, const double *q, int64_t nq, int64_t qs,

@@ -623,6 +623,28 @@ extern "C" int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64
   return launch_status();
 }
 
+__global__ void ingest_summary_kernel(const double *axes, int64_t cap, const int64_t *count, int dim,
+                                      int32_t *status, double *out) {
+  if (threadIdx.x != 0) return;
+  out[0] = (double)*status;
+  *status = 0;
+  for (int a = 0; a < 4; ++a) {
+    const int64_t n = a < dim ? count[a] : 0;
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    out[1 + a] = (double)n;
+    out[5 + 3 * a] = n >= 1 ? axes[a * cap] : nan;
+    out[6 + 3 * a] = n >= 2 ? axes[a * cap + 1] : nan;
+    out[7 + 3 * a] = n >= 2 ? axes[a * cap + n - 2] : nan;
+  }
+}
+
+extern "C" int arb_ingest_summary(const double *axes, int64_t axis_cap, const int64_t *axis_count, int32_t dim,
+                                  int32_t *status, double *out, arb_stream_t stream) {
+  if (!axes || !axis_count || !status || !out || (dim != 3 && dim != 4) || axis_cap <= 0) return ARB_ERR_INVALID;
+  ingest_summary_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(axes, axis_cap, axis_count, dim, status, out);
+  return launch_status();
+}
+
 extern "C" int arb_status_fetch(int32_t *status, arb_stream_t stream) {
   if (!status) return ARB_ERR_INVALID;
   int32_t h = 0;

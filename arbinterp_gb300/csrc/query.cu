@@ -93,6 +93,8 @@ extern "C" int arb_query_eval_otf(const arb_grid *g, int32_t precision, double *
   const bool mixed = precision == ARB_PREC_MIXED;
   if (mixed ? !g->grid32 : !g->grid64) return ARB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
+  const arb_query_out out_norm = normalize_out(*out, g->dim);
+  out = &out_norm;
   const KParams kp = make_kparams(g);
   if (g->dim == 3) {
     const int T = 256;
@@ -127,6 +129,8 @@ extern "C" int arb_query_eval(const arb_grid *g, double *q, int64_t nq, int64_t 
   if (nq == 0) return ARB_OK;
   const bool mixed = g->table_prec == ARB_PREC_MIXED;
   cudaStream_t s = (cudaStream_t)stream;
+  const arb_query_out out_norm = normalize_out(*out, g->dim);
+  out = &out_norm;
   const KParams kp = make_kparams(g);
   const int T = 256;
   const unsigned B = (unsigned)((nq + T - 1) / T);

@@ -6,31 +6,52 @@
 // sort, then evaluated bin by bin, so neighbouring threads share grid data in
 // L1/L2 and each grid point is fetched from HBM about once.
 //
-//   locate   : float64 cell index + fractional offset (exactly the
-//              reference's iu = (q - IntMin)/h, floor, flat index), the
-//              out-of-volume bookkeeping of rQuery (NaN rows, queryInds), the
-//              packed cell coordinates, and bin id + rank within the bin
-//              (atomic histogram)
+//   count    : cell index + fractional offset (exactly the reference's
+//              iu = (q - IntMin)/h, floor, flat index), the out-of-volume
+//              bookkeeping of rQuery (NaN rows, queryInds) and the bin
+//              histogram (fire-and-forget atomics)
 //   scan     : exclusive prefix sum of the bin histogram
-//   scatter  : records (packed cell, row, frac) into bin order
+//   place    : the same coordinate step again, a slot in the query's bin
+//              (atomic on the running offset) and one 32-byte record
+//              (packed cell, row, fraction) written there; afterwards
+//              hist[b] is the end of bin b
 //   evaluate : on-the-fly or table evaluation in bin order, outputs written
 //              to the query's original row
-// The float64 index step runs once per query; the evaluation pass does no
-// float64 arithmetic and no integer division in mixed precision.
+// Recomputing the coordinate step (float32 pipe in mixed precision) is
+// cheaper than storing it: the unsorted intermediates and a separate scatter
+// pass cost three partial-sector writes per query, the record one full one.
+// The evaluation pass does no float64 arithmetic and no integer division in
+// mixed precision.
 #include <mutex>
 
 #include "eval.cuh"
 
 namespace arb {
 
+// Bin-ordered query record: packed cell (or CELL_SPECIAL | code), the
+// query's row and its fractional offsets (float32 in mixed precision: 32
+// bytes, one sector; float64: 48 bytes).
+template <typename T>
+struct QRec;
+template <>
+struct __align__(32) QRec<float> {
+  unsigned long long cell;
+  uint32_t row;
+  float f[4];
+  uint32_t pad;
+};
+template <>
+struct __align__(16) QRec<double> {
+  unsigned long long cell;
+  uint32_t row;
+  uint32_t pad;
+  double f[4];
+};
+static_assert(sizeof(QRec<float>) == 32 && sizeof(QRec<double>) == 48, "record sizes");
+
 struct SortedWork {
-  uint32_t *hist;              // nbins + 1 (exclusive offsets after the scan)
-  uint2 *binrank;              // nq
-  unsigned long long *cell;    // nq: packed cell (or CELL_SPECIAL | code)
-  void *frac;                  // nq * DIM values of T
-  unsigned long long *s_cell;  // nq, bin order
-  uint32_t *s_row;             // nq
-  void *s_frac;                // nq * DIM
+  uint32_t *hist;  // nbins + 1: counts, exclusive offsets after the scan, bin ends after placement
+  void *rec;       // nq records (QRec<float> or QRec<double>), bin order
 };
 
 struct BinGeom {
@@ -69,25 +90,18 @@ static size_t carve(SortedWork *w, void *base, const arb_grid *g, int precision,
   };
   SortedWork t;
   t.hist = (uint32_t *)take(sizeof(uint32_t) * (bg.nbins + 1));
-  t.binrank = (uint2 *)take(sizeof(uint2) * nq);
-  t.cell = (unsigned long long *)take(sizeof(unsigned long long) * nq);
-  t.frac = take(tsz * g->dim * nq);
-  t.s_cell = (unsigned long long *)take(sizeof(unsigned long long) * nq);
-  t.s_row = (uint32_t *)take(sizeof(uint32_t) * nq);
-  t.s_frac = take(tsz * g->dim * nq);
+  t.rec = take((tsz == 4 ? sizeof(QRec<float>) : sizeof(QRec<double>)) * nq);
   if (w) *w = t;
   return off;
 }
 
+// Coordinate step of query row i: cell index, fraction, packed cell word
+// and bin (the special bin nbins for rows that need no evaluation).
 template <int DIM, bool EXACT, typename T>
-__global__ void __launch_bounds__(256) locate_kernel(arb_grid g, KParams kp, BinGeom bg, double *q,
-                                                     int64_t nq, int64_t qs, int wb, arb_query_out o,
-                                                     int32_t *status, SortedWork w) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nq) return;
-  double *qr = q + i * qs;
+__device__ __forceinline__ CoordStep bin_step(const arb_grid &g, const KParams &kp, const BinGeom &bg,
+                                              const double *qr, T frac[DIM], unsigned long long &cw, int64_t &bin,
+                                              bool &bad_index) {
   double qv[DIM];
-  T frac[DIM];
 #pragma unroll
   for (int a = 0; a < DIM; ++a) qv[a] = qr[a];
   CoordStep s;
@@ -95,16 +109,12 @@ __global__ void __launch_bounds__(256) locate_kernel(arb_grid g, KParams kp, Bin
     s = coord_step<DIM, true>(qv, g, kp.inv_h, frac);
   else
     s = coord_step_fast<DIM>(qv, kp.ax, g, frac);
-  append_oob(o, i, s.oob);
-  if (s.oob && wb)
-    for (int64_t c = 0; c < qs; ++c) qr[c] = qnan();
-  if (o.inds) o.inds[i] = s.idx;
-  unsigned long long cw;
-  int64_t bin = bg.nbins;
+  bin = bg.nbins;
+  bad_index = false;
   if (s.oob || s.nan) {
     cw = CELL_SPECIAL;
   } else if (s.idx > g.nc) {
-    set_status(status, ARB_ERR_CELL_INDEX);
+    bad_index = true;
     cw = CELL_SPECIAL;
   } else if (s.idx == g.nc) {
     cw = CELL_SPECIAL | 1ULL;
@@ -116,12 +126,57 @@ __global__ void __launch_bounds__(256) locate_kernel(arb_grid g, KParams kp, Bin
 #pragma unroll
     for (int a = DIM - 2; a >= 0; --a) bin = bin * bg.nb[a] + (c[a] >> bg.shift);
   }
-  const uint32_t rank = atomicAdd(&w.hist[bin], 1u);
-  w.binrank[i] = make_uint2((uint32_t)bin, rank);
-  w.cell[i] = cw;
-  T *fr = reinterpret_cast<T *>(w.frac) + i * DIM;
+  return s;
+}
+
+template <int DIM, bool EXACT, typename T>
+__global__ void __launch_bounds__(256) bin_count_kernel(arb_grid g, KParams kp, BinGeom bg, double *q, int64_t nq,
+                                                        int64_t qs, int wb, arb_query_out o, int32_t *status,
+                                                        SortedWork w) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  double *qr = q + i * qs;
+  T frac[DIM];
+  unsigned long long cw;
+  int64_t bin;
+  bool bad;
+  const CoordStep s = bin_step<DIM, EXACT, T>(g, kp, bg, qr, frac, cw, bin, bad);
+  append_oob(o, i, s.oob);
+  if (o.inds) o.inds[i] = s.idx;
+  if (bad) set_status(status, ARB_ERR_CELL_INDEX);
+  atomicAdd(&w.hist[bin], 1u);
+  // the caller's out-of-volume rows become NaN (the place pass reads them
+  // back as NaN rows: the same special bin)
+  if (s.oob && wb)
+    for (int64_t c = 0; c < qs; ++c) qr[c] = qnan();
+}
+
+template <int DIM, bool EXACT, typename T>
+__global__ void __launch_bounds__(256) bin_place_kernel(arb_grid g, KParams kp, BinGeom bg, const double *q,
+                                                        int64_t nq, int64_t qs, SortedWork w) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  T frac[DIM];
+  unsigned long long cw;
+  int64_t bin;
+  bool bad;
+  (void)bin_step<DIM, EXACT, T>(g, kp, bg, q + i * qs, frac, cw, bin, bad);
+  const uint32_t pos = atomicAdd(&w.hist[bin], 1u);
+  QRec<T> r;
+  r.cell = cw;
+  r.row = (uint32_t)i;
 #pragma unroll
-  for (int a = 0; a < DIM; ++a) fr[a] = frac[a];
+  for (int a = 0; a < 4; ++a) r.f[a] = a < DIM ? frac[a] : T(0);
+  r.pad = 0;
+  if constexpr (sizeof(T) == 4) {
+    // one 32-byte store: a whole sector, no partial-sector merge in L2
+    const uint32_t *u = reinterpret_cast<const uint32_t *>(&r);
+    asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(reinterpret_cast<QRec<T> *>(w.rec) + pos),
+                 "r"(u[0]), "r"(u[1]), "r"(u[2]), "r"(u[3]), "r"(u[4]), "r"(u[5]), "r"(u[6]), "r"(u[7])
+                 : "memory");
+  } else {
+    reinterpret_cast<QRec<T> *>(w.rec)[pos] = r;
+  }
 }
 
 // Exclusive scan of n counters in one block (n up to a few million).
@@ -147,20 +202,6 @@ __global__ void __launch_bounds__(1024) scan_kernel(uint32_t *hist, int64_t n) {
   }
 }
 
-template <int DIM, typename T>
-__global__ void __launch_bounds__(256) scatter_kernel(int64_t nq, SortedWork w) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nq) return;
-  const uint2 br = w.binrank[i];
-  const int64_t pos = (int64_t)w.hist[br.x] + br.y;
-  w.s_cell[pos] = w.cell[i];
-  w.s_row[pos] = (uint32_t)i;
-  const T *src = reinterpret_cast<const T *>(w.frac) + i * DIM;
-  T *dst = reinterpret_cast<T *>(w.s_frac) + pos * DIM;
-#pragma unroll
-  for (int a = 0; a < DIM; ++a) dst[a] = src[a];
-}
-
 template <int DIM, int F, bool MIXED, bool TABLE>
 __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_grid g, KParams kp,
                                                                            int64_t nq, arb_query_out o,
@@ -168,8 +209,9 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
   using T = typename std::conditional<MIXED, float, double>::type;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nq) return;
-  const unsigned long long cw = w.s_cell[t];
-  const int64_t i = w.s_row[t];
+  const QRec<T> r = reinterpret_cast<const QRec<T> *>(w.rec)[t];
+  const unsigned long long cw = r.cell;
+  const int64_t i = r.row;
   if (cw & CELL_SPECIAL) {
     write_const<DIM, F>(o, i, (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
     return;
@@ -177,9 +219,8 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
   int64_t c[DIM];
   unpack_cell<DIM>(cw, c);
   T fr[DIM];
-  const T *src = reinterpret_cast<const T *>(w.s_frac) + t * DIM;
 #pragma unroll
-  for (int a = 0; a < DIM; ++a) fr[a] = src[a];
+  for (int a = 0; a < DIM; ++a) fr[a] = r.f[a];
   double val[F], grad[DIM];
 #pragma unroll
   for (int a = 0; a < DIM; ++a) grad[a] = 0.0;
@@ -216,16 +257,16 @@ __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KPar
   const float *glo = g.grid32 + npts * 4;
   const unsigned mask = 0xfu << (lane & 28);
   for (int64_t t = t0 + (threadIdx.x >> 2); t < t1; t += blockDim.x >> 2) {  // groups stay converged
-    const unsigned long long cw = w.s_cell[t];
-    const int64_t i = w.s_row[t];
+    const QRec<float> r = reinterpret_cast<const QRec<float> *>(w.rec)[t];
+    const unsigned long long cw = r.cell;
+    const int64_t i = r.row;
     if (cw & CELL_SPECIAL) {
       if (p == 0) write_const<3, 4>(o, i, (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
       continue;
     }
     int64_t c[3];
     unpack_cell<3>(cw, c);
-    const float *fr = reinterpret_cast<const float *>(w.s_frac) + t * 3;
-    const float fx = fr[0], fy = fr[1], fz = fr[2];
+    const float fx = r.f[0], fy = r.f[1], fz = r.f[2];
     float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
     cr_weights<float>(fx, wx);
     cr_dweights<float>(fx, dx);
@@ -268,19 +309,26 @@ __global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KPar
       Gy += __shfl_xor_sync(mask, Gy, off);
       Gz += __shfl_xor_sync(mask, Gz, off);
     }
-    if (p == 0) {
+    const double nv = f2d_exact(ref.w + (rlo + Vn));
+    if (interleaved_rows<3, 4>(o)) {
+      if (p == 0)
+        st_v4(o.comps + i * 8, f2d_exact(ref.x + Vx), f2d_exact(ref.y + Vy), f2d_exact(ref.z + Vz), nv);
+      else if (p == 2)
+        st_v4(o.comps + i * 8 + 4, f2d_exact(Gx * kp.inv_hf[0]), f2d_exact(Gy * kp.inv_hf[1]),
+              f2d_exact(Gz * kp.inv_hf[2]), 0.0);
+    } else if (p == 0) {
       if (o.comps) {
-        o.comps[i * 3 + 0] = f2d_exact(ref.x + Vx);
-        o.comps[i * 3 + 1] = f2d_exact(ref.y + Vy);
-        o.comps[i * 3 + 2] = f2d_exact(ref.z + Vz);
+        o.comps[i * o.comps_stride + 0] = f2d_exact(ref.x + Vx);
+        o.comps[i * o.comps_stride + 1] = f2d_exact(ref.y + Vy);
+        o.comps[i * o.comps_stride + 2] = f2d_exact(ref.z + Vz);
       }
     } else if (p == 1) {
-      if (o.norms) o.norms[i] = f2d_exact(ref.w + (rlo + Vn));
+      if (o.norms) o.norms[i * o.norms_stride] = nv;
     } else if (p == 2) {
       if (o.grads) {
-        o.grads[i * 3 + 0] = f2d_exact(Gx * kp.inv_hf[0]);
-        o.grads[i * 3 + 1] = f2d_exact(Gy * kp.inv_hf[1]);
-        o.grads[i * 3 + 2] = f2d_exact(Gz * kp.inv_hf[2]);
+        o.grads[i * o.grads_stride + 0] = f2d_exact(Gx * kp.inv_hf[0]);
+        o.grads[i * o.grads_stride + 1] = f2d_exact(Gy * kp.inv_hf[1]);
+        o.grads[i * o.grads_stride + 2] = f2d_exact(Gz * kp.inv_hf[2]);
       }
     }
   }
@@ -359,6 +407,35 @@ __device__ __forceinline__ void load_bin_tile(const arb_grid &g, const BinGeom &
   }
 }
 
+// Packed float32 FMA on (x, y) pairs: d = a * b + c per component.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+
+// In-place rewrite of a 'both' tile's |B| word: hi_n := (hi_n - hi_c) +
+// (lo_n - lo_c) with c the tile's centre point (clamped into the grid), so
+// one float per point carries |B| relative to a bin-local reference with
+// float32 resolution of the bin's own variation; every block delta is then
+// one subtraction of two such words.
+__device__ __forceinline__ void rebase_tile_norm(BinTile<4> &t, const int64_t o[3], const arb_grid &g, float &ch,
+                                                 float &cl) {
+  int lc[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) lc[a] = (int)min((int64_t)(TILE_EDGE / 2), g.n[a] - 1 - o[a]);
+  const int ec = (lc[2] * TILE_EDGE + lc[1]) * TILE_EDGE + lc[0];
+  ch = t.hi[ec].w;  // the centre's (hi, lo), kept in registers for the norm values
+  cl = t.lo[ec];
+  __syncthreads();  // everyone has the centre before it is rewritten
+  for (int e = threadIdx.x; e < TILE_PTS; e += blockDim.x) t.hi[e].w = (t.hi[e].w - ch) + (t.lo[e] - cl);
+  __syncthreads();
+}
+
 template <int F>
 __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
                                                        arb_query_out o, SortedWork w) {
@@ -370,15 +447,16 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
   const int64_t nbins = bg.nbins;
   int stage = 0;
   int64_t b = blockIdx.x;
-  // bins with no query need no copy
-  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb + 1] - (int64_t)w.hist[bb] : 0; };
+  // after placement hist[b] is the end of bin b; bins with no query need no copy
+  auto bin_begin = [&](int64_t bb) { return bb > 0 ? (int64_t)w.hist[bb - 1] : (int64_t)0; };
+  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb] - bin_begin(bb) : 0; };
   if (count(b) > 0) load_bin_tile<F>(g, bg, b, tiles[0]);
   cp_async_commit();
   for (; b < nbins; b += gridDim.x) {
     const int64_t bn = b + gridDim.x;
     if (count(bn) > 0) load_bin_tile<F>(g, bg, bn, tiles[stage ^ 1]);
     cp_async_commit();
-    const int64_t t0 = w.hist[b], t1 = w.hist[b + 1];
+    const int64_t t0 = bin_begin(b), t1 = w.hist[b];
     cp_async_wait1();
     __syncthreads();
     if (t1 > t0) {
@@ -386,15 +464,16 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
       int64_t og[3];
       bin_origin(b, bg, og);
       if (F == 4) {
+        float nch, ncl;
+        rebase_tile_norm(reinterpret_cast<BinTile<4> &>(tiles[stage]), og, g, nch, ncl);
         // 4 lanes per query, lane p owning x offset p of every block row
         for (int64_t t = t0 + (threadIdx.x >> 2); t < t1; t += blockDim.x >> 2) {
-          const unsigned long long cw = w.s_cell[t];
-          const int64_t i = w.s_row[t];
+          const QRec<float> r = reinterpret_cast<const QRec<float> *>(w.rec)[t];
+          const int64_t i = r.row;
           int64_t c[3];
-          unpack_cell<3>(cw, c);
+          unpack_cell<3>(r.cell, c);
           const int lp = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));
-          const float *fr = reinterpret_cast<const float *>(w.s_frac) + t * 3;
-          const float fx = fr[0], fy = fr[1], fz = fr[2];
+          const float fx = r.f[0], fy = r.f[1], fz = r.f[2];
           float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
           cr_weights<float>(fx, wx);
           cr_dweights<float>(fx, dx);
@@ -403,35 +482,34 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
           cr_weights<float>(fz, wz);
           cr_dweights<float>(fz, dz);
           const int lref = lp + TILE_EDGE * TILE_EDGE + TILE_EDGE + 1;
-          const float nref = reinterpret_cast<const BinTile<4> &>(T).hi[lref].w;
-          const float rlo = reinterpret_cast<const BinTile<4> &>(T).lo[lref];
+          const float nref = reinterpret_cast<const BinTile<4> &>(T).hi[lref].w;  // rebased |B| at the corner
           // Components (values only) accumulate raw float32 values; |B|
           // accumulates deltas to the corner so its derivatives keep full
           // relative precision.  y first, then z: d/dz reuses the layer sums.
-          float Sx = 0.f, Sy_ = 0.f, Sz_ = 0.f, Sn = 0.f, Gy = 0.f, Gz = 0.f;
+          float2 Sxy = make_float2(0.f, 0.f), Szn = make_float2(0.f, 0.f);
+          float Gy = 0.f, Gz = 0.f;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            float ax = 0.f, ay = 0.f, az = 0.f, an = 0.f, gy = 0.f;
+            float2 axy = make_float2(0.f, 0.f), azn = make_float2(0.f, 0.f);
+            float gy = 0.f;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
               const int e = lp + (k * TILE_EDGE + j) * TILE_EDGE + p;
               const float4 v = reinterpret_cast<const BinTile<4> &>(T).hi[e];
-              const float lo = reinterpret_cast<const BinTile<4> &>(T).lo[e];
-              const float dn = (v.w - nref) + (lo - rlo);
-              ax += wy[j] * v.x;
-              ay += wy[j] * v.y;
-              az += wy[j] * v.z;
-              an += wy[j] * dn;
+              const float dn = v.w - nref;
+              const float2 wj = make_float2(wy[j], wy[j]);
+              axy = ffma2(wj, make_float2(v.x, v.y), axy);
+              azn = ffma2(wj, make_float2(v.z, dn), azn);
               gy += dy[j] * dn;
             }
-            Sx += wz[k] * ax;
-            Sy_ += wz[k] * ay;
-            Sz_ += wz[k] * az;
-            Sn += wz[k] * an;
+            const float2 wk = make_float2(wz[k], wz[k]);
+            Sxy = ffma2(wk, axy, Sxy);
+            Szn = ffma2(wk, azn, Szn);
             Gy += wz[k] * gy;
-            Gz += dz[k] * an;
+            Gz += dz[k] * azn.y;
           }
-          float Vx = wx[p] * Sx, Vy = wx[p] * Sy_, Vz = wx[p] * Sz_, Vn = wx[p] * Sn;
+          const float Sn = Szn.y;
+          float Vx = wx[p] * Sxy.x, Vy = wx[p] * Sxy.y, Vz = wx[p] * Szn.x, Vn = wx[p] * Sn;
           float Gx = dx[p] * Sn;
           Gy *= wx[p];
           Gz *= wx[p];
@@ -445,19 +523,27 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
             Gy += __shfl_xor_sync(mask, Gy, off);
             Gz += __shfl_xor_sync(mask, Gz, off);
           }
-          if (p == 0) {
+          // |B| = centre (hi + lo) + rebased corner + interpolated delta
+          const double nv = f2d_exact(nch) + f2d_exact(ncl + (nref + Vn));
+          if (interleaved_rows<3, 4>(o)) {
+            if (p == 0)
+              st_v4(o.comps + i * 8, f2d_exact(Vx), f2d_exact(Vy), f2d_exact(Vz), nv);
+            else if (p == 2)
+              st_v4(o.comps + i * 8 + 4, f2d_exact(Gx * kp.inv_hf[0]), f2d_exact(Gy * kp.inv_hf[1]),
+                    f2d_exact(Gz * kp.inv_hf[2]), 0.0);
+          } else if (p == 0) {
             if (o.comps) {
-              o.comps[i * 3 + 0] = f2d_exact(Vx);
-              o.comps[i * 3 + 1] = f2d_exact(Vy);
-              o.comps[i * 3 + 2] = f2d_exact(Vz);
+              o.comps[i * o.comps_stride + 0] = f2d_exact(Vx);
+              o.comps[i * o.comps_stride + 1] = f2d_exact(Vy);
+              o.comps[i * o.comps_stride + 2] = f2d_exact(Vz);
             }
           } else if (p == 1) {
-            if (o.norms) o.norms[i] = f2d_exact(nref + (rlo + Vn));
+            if (o.norms) o.norms[i * o.norms_stride] = nv;
           } else if (p == 2) {
             if (o.grads) {
-              o.grads[i * 3 + 0] = f2d_exact(Gx * kp.inv_hf[0]);
-              o.grads[i * 3 + 1] = f2d_exact(Gy * kp.inv_hf[1]);
-              o.grads[i * 3 + 2] = f2d_exact(Gz * kp.inv_hf[2]);
+              o.grads[i * o.grads_stride + 0] = f2d_exact(Gx * kp.inv_hf[0]);
+              o.grads[i * o.grads_stride + 1] = f2d_exact(Gy * kp.inv_hf[1]);
+              o.grads[i * o.grads_stride + 2] = f2d_exact(Gz * kp.inv_hf[2]);
             }
           }
         }
@@ -467,10 +553,10 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
     stage ^= 1;
   }
   // records that need no evaluation (out of volume, NaN, sentinel column)
-  for (int64_t t = (int64_t)w.hist[nbins] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
+  for (int64_t t = bin_begin(nbins) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned long long cw = w.s_cell[t];
-    write_const<3, F>(o, w.s_row[t], (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
+    const QRec<float> r = reinterpret_cast<const QRec<float> *>(w.rec)[t];
+    write_const<3, F>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
   }
 }
 
@@ -512,9 +598,9 @@ static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, 
   using T = typename std::conditional<MIXED, float, double>::type;
   const int TB = 256;
   const unsigned B = (unsigned)((nq + TB - 1) / TB);
-  locate_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, wb, *out, status, w);
+  bin_count_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, wb, *out, status, w);
   scan_kernel<<<1, 1024, 0, s>>>(w.hist, bg.nbins + 1);
-  scatter_kernel<DIM, T><<<B, TB, 0, s>>>(nq, w);
+  bin_place_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, w);
 }
 
 template <int DIM, bool MIXED>
@@ -597,6 +683,8 @@ extern "C" int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32
   if (carve(&w, work, g, precision, nq) > work_bytes) return ARB_ERR_INVALID;
   const BinGeom bg = bin_geom(g);
   cudaStream_t s = (cudaStream_t)stream;
+  const arb_query_out out_norm = normalize_out(*out, g->dim);
+  out = &out_norm;
   if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nbins + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
   const KParams kp = make_kparams(g);
   if (g->dim == 3) {
@@ -637,6 +725,8 @@ extern "C" int arb_query_bin(const arb_grid *g, int32_t precision, double *q, in
   if (carve(&w, work, g, precision, nq) > work_bytes) return ARB_ERR_INVALID;
   const BinGeom bg = bin_geom(g);
   cudaStream_t s = (cudaStream_t)stream;
+  const arb_query_out out_norm = normalize_out(*out, g->dim);
+  out = &out_norm;
   if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nbins + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
   const KParams kp = make_kparams(g);
   const bool mixed = precision == ARB_PREC_MIXED;
@@ -667,6 +757,8 @@ extern "C" int arb_query_eval_binned(const arb_grid *g, int32_t precision, int32
   SortedWork w;
   if (carve(&w, work, g, precision, nq) > work_bytes) return ARB_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
+  const arb_query_out out_norm = normalize_out(*out, g->dim);
+  out = &out_norm;
   const KParams kp = make_kparams(g);
   if (g->dim == 3) {
     if (mixed) launch_eval<3, true>(g, kp, nq, out, w, use_table, s);

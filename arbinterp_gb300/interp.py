@@ -152,14 +152,22 @@ class _Interpolant:
                   if self.precision == "mixed" else None)
         raw = torch.empty(npts * 3, dtype=torch.float64, device=dev) if kind == _lib.KIND_NORM else None
         ax64 = axes[: dim * cap].view(dim, cap)
+        summ = torch.empty(17, dtype=torch.float64, device=dev)
+
+        def summary():
+            # status, axis counts and the axis samples the attributes need, in one copy
+            check(L.arb_ingest_summary(axes.data_ptr(), cap, counts.data_ptr(), dim, status.data_ptr(),
+                                       summ.data_ptr(), s), "arb_ingest_summary")
+            return summ.cpu().numpy()
+
         done = False
         if _ORDERED_INGEST and npts < 0xFFFFFFFF:
             # rows in meshgrid order (the common case): one pass, no sort
             check(L.arb_ingest_ordered(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
                                        counts.data_ptr(), grid64.data_ptr(), _ptr(grid32), _ptr(raw),
                                        work.data_ptr(), wb, status.data_ptr(), s), "arb_ingest_ordered")
-            done = L.arb_status_fetch(status.data_ptr(), s) == 0
-        n = [int(v) for v in counts.cpu()] if done else None
+            sm = summary()
+            done = int(sm[0]) == 0
         if not done:
             check(L.arb_ingest_axes(ft.data_ptr(), is32, npts, ncol, dim, cap, axes.data_ptr(),
                                     counts.data_ptr(), work.data_ptr(), wb, status.data_ptr(), s),
@@ -179,22 +187,22 @@ class _Interpolant:
             check(L.arb_ingest_scatter(ft.data_ptr(), is32, npts, ncol, dim, ax64.data_ptr(), cap,
                                        n_c, kind, grid64.data_ptr(), _ptr(grid32), _ptr(raw),
                                        claim.data_ptr(), status.data_ptr(), s), "arb_ingest_scatter")
-            if self.check:
-                st = L.arb_status_fetch(status.data_ptr(), s)
-                if st:
-                    raise ValueError("field rows are not a full regular grid (duplicate or off-axis points)")
+            sm = summary()
+            if self.check and int(sm[0]):
+                raise ValueError("field rows are not a full regular grid (duplicate or off-axis points)")
             del claim
-        self._axes_dev = [ax64[a, : n[a]].clone() for a in range(dim)]
-        ax = [t.cpu().numpy().astype(self._field_dtype) for t in self._axes_dev]
+        n = [int(sm[1 + a]) for a in range(dim)]
+        self._axes_dev = [ax64[a, : n[a]] for a in range(dim)]
         self._n = n
         self._npts = npts
         self.ingest_path = "ordered" if done else "general"
         self._grid64, self._grid32, self._raw = grid64, grid32, raw
         self._status = status
         # reference attributes, computed in the field's own dtype (ARB:541-568)
-        h = [np.abs(ax[a][0] - ax[a][1]) for a in range(dim)]
-        lo = [ax[a][1] for a in range(dim)]
-        hi = [ax[a][n[a] - 2] for a in range(dim)]
+        dt = self._field_dtype
+        h = [np.abs(dt(sm[5 + 3 * a]) - dt(sm[6 + 3 * a])) for a in range(dim)]
+        lo = [dt(sm[6 + 3 * a]) for a in range(dim)]
+        hi = [dt(sm[7 + 3 * a]) for a in range(dim)]
         self._h, self._lo, self._hi = h, lo, hi
         names = "xyzt"
         for a in range(dim):
@@ -280,13 +288,25 @@ class _Interpolant:
         self._solved = None
         self._g.table = None
 
+    def _row_layout(self):
+        """Interleaved output rows: (doubles per row, comps col, norm col, grads col);
+        both mode (cx cy cz |B| gx gy gz [gt]), scalar/norm (v gx gy gz [gt ...]),
+        vector (cx cy cz -).  One row is one or two 32-byte sectors."""
+        dim, kind = self._dim, self._kind
+        if kind == _lib.KIND_BOTH:
+            return 8, 0, 3, 4
+        if kind == _lib.KIND_VECTOR:
+            return 4, 0, None, None
+        return (4 if dim == 3 else 8), None, 0, 1
+
     def _outputs(self, n, want_oob):
         dev = self.device
-        dim, kind = self._dim, self._kind
-        f64 = dict(dtype=torch.float64, device=dev)
-        comps = torch.empty((n, 3), **f64) if kind in (_lib.KIND_VECTOR, _lib.KIND_BOTH) else None
-        norms = torch.empty((n, 1), **f64) if kind != _lib.KIND_VECTOR else None
-        grads = torch.empty((n, dim), **f64) if kind != _lib.KIND_VECTOR else None
+        dim = self._dim
+        R, ci, ni, gi = self._row_layout()
+        rows = torch.empty((n, R), dtype=torch.float64, device=dev)
+        comps = rows[:, ci:ci + 3] if ci is not None else None
+        norms = rows[:, ni:ni + 1] if ni is not None else None
+        grads = rows[:, gi:gi + dim] if gi is not None else None
         inds = torch.empty(n, dtype=torch.int64, device=dev)
         oob = torch.empty(n, dtype=torch.int64, device=dev) if want_oob else None
         cnt = torch.zeros(1, dtype=torch.int64, device=dev) if want_oob else None
@@ -297,7 +317,8 @@ class _Interpolant:
         L = lib()
         res = self._outputs(n, want_oob)
         comps, norms, grads, inds, oob, cnt = res
-        out = ArbQueryOut(_ptr(comps), _ptr(norms), _ptr(grads), _ptr(inds), _ptr(oob), _ptr(cnt))
+        R = self._row_layout()[0]
+        out = ArbQueryOut(_ptr(comps), _ptr(norms), _ptr(grads), _ptr(inds), _ptr(oob), _ptr(cnt), R, R, R)
         s = _stream()
         table = bool(plan["table"])
         prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_MIXED
@@ -362,14 +383,12 @@ class _Interpolant:
         qc = np.ascontiguousarray(qa, dtype=np.float64)
         qd = torch.from_numpy(qc).to(self.device, non_blocking=True)
         comps, norms, grads, inds, oob, cnt = self._run(qd, n, qs, False, True)
-        host = []
-        for t in (comps, norms, grads):
-            if t is None:
-                host.append(None)
-                continue
-            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-            h.copy_(t, non_blocking=True)
-            host.append(h)
+        # one copy of the interleaved rows; the outputs are column views of it
+        rows = (comps if comps is not None else norms)._base
+        hrows = torch.empty(rows.shape, dtype=rows.dtype, pin_memory=True)
+        hrows.copy_(rows, non_blocking=True)
+        R, ci, ni, gi = self._row_layout()
+        host = [None if c is None else hrows[:, c:c + w] for c, w in ((ci, 3), (ni, 1), (gi, dim))]
         st = self._fetch_status()          # synchronises the stream
         nbad = int(cnt.item())
         if nbad:

@@ -79,8 +79,14 @@ typedef struct arb_grid {
   int32_t bin_shift;    /* log2 cells per bin edge for grouped queries; 0 = default (3D: 3, 4D: 2) */
 } arb_grid;
 
-/* Query outputs.  Any pointer may be NULL when not wanted.  Row-major like
- * the reference's return arrays. */
+/* Query outputs.  Any pointer may be NULL when not wanted.  Rows are
+ * row-major like the reference's return arrays; each of comps, norms and
+ * grads has its own row stride in doubles (0 = packed: 3, 1 and dim).
+ * Interleaved rows: when comps, norms and grads share rows of R doubles —
+ * both mode: norms = comps + 3, grads = comps + 4, R = 8; scalar / norm
+ * mode: grads = norms + 1, R = 4 (3D) or 8 (4D); vector mode: R = 4 — and
+ * the first output is 32-byte aligned, the kernels store whole 32-byte
+ * sectors and may write 0 into the row's unused trailing doubles. */
 typedef struct arb_query_out {
   double *comps;     /* [nq][3]   vector and both modes                     */
   double *norms;     /* [nq]      scalar, norm and both modes               */
@@ -88,6 +94,7 @@ typedef struct arb_query_out {
   int64_t *inds;     /* [nq]      cell index per row (queryInds)            */
   int64_t *oob_rows; /* [nq]      rows found outside the volume, any order  */
   unsigned long long *oob_count; /* device counter for oob_rows (zeroed by caller) */
+  int64_t comps_stride, norms_stride, grads_stride; /* row strides in doubles, 0 = packed */
 } arb_query_out;
 
 /* ---- ingest: replaces getFieldParams (src/ARBInterp/ARBInterp.py:528-568,
@@ -135,6 +142,14 @@ int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64_t npts, in
                        int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,
                        int64_t *axis_count, double *grid64, float *grid32, double *raw_out,
                        void *work, size_t work_bytes, int32_t *status, arb_stream_t stream);
+
+/* Everything the host needs after an ingest, for one device-to-host copy:
+ * out[0] = *status (then cleared), out[1 + a] = axis_count[a], and per axis
+ * a the samples 0, 1 and n_a - 2 at out[5 + 3a .. 7 + 3a] (the reference's
+ * h, IntMin and IntMax come from them, ARB:541-568); 17 doubles.  No
+ * counterpart in the reference (host-side arrays there). */
+int arb_ingest_summary(const double *axes, int64_t axis_cap, const int64_t *axis_count, int32_t dim,
+                       int32_t *status, double *out, arb_stream_t stream);
 
 /* ---- finite-difference planes: replaces the D matrix of makeAMatrix
  *      (src/ARBInterp/ARBInterp.py:129-173, 762-876) applied per grid point.
