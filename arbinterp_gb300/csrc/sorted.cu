@@ -418,24 +418,6 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
   return d;
 }
 
-// In-place rewrite of a 'both' tile's |B| word: hi_n := (hi_n - hi_c) +
-// (lo_n - lo_c) with c the tile's centre point (clamped into the grid), so
-// one float per point carries |B| relative to a bin-local reference with
-// float32 resolution of the bin's own variation; every block delta is then
-// one subtraction of two such words.
-__device__ __forceinline__ void rebase_tile_norm(BinTile<4> &t, const int64_t o[3], const arb_grid &g, float &ch,
-                                                 float &cl) {
-  int lc[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) lc[a] = (int)min((int64_t)(TILE_EDGE / 2), g.n[a] - 1 - o[a]);
-  const int ec = (lc[2] * TILE_EDGE + lc[1]) * TILE_EDGE + lc[0];
-  ch = t.hi[ec].w;  // the centre's (hi, lo), kept in registers for the norm values
-  cl = t.lo[ec];
-  __syncthreads();  // everyone has the centre before it is rewritten
-  for (int e = threadIdx.x; e < TILE_PTS; e += blockDim.x) t.hi[e].w = (t.hi[e].w - ch) + (t.lo[e] - cl);
-  __syncthreads();
-}
-
 template <int F>
 __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
                                                        arb_query_out o, SortedWork w) {
@@ -464,8 +446,6 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
       int64_t og[3];
       bin_origin(b, bg, og);
       if (F == 4) {
-        float nch, ncl;
-        rebase_tile_norm(reinterpret_cast<BinTile<4> &>(tiles[stage]), og, g, nch, ncl);
         // 4 lanes per query, lane p owning x offset p of every block row
         for (int64_t t = t0 + (threadIdx.x >> 2); t < t1; t += blockDim.x >> 2) {
           const QRec<float> r = reinterpret_cast<const QRec<float> *>(w.rec)[t];
@@ -482,7 +462,8 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
           cr_weights<float>(fz, wz);
           cr_dweights<float>(fz, dz);
           const int lref = lp + TILE_EDGE * TILE_EDGE + TILE_EDGE + 1;
-          const float nref = reinterpret_cast<const BinTile<4> &>(T).hi[lref].w;  // rebased |B| at the corner
+          const float nref = reinterpret_cast<const BinTile<4> &>(T).hi[lref].w;
+          const float rlo = reinterpret_cast<const BinTile<4> &>(T).lo[lref];
           // Components (values only) accumulate raw float32 values; |B|
           // accumulates deltas to the corner so its derivatives keep full
           // relative precision.  y first, then z: d/dz reuses the layer sums.
@@ -496,7 +477,7 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
             for (int j = 0; j < 4; ++j) {
               const int e = lp + (k * TILE_EDGE + j) * TILE_EDGE + p;
               const float4 v = reinterpret_cast<const BinTile<4> &>(T).hi[e];
-              const float dn = v.w - nref;
+              const float dn = (v.w - nref) + (reinterpret_cast<const BinTile<4> &>(T).lo[e] - rlo);
               const float2 wj = make_float2(wy[j], wy[j]);
               axy = ffma2(wj, make_float2(v.x, v.y), axy);
               azn = ffma2(wj, make_float2(v.z, dn), azn);
@@ -523,8 +504,7 @@ __global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp
             Gy += __shfl_xor_sync(mask, Gy, off);
             Gz += __shfl_xor_sync(mask, Gz, off);
           }
-          // |B| = centre (hi + lo) + rebased corner + interpolated delta
-          const double nv = f2d_exact(nch) + f2d_exact(ncl + (nref + Vn));
+          const double nv = f2d_exact(nref + (rlo + Vn));
           if (interleaved_rows<3, 4>(o)) {
             if (p == 0)
               st_v4(o.comps + i * 8, f2d_exact(Vx), f2d_exact(Vy), f2d_exact(Vz), nv);

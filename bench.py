@@ -59,6 +59,9 @@ def parse():
     return p.parse_args()
 
 
+EVAL_SMALL_TRAFFIC = 249.86e6  # dram read + write of eval_bin_kernel<4> on the 160^3 case (ncu capture)
+
+
 def run_profile(args):
     """Workloads for ncu captures (profiles/ cites these command lines)."""
     import torch
@@ -328,8 +331,9 @@ def main():
     value = world * nq * args.steps / dt
 
     # The dominant kernel is the evaluation pass over the bin-ordered records
-    # (46% of the step in the ncu launch list).  Bin the queries once, then
-    # time the evaluation launch alone on the launching stream.
+    # (56% of the step in the ncu launch list).  Bin the queries once, then
+    # time the evaluation launch alone on the launching stream, with the
+    # interleaved output rows the public API uses.
     from arbinterp_gb300 import _lib as LB
     L = LB.lib()
     o = tricubic(field, "quiet", mode="both", precision=prec, strategy=strat)
@@ -340,24 +344,27 @@ def main():
     need = int(L.arb_query_sorted_work_bytes(o._g, pc, nq))
     ws = torch.empty(need, dtype=torch.uint8, device=dev)
     f64 = dict(dtype=torch.float64, device=dev)
-    oc, on, og = torch.empty((nq, 3), **f64), torch.empty((nq, 1), **f64), torch.empty((nq, 3), **f64)
+    rows = torch.empty((nq, 8), **f64)                       # cx cy cz |B| gx gy gz -
     oi = torch.empty(nq, dtype=torch.int64, device=dev)
     st = torch.zeros(1, dtype=torch.int32, device=dev)
-    qo = LB.ArbQueryOut(oc.data_ptr(), on.data_ptr(), og.data_ptr(), oi.data_ptr(), None, None)
+    rp = rows.data_ptr()
+    qo = LB.ArbQueryOut(rp, rp + 24, rp + 32, oi.data_ptr(), None, None, 8, 8, 8)
     sp = torch.cuda.current_stream().cuda_stream
     LB.check(L.arb_query_bin(o._g, pc, q.clone().data_ptr(), nq, 3, 0, qo, ws.data_ptr(), need,
                              st.data_ptr(), sp), "arb_query_bin")
     kt = cuda_time(lambda: L.arb_query_eval_binned(o._g, pc, int(use_tab), nq, qo, ws.data_ptr(), need, sp),
                    5, 2) / 5
-    rec = 8 + 4 + 3 * (4 if prec == "mixed" else 8)          # packed cell, row, fraction
+    rec = 32 if prec == "mixed" else 48                       # bin-ordered query record
     grid_bytes = o._npts * (20 if prec == "mixed" else 32)    # grid read once (compulsory)
     algo = nq * (rec + 7 * 8) + (nq * 4 * 64 * (4 if prec == "mixed" else 8) if use_tab else grid_bytes)
     kname = ("eval_sorted_kernel<3,4,table>" if use_tab else
-             ("eval_sorted_coop4_kernel" if prec == "mixed" else "eval_sorted_kernel<3,4,fp64>"))
-    # DRAM traffic per launch, scaled from the small-case ncu capture
-    # (profiles/query_ingest_kernels__tricubic160_both_mixed.md: 523.8 MB for
-    # 2.02e6 queries on a 160^3 grid whose mixed grid is 81.9 MB)
-    traffic = (nq * (523.79e6 - 81.92e6) / 2.02e6 + grid_bytes) if (prec == "mixed" and not use_tab) else None
+             ("eval_bin_kernel<4>" if prec == "mixed" else "eval_sorted_kernel<3,4,fp64>"))
+    # DRAM traffic per launch, scaled from the small-case ncu capture of the
+    # same kernel (profiles/eval_bin_kernel__tricubic160_both_mixed.md:
+    # EVAL_SMALL_TRAFFIC bytes for 2.02e6 queries on a 160^3 grid whose mixed
+    # grid is 81.92 MB), per query plus one read of the grid
+    traffic = ((nq * (EVAL_SMALL_TRAFFIC - 81.92e6) / 2.02e6 + grid_bytes)
+               if (prec == "mixed" and not use_tab) else None)
     peak, peak_src = measured_peaks()
     achieved = algo / kt / 1e9
 
@@ -440,7 +447,11 @@ def main():
         cpu = cpu_baseline(field.cpu().numpy(), q.cpu().numpy(), lo, hi, h)
 
     if rank == 0:
-        launches_per_step = 6   # ingest: init, min, collect, sort, scatter; query: 1
+        # this library's kernels per step: ingest (meshgrid-order rows: probe, gather, summary;
+        # otherwise those three plus axes init/collect/sort, index, gather, summary) and the
+        # query (binned: count, scan, place, evaluate; plain: one)
+        launches_per_step = ((3 if o.ingest_path == "ordered" else 9) +
+                             (4 if o.last_plan.get("binned") else 1))
         line = {
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
