@@ -309,12 +309,7 @@ def main():
         o = tricubic(field, "quiet", mode="both", precision=prec, strategy=strat)
         return o.Query(q)
 
-    def tmax(t):
-        if world == 1:
-            return t
-        tt = torch.tensor([t], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        return float(tt.item())
+    from arbinterp_gb300.replicas import max_over_ranks as tmax   # replicas: whole-job time = max over ranks
 
     gpu_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0]) if \
         os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local
