@@ -53,6 +53,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--kernel-only", action="store_true", help="time only the query kernel (profiling)")
+    p.add_argument("--workload", default=None, choices=["c0", "c2", "c3", "c4"],
+                   help="measure one of the other seeded configurations and print its own JSON line: "
+                        "c0 = 41^3 scalar, 1e5 queries; c2 = 4D 64^3x32 scalar, 1e7 queries; c3 = 512 batched "
+                        "scalar fields in one persistent launch / CUDA graph; c4 = differentiable 128^3 "
+                        "float32 field, 1e6 queries, forward + backward")
     p.add_argument("--profile", default=None, choices=["step", "small", "small-table", "small-fp64", "small-coef"],
                    help="run a fixed workload for an ncu capture and exit (no timing, no JSON): "
                         "'step' = two full bench steps; 'small*' = 160^3 dipole field, 2.02e6 queries")
@@ -88,6 +93,179 @@ def run_profile(args):
             o.Query(q)
     torch.cuda.synchronize()
     print("profile workload done")
+
+
+# ---------------------------------------------------------------- other configurations
+def _normwise(a, b):
+    import torch
+    m = torch.isfinite(b).all(1)
+    return [float(x) for x in (a[m] - b[m]).abs().amax(0) / b[m].abs().amax(0).clamp_min(1e-300)]
+
+
+def run_workload(args):
+    """Seeded stand-ins for the other configurations; one JSON line each.
+    Mixed precision is compared with the float64 GPU path (itself pinned to
+    the reference by the parity tests)."""
+    import numpy as np
+    import torch
+    from arbinterp_gb300 import tricubic, quadcubic, synth, _lib
+    _lib.lib()
+    dev = torch.device("cuda")
+    gpu_index = torch.cuda.current_device()
+    line = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "higher_is_better": True, "workload": args.workload}
+    if args.workload in ("c0", "c2"):
+        if args.workload == "c0":
+            field = synth.gaussian_field3(n=(41, 41, 41), h=(0.1, 0.12, 0.08), seed=0, device=dev)
+            cls, dim, nin, nout = tricubic, 3, 100_000, 1_000
+            desc = "tricubic 41^3 scalar (8 Gaussians), construct + 1.01e5 queries (1e3 outside)"
+        else:
+            field = synth.moving_gaussian_field4(device=dev)
+            cls, dim, nin, nout = quadcubic, 4, 10_000_000, 0
+            desc = "quadcubic 64^3 x 32 scalar (6 moving Gaussians), construct + 1e7 queries"
+        o64 = cls(field, "quiet")
+        lo = [float(v) for v in o64._lo]
+        hi = [float(v) for v in o64._hi]
+        q = synth.uniform_queries(lo, hi, nin, nout, [float(v) for v in o64._h], seed=5, device=dev)
+        nq = q.shape[0]
+        res = {}
+        for prec in ("fp64", "mixed"):
+            for strat in (("otf", "table") if args.workload == "c2" else ("auto",)):
+                def step():
+                    return cls(field, "quiet", precision=prec, strategy=strat).Query(q)
+                with ClockSampler(gpu_index) as clk:
+                    dt = cuda_time(step, args.steps, args.warmup)
+                out = step()
+                res[(prec, strat)] = {"value": nq * args.steps / dt, "unit": "queries/s",
+                                      "ms_per_step": 1000 * dt / args.steps, "clocks": clk.summary(),
+                                      "_out": out}
+        ref = res[("fp64", "otf" if args.workload == "c2" else "auto")]["_out"]
+        for k, r in res.items():
+            got = r.pop("_out")
+            r["max_rel_err_vs_fp64"] = {"norms": _normwise(got[0], ref[0]), "grads": _normwise(got[1], ref[1])}
+        head = res[("mixed", "otf" if args.workload == "c2" else "auto")]
+        line.update({"metric": f"{args.workload}: queries/s, construct + query", "value": head["value"],
+                     "unit": "queries/s", "ms_per_step": head["ms_per_step"], "dtype": "f32",
+                     "config": {"workload": desc, "precision": "mixed"},
+                     "paths": {f"{p}/{s}": v for (p, s), v in res.items()}})
+    elif args.workload == "c3":
+        from arbinterp_gb300.batched import BatchedTricubic
+        fields, qs, counts = [], [], []
+        for f, nqf, seed in synth.batched_fields(device=dev):
+            o = tricubic(f, "quiet")
+            fields.append(f)
+            qs.append(synth.uniform_queries([float(v) for v in o._lo], [float(v) for v in o._hi], nqf, 0,
+                                            [float(v) for v in o._h], seed=seed % (1 << 30), device=dev))
+            counts.append(nqf)
+            del o
+        q = torch.cat(qs)
+        del qs
+        nq = q.shape[0]
+        out = {}
+        for prec in ("mixed", "fp64"):
+            b = BatchedTricubic(fields, precision=prec)
+            b.tune(q, counts)
+            qbuf = q.clone()
+            graph, outs = b.capture(qbuf, counts)
+            with ClockSampler(gpu_index) as clk:
+                dt = cuda_time(graph.replay, args.steps, args.warmup)
+            out[prec] = {"value": nq * args.steps / dt, "ms_per_step": 1000 * dt / args.steps,
+                         "tile_rows": b.tile_rows, "table_ratio": b.table_ratio, "clocks": clk.summary(),
+                         "_o": [t.clone() for t in outs]}
+            del b, graph, outs
+        off = np.concatenate([[0], np.cumsum(counts)])
+        per_field = []
+        for k in range(len(fields)):
+            sl = slice(int(off[k]), int(off[k + 1]))
+            e = [max(_normwise(a[sl], r[sl])) for a, r in zip(out["mixed"]["_o"], out["fp64"]["_o"])]
+            per_field.append(max(e))
+        for v in out.values():
+            v.pop("_o")
+        line.update({"metric": "c3: batched queries/s (one persistent launch, CUDA graph replay)",
+                     "value": out["mixed"]["value"], "unit": "queries/s",
+                     "ms_per_step": out["mixed"]["ms_per_step"], "dtype": "f32",
+                     "config": {"workload": f"{len(fields)} scalar fields, edges 16-128 log-uniform, "
+                                            f"{nq} queries in total (1e3-1e6 per field)",
+                                "precision": "mixed"},
+                     "paths": out,
+                     "per_field_max_rel_err_vs_fp64": {"max": max(per_field), "median": float(np.median(per_field))}})
+    else:  # c4
+        from arbinterp_gb300.autograd import TricubicField
+        # float32 samples; both precisions get the same (float64) geometry
+        rows = synth.gaussian_field3(n=(128, 128, 128), h=(0.1, 0.12, 0.08), seed=7, device=dev,
+                                     dtype=torch.float32).to(torch.float64)
+        f64 = TricubicField(rows, precision="fp64")
+        lo = [float(v) for v in f64.interp._lo]
+        hi = [float(v) for v in f64.interp._hi]
+        q = synth.uniform_queries(lo, hi, 1_000_000, 0, [float(v) for v in f64.interp._h], seed=8, device=dev)
+        v64 = f64.initial_values()
+        with torch.no_grad():
+            truth, _ = f64(v64, q)
+        gen = torch.Generator(device=dev).manual_seed(9)
+        target = truth + 1e-3 * torch.randn(truth.shape, generator=gen, device=dev, dtype=truth.dtype)
+        # rows whose cell index passes the last cell (float32 axes are not exactly evenly spaced, so
+        # floor((q - IntMin) / h) can reach the upper face; the reference raises IndexError there)
+        # come back NaN and are left out of the loss
+        keep = torch.isfinite(truth)
+        res = {}
+        for prec in ("mixed", "fp64"):
+            fld = TricubicField(rows, precision=prec) if prec == "mixed" else f64
+            vals = fld.initial_values().to(torch.float32 if prec == "mixed" else torch.float64)
+
+            def fwd_bwd():
+                v = vals.clone().requires_grad_(True)
+                qq = q.clone().requires_grad_(True)
+                val, _ = fld(v, qq)
+                diff = torch.where(keep, val - target.to(val.dtype), torch.zeros_like(val))
+                loss = (diff * diff).sum()
+                loss.backward()
+                return v.grad, qq.grad
+            with ClockSampler(gpu_index) as clk:
+                dt = cuda_time(fwd_bwd, args.steps, args.warmup)
+            gv, gq = fwd_bwd()
+            res[prec] = {"value": q.shape[0] * args.steps / dt, "ms_per_step": 1000 * dt / args.steps,
+                         "clocks": clk.summary(), "_g": (gv.double(), gq.double())}
+        # central differences of the (quadratic) loss on 1000 random grid values, float64
+        idx = torch.randperm(v64.numel(), generator=torch.Generator().manual_seed(10))[:1000].to(dev)
+
+        def loss64(v):
+            with torch.no_grad():
+                val, _ = f64(v, q)
+                return float(((val - target)[keep] ** 2).sum())
+        g64 = res["fp64"]["_g"][0]
+        gscale = float(g64[torch.isfinite(g64)].abs().max())
+        fd_err, fd_nan = [], 0
+        for j in idx.tolist():
+            eps = 1e-3
+            vp, vm = v64.clone(), v64.clone()
+            vp[j] += eps
+            vm[j] -= eps
+            fd = (loss64(vp) - loss64(vm)) / (2 * eps)
+            e = abs(fd - float(g64[j])) / max(1e-300, gscale)
+            if e == e:
+                fd_err.append(e)
+            else:
+                fd_nan += 1
+        gv_m, gq_m = res["mixed"]["_g"]
+        gv_d, gq_d = res["fp64"]["_g"]
+        m = torch.isfinite(gq_d).all(1)
+        for v in res.values():
+            v.pop("_g")
+        line.update({"metric": "c4: forward + backward queries/s (loss = sum of squared residuals)",
+                     "value": res["mixed"]["value"], "unit": "queries/s",
+                     "ms_per_step": res["mixed"]["ms_per_step"], "dtype": "f32",
+                     "config": {"workload": "128^3 float32 scalar field (8 Gaussians), 1e6 queries, targets = "
+                                            "float64 interpolant + N(0, 1e-3)", "precision": "mixed",
+                                "rows_left_out": int((~keep).sum())},
+                     "paths": res,
+                     "grad_values_fd_check": {"entries": len(fd_err) + fd_nan, "nan_entries": fd_nan,
+                                              "max_rel_err": max(fd_err) if fd_err else None,
+                                              "truth_nan": int(torch.isnan(truth).sum()),
+                                              "grad_nan": int(torch.isnan(g64).sum())},
+                     "mixed_vs_fp64_grad": {
+                         "values": float((gv_m - gv_d).abs().max() / gv_d.abs().max()),
+                         "queries": float((gq_m[m] - gq_d[m]).abs().max() / gq_d[m].abs().max())}})
+    print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------- clocks
@@ -286,6 +464,8 @@ def main():
         return run_reference(args)
     if args.profile:
         return run_profile(args)
+    if args.workload:
+        return run_workload(args)
     import numpy as np
     import torch
     import torch.distributed as dist
