@@ -233,7 +233,9 @@ static int coef_solve_mixed(const arb_grid *g, int64_t cell0, int64_t ncells, fl
 
 extern "C" int arb_coef_solve(const arb_grid *g, int32_t precision, int64_t cell0, int64_t ncells,
                               void *table, int32_t *status, arb_stream_t stream) {
-  if (!g || !table || !g->grid64) return ARB_ERR_INVALID;
+  // the 3D mixed solve reads only the float32 split; every other solve the float64 grid
+  const bool tc3 = precision == ARB_PREC_MIXED && g && g->dim == 3 && g->grid32;
+  if (!g || !table || (!tc3 && !g->grid64)) return ARB_ERR_INVALID;
   if (cell0 < 0 || ncells < 0 || cell0 + ncells > g->nc) return ARB_ERR_INVALID;
   if (ncells == 0) return ARB_OK;
   cudaStream_t s = (cudaStream_t)stream;

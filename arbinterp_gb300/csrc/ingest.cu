@@ -280,12 +280,14 @@ __device__ __forceinline__ void write_slot(const TF *row, int64_t dest, int64_t 
       raw_out[dest * 3 + 2] = (double)bz;
     }
   }
-  if (F == 4) {
-    reinterpret_cast<double2 *>(grid64)[dest * 2] = make_double2(out[0], out[1 % F]);
-    reinterpret_cast<double2 *>(grid64)[dest * 2 + 1] = make_double2(out[2 % F], out[3 % F]);
-  } else {
+  if (grid64) {
+    if (F == 4) {
+      reinterpret_cast<double2 *>(grid64)[dest * 2] = make_double2(out[0], out[1 % F]);
+      reinterpret_cast<double2 *>(grid64)[dest * 2 + 1] = make_double2(out[2 % F], out[3 % F]);
+    } else {
 #pragma unroll
-    for (int f = 0; f < F; ++f) grid64[dest * F + f] = out[f];
+      for (int f = 0; f < F; ++f) grid64[dest * F + f] = out[f];
+    }
   }
   if (grid32) {
     float hi[4], lo[4];
@@ -526,7 +528,7 @@ extern "C" int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64
                                   const int64_t *n, int32_t kind, double *grid64, float *grid32,
                                   double *raw_out, uint32_t *claim, int32_t *status,
                                   arb_stream_t stream) {
-  if (!field || !axes || !n || !grid64 || !claim || !status) return ARB_ERR_INVALID;
+  if (!field || !axes || !n || (!grid64 && !grid32) || !claim || !status) return ARB_ERR_INVALID;
   if (dim != 3 && dim != 4) return ARB_ERR_INVALID;
   int64_t prod = 1;
   for (int a = 0; a < dim; ++a) {
@@ -581,7 +583,7 @@ extern "C" int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64
                                   int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,
                                   int64_t *axis_count, double *grid64, float *grid32, double *raw_out,
                                   void *work, size_t work_bytes, int32_t *status, arb_stream_t stream) {
-  if (!field || !axis_out || !axis_count || !grid64 || !work || !status) return ARB_ERR_INVALID;
+  if (!field || !axis_out || !axis_count || (!grid64 && !grid32) || !work || !status) return ARB_ERR_INVALID;
   if ((dim != 3 && dim != 4) || npts <= 0 || axis_cap <= 0 || axis_cap > ARB_MAX_AXIS_CAP ||
       work_bytes < arb_ingest_axes_work_bytes(dim))
     return ARB_ERR_INVALID;

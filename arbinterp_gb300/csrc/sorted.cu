@@ -419,7 +419,7 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
 }
 
 template <int F>
-__global__ void __launch_bounds__(256, 3) eval_bin_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
+__global__ void __launch_bounds__(256, 4) eval_bin_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
                                                        arb_query_out o, SortedWork w) {
   extern __shared__ __align__(16) unsigned char bin_smem[];
   BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(bin_smem);
@@ -564,7 +564,7 @@ static bool launch_eval_bin(const arb_grid *g, const KParams &kp, const BinGeom 
       return false;
     attr = true;
   }
-  int64_t grid = (int64_t)sm_count_sorted() * 3;  // 3 resident per SM (registers)
+  int64_t grid = (int64_t)sm_count_sorted() * 4;  // 4 resident per SM (64 registers)
   if (grid > bg.nbins) grid = bg.nbins;
   if (grid < 1) grid = 1;
   eval_bin_kernel<4><<<(unsigned)grid, 256, smem, s>>>(*g, kp, bg, nq, *out, w);

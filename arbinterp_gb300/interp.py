@@ -145,12 +145,19 @@ class _Interpolant:
         status = torch.zeros(1, dtype=torch.int32, device=dev)
         s = _stream()
         kind, F = self._kind, self._F
-        grid64 = torch.empty(npts * F, dtype=torch.float64, device=dev)
+        # Mixed precision with the caller's own CUDA tensor: the float64 grid is
+        # not needed by the float32 query path and is produced on first use from
+        # that tensor (if it is still unmodified) instead of on every construction.
+        lazy64 = (self.precision == "mixed" and isinstance(field, torch.Tensor)
+                  and ft.data_ptr() == field.data_ptr())
+        self._src = (ft, ft._version, is32, ncol) if lazy64 else None
+        grid64 = None if lazy64 else torch.empty(npts * F, dtype=torch.float64, device=dev)
         # mixed-precision grid: F=1 (hi, lo); F=3 float4 of hi; F=4 float4 of hi + lo of |B|
         g32_floats = {1: 2, 3: 4, 4: 5}[F]
         grid32 = (torch.empty(npts * g32_floats, dtype=torch.float32, device=dev)
                   if self.precision == "mixed" else None)
-        raw = torch.empty(npts * 3, dtype=torch.float64, device=dev) if kind == _lib.KIND_NORM else None
+        raw = (torch.empty(npts * 3, dtype=torch.float64, device=dev)
+               if kind == _lib.KIND_NORM and not lazy64 else None)
         ax64 = axes[: dim * cap].view(dim, cap)
         summ = torch.empty(17, dtype=torch.float64, device=dev)
 
@@ -164,7 +171,7 @@ class _Interpolant:
         if _ORDERED_INGEST and npts < 0xFFFFFFFF:
             # rows in meshgrid order (the common case): one pass, no sort
             check(L.arb_ingest_ordered(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
-                                       counts.data_ptr(), grid64.data_ptr(), _ptr(grid32), _ptr(raw),
+                                       counts.data_ptr(), _ptr(grid64), _ptr(grid32), _ptr(raw),
                                        work.data_ptr(), wb, status.data_ptr(), s), "arb_ingest_ordered")
             sm = summary()
             done = int(sm[0]) == 0
@@ -185,7 +192,7 @@ class _Interpolant:
             claim = torch.empty(npts, dtype=torch.int32, device=dev)
             n_c = (ctypes.c_int64 * 4)(*(n + [1] * (4 - dim)))
             check(L.arb_ingest_scatter(ft.data_ptr(), is32, npts, ncol, dim, ax64.data_ptr(), cap,
-                                       n_c, kind, grid64.data_ptr(), _ptr(grid32), _ptr(raw),
+                                       n_c, kind, _ptr(grid64), _ptr(grid32), _ptr(raw),
                                        claim.data_ptr(), status.data_ptr(), s), "arb_ingest_scatter")
             sm = summary()
             if self.check and int(sm[0]):
@@ -196,7 +203,8 @@ class _Interpolant:
         self._n = n
         self._npts = npts
         self.ingest_path = "ordered" if done else "general"
-        self._grid64, self._grid32, self._raw = grid64, grid32, raw
+        self._grid64_t, self._grid32, self._raw_t = grid64, grid32, raw
+        self._ingest_ordered = done
         self._status = status
         # reference attributes, computed in the field's own dtype (ARB:541-568)
         dt = self._field_dtype
@@ -222,11 +230,57 @@ class _Interpolant:
             g.hi[a] = float(hi[a]) if a < dim else 0.0
             g.h[a] = float(h[a]) if a < dim else 1.0
         g.nc = self.nc
-        g.grid64 = grid64.data_ptr()
+        g.grid64 = _ptr(grid64)
         g.grid32 = _ptr(grid32)
         g.table = None
         g.table_prec = 0
         self._g = g
+
+    @property
+    def _grid64(self):
+        """[npts*F] float64 grid values (produced on first use in the lazy case)."""
+        if self._grid64_t is None:
+            self._materialise_grid64()
+        return self._grid64_t
+
+    @property
+    def _raw(self):
+        if self._grid64_t is None and self._src is not None:
+            self._materialise_grid64()
+        return self._raw_t
+
+    def _materialise_grid64(self):
+        ft, version, is32, ncol = self._src
+        if ft._version != version:
+            raise RuntimeError("the field tensor was modified in place after this mixed-precision interpolant "
+                               "was built; its float64 grid values are no longer available")
+        L = lib()
+        dim, npts, F, dev = self._dim, self._npts, self._F, self.device
+        s = _stream()
+        grid64 = torch.empty(npts * F, dtype=torch.float64, device=dev)
+        raw = torch.empty(npts * 3, dtype=torch.float64, device=dev) if self._kind == _lib.KIND_NORM else None
+        cap = max(4, min(npts, _AXIS_CAP))
+        axes = torch.empty(2 * dim * cap, dtype=torch.float64, device=dev)
+        counts = torch.zeros(dim, dtype=torch.int64, device=dev)
+        wb = L.arb_ingest_axes_work_bytes(dim)
+        work = torch.empty(int(wb), dtype=torch.uint8, device=dev)
+        if self._ingest_ordered:
+            check(L.arb_ingest_ordered(ft.data_ptr(), is32, npts, ncol, dim, self._kind, cap, axes.data_ptr(),
+                                       counts.data_ptr(), grid64.data_ptr(), None, _ptr(raw), work.data_ptr(),
+                                       wb, self._status.data_ptr(), s), "arb_ingest_ordered")
+        else:
+            check(L.arb_ingest_axes(ft.data_ptr(), is32, npts, ncol, dim, cap, axes.data_ptr(),
+                                    counts.data_ptr(), work.data_ptr(), wb, self._status.data_ptr(), s),
+                  "arb_ingest_axes")
+            claim = torch.empty(npts, dtype=torch.int32, device=dev)
+            n_c = (ctypes.c_int64 * 4)(*(self._n + [1] * (4 - dim)))
+            check(L.arb_ingest_scatter(ft.data_ptr(), is32, npts, ncol, dim, axes.data_ptr(), cap, n_c,
+                                       self._kind, grid64.data_ptr(), None, _ptr(raw), claim.data_ptr(),
+                                       self._status.data_ptr(), s), "arb_ingest_scatter")
+        if L.arb_status_fetch(self._status.data_ptr(), s):
+            raise RuntimeError("re-reading the field for its float64 grid values failed")
+        self._grid64_t, self._raw_t = grid64, raw
+        self._g.grid64 = grid64.data_ptr()
 
     def _set_counts(self, n):
         raise NotImplementedError
@@ -247,6 +301,8 @@ class _Interpolant:
 
     def _solve(self, cell0, ncells):
         self._ensure_table()
+        if not (self.precision == "mixed" and self._dim == 3):
+            self._grid64                      # the float64 grid (materialised if needed)
         L = lib()
         rc = L.arb_coef_solve(self._g, self._table_prec, cell0, ncells,
                               self._table.data_ptr() + cell0 * self._F * self._M * self._table.element_size(),

@@ -120,7 +120,9 @@ int arb_ingest_axes(const void *field, int32_t field_is_f32, int64_t npts, int32
  * columns [npts][ncol-dim] in sorted order.  claim is npts uint32 of scratch
  * (it receives the inverse permutation grid slot -> row, and detects
  * duplicate points).  n holds the host-side axis counts returned by
- * arb_ingest_axes.  npts < 2^32. */
+ * arb_ingest_axes.  grid64 may be NULL when grid32 is given (a
+ * mixed-precision interpolant whose float64 values are produced later, by a
+ * second call with grid32 NULL).  npts < 2^32. */
 int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
                        int32_t dim, const double *axes, int64_t axis_cap, const int64_t *n,
                        int32_t kind, double *grid64, float *grid32, double *raw_out,
@@ -136,7 +138,8 @@ int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64_t npts, in
  * (or not a full grid) it sets ARB_ERR_IRREGULAR_GRID in *status and leaves
  * the outputs undefined: the caller then runs arb_ingest_axes +
  * arb_ingest_scatter, which give the authoritative answer.  work holds
- * arb_ingest_axes_work_bytes(dim) bytes.  npts < 2^32.  Replaces the same
+ * arb_ingest_axes_work_bytes(dim) bytes.  grid64 or grid32 may be NULL (not
+ * both), as for arb_ingest_scatter.  npts < 2^32.  Replaces the same
  * reference code as the two-step ingest (ARB:528-568, 1264-1320). */
 int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
                        int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,

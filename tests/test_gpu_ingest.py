@@ -112,3 +112,30 @@ def test_other_orders_fall_back():
     dup[5] = dup[6]                                     # duplicate point, one slot empty
     with pytest.raises(ValueError):
         tricubic(dup, "quiet")
+
+
+@pytest.mark.parametrize("mode", ["both", "norm"])
+def test_mixed_device_field_float64_grid_on_first_use(mode):
+    """Mixed precision on a CUDA field tensor skips the float64 grid at
+    construction; it is produced from the (unmodified) tensor when first
+    needed and equals the eagerly built one."""
+    import torch
+    from arbinterp_gb300 import tricubic
+    f = torch.from_numpy(_field(3, (2, 1, 0), (), vector=True)).cuda()
+    eager = tricubic(f.cpu().numpy(), "quiet", mode=mode, precision="mixed")   # NumPy input: eager
+    lazy = tricubic(f, "quiet", mode=mode, precision="mixed")
+    assert eager._grid64_t is not None and lazy._grid64_t is None
+    q = np.random.default_rng(6).uniform(f[:, :3].min(0).values.cpu().numpy(),
+                                         f[:, :3].max(0).values.cpu().numpy(), (300, 3))
+    for x, y in zip(lazy.Query(q.copy()), eager.Query(q.copy())):
+        assert np.array_equal(x, y, equal_nan=True)
+    assert lazy._grid64_t is None                   # queries never needed it
+    assert np.array_equal(lazy.inputfield, eager.inputfield)
+    assert lazy._grid64_t is not None
+    for name in ("Bx", "By", "Bz", "Bn") if mode == "both" else ("Bn",):
+        a, b = getattr(lazy, name), getattr(eager, name)
+        assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max(), name   # double-float |B| vs float64
+    again = tricubic(f, "quiet", mode=mode, precision="mixed")
+    f[0, 3] += 1.0                                   # the caller changes the field in place
+    with pytest.raises(RuntimeError):
+        again.inputfield
