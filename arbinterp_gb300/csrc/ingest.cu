@@ -447,7 +447,9 @@ __global__ void __launch_bounds__(256) ordered_gather_kernel(const TF *field, in
                                                              const double *axes, int64_t cap, const OrderWork *w,
                                                              double *grid64, float *grid32, double *raw_out,
                                                              int32_t *status) {
-  if (!w->ok) return;
+  // rows whose fastest axis is x: slot order is row order (up to direction),
+  // both sides coalesced; other orders go through ordered_tile_kernel
+  if (!w->ok || (w->stride[0] != 1 && w->stride[0] != -1)) return;
   uint32_t nn[DIM];
   int64_t st[DIM];
 #pragma unroll
@@ -477,6 +479,104 @@ __global__ void __launch_bounds__(256) ordered_gather_kernel(const TF *field, in
     if (!ok) set_status(status, ARB_ERR_IRREGULAR_GRID);
     write_slot<TF, KIND>(row, dest, npts, DIM, grid64, grid32, raw_out);
   }
+}
+
+// Rows whose fastest axis S is not x (e.g. meshgrid(..., indexing='ij') with
+// x slowest): consecutive grid slots come from rows |stride_x| apart, so a
+// direct gather reads one scattered row per slot.  Instead a CTA takes a
+// 32 (x) x 32 (S) tile at fixed other coordinates, reads its 1024 rows with
+// consecutive threads on consecutive rows (S runs along the rows), keeps them
+// in shared memory, and writes the slots with consecutive threads on
+// consecutive x.  Persistent over tiles.
+constexpr int OT = 32;
+
+template <typename TF, int KIND, int DIM>
+__global__ void __launch_bounds__(256) ordered_tile_kernel(const TF *field, int64_t npts, const double *axes,
+                                                           int64_t cap, const OrderWork *w, double *grid64,
+                                                           float *grid32, double *raw_out, int32_t *status) {
+  constexpr int NC = DIM + (KIND == ARB_KIND_SCALAR ? 1 : 3);
+  if (!w->ok || w->stride[0] == 1 || w->stride[0] == -1) return;
+  extern __shared__ __align__(16) unsigned char ot_smem[];
+  TF(*tile)[OT + 1][NC] = reinterpret_cast<TF(*)[OT + 1][NC]>(ot_smem);
+  int64_t nn[DIM], st[DIM];
+  int S = 1;
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    nn[a] = w->n[a];
+    st[a] = w->stride[a];
+    if (st[a] == 1 || st[a] == -1) S = a;
+  }
+  int64_t pstride[DIM];  // slot strides (x fastest)
+  pstride[0] = 1;
+#pragma unroll
+  for (int a = 1; a < DIM; ++a) pstride[a] = pstride[a - 1] * nn[a - 1];
+  const int64_t tx_n = (nn[0] + OT - 1) / OT, ts_n = (nn[S] + OT - 1) / OT;
+  const int64_t ntiles = tx_n * ts_n * (npts / (nn[0] * nn[S]));
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int64_t i[DIM];
+    const int64_t xt = t % tx_n;
+    int64_t r = t / tx_n;
+    const int64_t stile = r % ts_n;
+    r /= ts_n;
+#pragma unroll
+    for (int a = 1; a < DIM; ++a) {  // the remaining axes, slowest last
+      if (a == S) continue;
+      i[a] = r % nn[a];
+      r /= nn[a];
+    }
+    // load: consecutive threads read consecutive rows (along S)
+    for (int k = ty; k < OT; k += 8) {
+      i[0] = xt * OT + k;
+      i[S] = stile * OT + tx;
+      if (i[0] < nn[0] && i[S] < nn[S]) {
+        int64_t src = 0;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) src += st[a] > 0 ? i[a] * st[a] : (nn[a] - 1 - i[a]) * (-st[a]);
+        load_field_row<TF, NC>(field + src * NC, tile[k][tx]);
+      }
+    }
+    __syncthreads();
+    // write: consecutive threads write consecutive slots (along x)
+    for (int k = ty; k < OT; k += 8) {
+      i[0] = xt * OT + tx;
+      i[S] = stile * OT + k;
+      if (i[0] < nn[0] && i[S] < nn[S]) {
+        const TF *row = tile[tx][k];
+        int64_t dest = 0;
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+          dest += i[a] * pstride[a];
+          ok &= __double_as_longlong(to_f64(row[a])) == __double_as_longlong(__ldg(axes + a * cap + i[a]));
+        }
+        if (!ok) set_status(status, ARB_ERR_IRREGULAR_GRID);
+        write_slot<TF, KIND>(row, dest, npts, DIM, grid64, grid32, raw_out);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename TF, int KIND, int DIM>
+static void launch_ordered_tile(const void *field, int64_t npts, const double *axes, int64_t cap,
+                                const OrderWork *w, double *grid64, float *grid32, double *raw_out, int32_t *status,
+                                cudaStream_t s) {
+  constexpr int NC = DIM + (KIND == ARB_KIND_SCALAR ? 1 : 3);
+  const size_t smem = sizeof(TF) * OT * (OT + 1) * NC;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(ordered_tile_kernel<TF, KIND, DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    attr = true;
+  }
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t grid = (int64_t)sms * 4, tiles_max = npts / (OT * 4) + 1;  // tiles >= npts / 1024 when a tile is full
+  if (grid > tiles_max) grid = tiles_max;
+  ordered_tile_kernel<TF, KIND, DIM><<<(unsigned)grid, 256, smem, s>>>((const TF *)field, npts, axes, cap, w,
+                                                                       grid64, grid32, raw_out, status);
 }
 
 static int grid_blocks(int64_t n, int threads) {
@@ -600,13 +700,16 @@ extern "C" int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64
                                                    axis_count, w, status);
   const int T = 256;
   const int B = grid_blocks(npts, T);
-#define ARB_OGATHER(TF, K)                                                                              \
-  if (dim == 3)                                                                                         \
-    ordered_gather_kernel<TF, K, 3><<<B, T, 0, s>>>((const TF *)field, npts, ncol, axis_out, axis_cap, w, \
-                                                    grid64, grid32, raw_out, status);                     \
-  else                                                                                                  \
-    ordered_gather_kernel<TF, K, 4><<<B, T, 0, s>>>((const TF *)field, npts, ncol, axis_out, axis_cap, w, \
-                                                    grid64, grid32, raw_out, status)
+#define ARB_OGATHER(TF, K)                                                                                 \
+  if (dim == 3) {                                                                                          \
+    ordered_gather_kernel<TF, K, 3><<<B, T, 0, s>>>((const TF *)field, npts, ncol, axis_out, axis_cap, w,    \
+                                                    grid64, grid32, raw_out, status);                        \
+    launch_ordered_tile<TF, K, 3>(field, npts, axis_out, axis_cap, w, grid64, grid32, raw_out, status, s); \
+  } else {                                                                                                 \
+    ordered_gather_kernel<TF, K, 4><<<B, T, 0, s>>>((const TF *)field, npts, ncol, axis_out, axis_cap, w,    \
+                                                    grid64, grid32, raw_out, status);                        \
+    launch_ordered_tile<TF, K, 4>(field, npts, axis_out, axis_cap, w, grid64, grid32, raw_out, status, s); \
+  }
 #define ARB_OGATHER_KIND(TF)                                         \
   switch (kind) {                                                    \
     case ARB_KIND_SCALAR: ARB_OGATHER(TF, ARB_KIND_SCALAR); break;   \
