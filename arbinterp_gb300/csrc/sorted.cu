@@ -446,9 +446,16 @@ __global__ void __launch_bounds__(256, 4) eval_bin_kernel(arb_grid g, KParams kp
       int64_t og[3];
       bin_origin(b, bg, og);
       if (F == 4) {
-        // 4 lanes per query, lane p owning x offset p of every block row
-        for (int64_t t = t0 + (threadIdx.x >> 2); t < t1; t += blockDim.x >> 2) {
-          const QRec<float> r = reinterpret_cast<const QRec<float> *>(w.rec)[t];
+        // 4 lanes per query, lane p owning x offset p of every block row; the
+        // next record is loaded while this one is evaluated
+        const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
+        const int64_t tstep = blockDim.x >> 2;
+        int64_t t = t0 + (threadIdx.x >> 2);
+        QRec<float> rnext;
+        if (t < t1) rnext = recs[t];
+        for (; t < t1; t += tstep) {
+          const QRec<float> r = rnext;
+          if (t + tstep < t1) rnext = recs[t + tstep];
           const int64_t i = r.row;
           int64_t c[3];
           unpack_cell<3>(r.cell, c);
