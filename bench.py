@@ -58,9 +58,14 @@ def parse():
                         "c0 = 41^3 scalar, 1e5 queries; c2 = 4D 64^3x32 scalar, 1e7 queries; c3 = 512 batched "
                         "scalar fields in one persistent launch / CUDA graph; c4 = differentiable 128^3 "
                         "float32 field, 1e6 queries, forward + backward")
-    p.add_argument("--profile", default=None, choices=["step", "small", "small-table", "small-fp64", "small-coef"],
+    p.add_argument("--profile", default=None,
+                   choices=["step", "small", "small-table", "small-fp64", "small-coef", "small-4d", "small-batched",
+                            "small-adjoint"],
                    help="run a fixed workload for an ncu capture and exit (no timing, no JSON): "
-                        "'step' = two full bench steps; 'small*' = 160^3 dipole field, 2.02e6 queries")
+                        "'step' = two full bench steps; 'small*' = 160^3 dipole field, 2.02e6 queries; "
+                        "'small-coef' = 96^3 table solve; 'small-4d' = 40^3x12 scalar, 2e6 queries (on the fly "
+                        "and table); 'small-batched' = 64 scalar fields; 'small-adjoint' = 96^3 scalar, 2e6 "
+                        "queries forward + backward")
     return p.parse_args()
 
 
@@ -76,6 +81,41 @@ def run_profile(args):
         field, q, lo, hi, h = make_workload(dev)
         for _ in range(2):
             tricubic(field, "quiet", mode="both", precision=args.precision, strategy=args.strategy).Query(q)
+    elif args.profile == "small-4d":
+        from arbinterp_gb300 import quadcubic
+        field = synth.moving_gaussian_field4(n=(40, 40, 40, 12), device=dev)
+        for prec in ("mixed", "fp64"):
+            for strat in ("otf", "table"):
+                o = quadcubic(field, "quiet", precision=prec, strategy=strat)
+                q = synth.uniform_queries([float(v) for v in o._lo], [float(v) for v in o._hi], 2_000_000, 0,
+                                          [float(v) for v in o._h], seed=3, device=dev)
+                o.Query(q)
+    elif args.profile == "small-batched":
+        from arbinterp_gb300.batched import BatchedTricubic
+        fields, qs, counts = [], [], []
+        for f, nqf, seed in synth.batched_fields(n_fields=64, device=dev):
+            o = tricubic(f, "quiet")
+            fields.append(f)
+            qs.append(synth.uniform_queries([float(v) for v in o._lo], [float(v) for v in o._hi], nqf, 0,
+                                            [float(v) for v in o._h], seed=seed % (1 << 30), device=dev))
+            counts.append(nqf)
+        b = BatchedTricubic(fields, precision="mixed")
+        b.tile_rows, b.table_ratio = 1024, None      # fixed plan: no tuning launches in the capture
+        b._apply_strategy(counts, None)
+        q = torch.cat(qs)
+        for _ in range(2):
+            b.query(q, counts)
+    elif args.profile == "small-adjoint":
+        from arbinterp_gb300.autograd import TricubicField
+        rows = synth.gaussian_field3(n=(96, 96, 96), seed=7, device=dev)
+        for prec in ("mixed", "fp64"):
+            fld = TricubicField(rows, precision=prec)
+            q = synth.uniform_queries([float(v) for v in fld.interp._lo], [float(v) for v in fld.interp._hi],
+                                      2_000_000, 0, [float(v) for v in fld.interp._h], seed=8, device=dev)
+            v = fld.initial_values().clone().requires_grad_(True)
+            qq = q.clone().requires_grad_(True)
+            val, _ = fld(v, qq)
+            torch.nan_to_num(val).sum().backward()
     elif args.profile == "small-coef":
         # 96^3 'both' field: 804k cells x 4 fields x 64 float32 coefficients = 0.82 GB table
         field = synth.dipole_field3(n=(96, 96, 96), seed=1, device=dev)
