@@ -75,6 +75,8 @@ SIGNATURES = {
                                         C.c_size_t, _P]),
     "arb_query_eval_sorted_noalloc": (C.c_int, [C.POINTER(ArbGrid), _I32, _I32, _P, _I64, _I64, _I32,
                                                 C.POINTER(ArbQueryOut), _P, _P]),
+    "arb_rk4_trajectories": (C.c_int, [C.POINTER(ArbGrid), _I32, _P, _I64, C.c_double, _I64, C.c_double,
+                                       C.POINTER(C.c_double), _P, _I64, _P, _P]),
     "arb_status_fetch": (C.c_int, [_P, _P]),
     "arb_version": (C.c_char_p, []),
 }

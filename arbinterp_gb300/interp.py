@@ -314,6 +314,47 @@ class _Interpolant:
         """Solve every cell's coefficients (ARB:523-525, 1260-1262)."""
         self._solve(0, self.nc)
 
+    def _table_meta(self):
+        """Geometry, precision and a checksum of the grid values a table belongs to."""
+        src = self._grid32 if self.precision == "mixed" else self._grid64
+        v = src.to(torch.float64)
+        w = torch.arange(1, v.numel() + 1, dtype=torch.float64, device=v.device) / v.numel()
+        checks = torch.stack([v.sum(), (v * v).sum(), (v * w).sum()]).cpu().numpy()
+        return {"dim": self._dim, "kind": self._kind, "nfield": self._F, "precision": self.precision,
+                "n": np.array(self._n, dtype=np.int64),
+                "lo": np.array(self._lo, dtype=np.float64), "hi": np.array(self._hi, dtype=np.float64),
+                "h": np.array(self._h, dtype=np.float64), "checks": checks}
+
+    def save_coefficients(self, path):
+        """Write the whole coefficient table (solving it first if needed) to
+        `path` (NumPy .npz): the cell-major table [nc][F][4^dim] in this
+        interpolant's precision, plus the grid geometry and a checksum of the
+        grid values (the reference's planned "save these coefficients to a
+        file for later use", CHANGELOG.md v1.8.0)."""
+        if not self._table_complete:
+            self.allCoeffs()
+        np.savez(path, table=self._table.cpu().numpy(), **self._table_meta())
+
+    def load_coefficients(self, path):
+        """Load a table written by `save_coefficients` for the same field
+        (geometry, mode, precision and grid values must match; ValueError
+        otherwise).  Later queries with strategy 'auto' or 'table' use it."""
+        d = np.load(path)
+        meta = self._table_meta()
+        for k in ("dim", "kind", "nfield", "n", "lo", "hi", "h"):
+            if not np.array_equal(np.asarray(d[k]), np.asarray(meta[k])):
+                raise ValueError(f"coefficient file does not match this interpolant ({k} differs)")
+        if str(d["precision"]) != self.precision:
+            raise ValueError(f"coefficient file holds a {d['precision']} table; this interpolant is {self.precision}")
+        if not np.allclose(d["checks"], meta["checks"], rtol=1e-12, atol=0):
+            raise ValueError("coefficient file was solved from different grid values")
+        t = d["table"]
+        if t.size != self.nc * self._F * self._M:
+            raise ValueError("coefficient file has the wrong table size")
+        self._ensure_table()
+        self._table.copy_(torch.from_numpy(t.reshape(-1)))
+        self._solved[:] = True
+
     def calcCoefficients(self, alphaindex):
         """Solve one cell (ARB:570-603, 1322-1355)."""
         i = int(alphaindex)
@@ -485,6 +526,43 @@ class _Interpolant:
         if k == _lib.KIND_BOTH:
             return c, nv, gv
         return nv, gv
+
+    def trajectories(self, x0, v0, dt, nsteps, coef=-1.0, gravity=(0.0, 0.0, 0.0), record_every=0):
+        """Integrate particles through the field on the device (3D, scalar,
+        norm or both mode): fourth-order Runge-Kutta on x' = v,
+        v' = coef * grad f(x) + gravity, with f the interpolated scalar or |B|
+        (coef = -mu/m for a weak-field seeker in a magnetic trap).
+
+        x0, v0: (N, 3) NumPy arrays or CUDA tensors.  Returns (x, v) after
+        nsteps steps of dt, and with record_every > 0 also the path
+        (nsteps // record_every, N, 6) of (x, v) states; arrays of the input
+        kind.  Particles that leave the interpolation volume come back NaN;
+        `self.lost` counts them."""
+        if self._dim != 3:
+            raise NotImplementedError("trajectories are built for 3D fields")
+        if self._kind == _lib.KIND_VECTOR:
+            raise ValueError("trajectories need a gradient: scalar, norm or both mode")
+        on_dev = isinstance(x0, torch.Tensor) and x0.is_cuda
+        dev = self.device
+        x = torch.as_tensor(x0, dtype=torch.float64).to(dev).reshape(-1, 3)
+        v = torch.as_tensor(v0, dtype=torch.float64).to(dev).reshape(-1, 3)
+        if x.shape != v.shape:
+            raise ValueError("x0 and v0 must have the same shape")
+        n = x.shape[0]
+        state = torch.cat([x, v], 1).contiguous()
+        nrec = nsteps // record_every if record_every > 0 else 0
+        path = torch.empty((nrec, n, 6), dtype=torch.float64, device=dev) if nrec else None
+        lost = torch.zeros(1, dtype=torch.int64, device=dev)
+        grav = (ctypes.c_double * 3)(*[float(v_) for v_ in gravity])
+        prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_MIXED
+        check(lib().arb_rk4_trajectories(self._g, prec, state.data_ptr(), n, float(dt), int(nsteps), float(coef),
+                                         grav, _ptr(path), int(record_every) if nrec else 0, lost.data_ptr(),
+                                         _stream()), "arb_rk4_trajectories")
+        self.lost = int(lost.item())
+        out = [state[:, :3], state[:, 3:]] + ([path] if nrec else [])
+        if not on_dev:
+            out = [t.cpu().numpy() for t in out]
+        return tuple(out)
 
     def Query(self, query):
         """Shape dispatch (Query1/2/3, ARB:177-211): rows -> rQuery, a single

@@ -282,6 +282,21 @@ int arb_query_eval_sorted_noalloc(const arb_grid *g, int32_t precision, int32_t 
                                   double *q, int64_t nq, int64_t q_stride, int32_t q_writeback,
                                   const arb_query_out *out, int32_t *status, arb_stream_t stream);
 
+/* ---- particle trajectories (no reference counterpart: the reference was
+ *      written to simulate particle motion in magnetic fields and planned
+ *      integrators for it, CHANGELOG.md v1.0.0).  Fourth-order Runge-Kutta on
+ *      x' = v, v' = coef * grad f(x) + gravity, f the interpolated scalar
+ *      (scalar / norm modes) or |B| (both mode), 3D only; one thread per
+ *      particle, four on-the-fly evaluations per step in the given precision.
+ *      state is [n][6] (x, y, z, vx, vy, vz), updated in place; a particle
+ *      whose stage leaves the interpolation volume (or lands on a cell index
+ *      >= nc) becomes NaN and increments *lost (device counter).  path, when
+ *      not NULL, receives the state every record_every steps:
+ *      [nsteps / record_every][n][6]. ------------------------------------- */
+int arb_rk4_trajectories(const arb_grid *g, int32_t precision, double *state, int64_t n, double dt,
+                         int64_t nsteps, double coef, const double *gravity, double *path,
+                         int64_t record_every, unsigned long long *lost, arb_stream_t stream);
+
 /* Reads (and clears) the device status word after the stream's work is
  * done; returns ARB_OK, an arb_status bit set, or ARB_ERR_CUDA. */
 int arb_status_fetch(int32_t *status, arb_stream_t stream);
