@@ -109,6 +109,12 @@ class _Interpolant:
         self._F = _F[kind]
         self._extra_col = extra_col
         self._sentinel_nan = sentinel_nan
+        bc = kwargs.get("boundary", None)
+        if bc is not None:
+            if bc not in ("neumann", "dirichlet"):
+                raise ValueError("boundary must be None, 'neumann' or 'dirichlet'")
+            field = self._pad_field(field, bc)
+        self.boundary = bc
         self._ingest(field)
         if not quiet:
             print(_BANNERS[banner])
@@ -120,6 +126,46 @@ class _Interpolant:
         self.last_plan = None
 
     # ------------------------------------------------------------------ ingest
+    def _pad_field(self, field, bc):
+        """Field rows extended by one ghost layer on every face, so that the
+        interpolation volume becomes the whole input grid (the reference
+        loses one cell layer per face; README.md "Further work will implement
+        boundary conditions of the Neumann or Dirichlet types").
+        'neumann': zero normal derivative at the boundary node, ghost = mirror
+        image of the first interior node (f[-1] = f[1]); 'dirichlet': the
+        boundary samples are the prescribed values, continued by odd
+        reflection (f[-1] = 2 f[0] - f[1], zero second difference at the
+        boundary node).  Ghost coordinates continue the axis spacing."""
+        dim = self._dim
+        dev = self.device
+        ft = field if isinstance(field, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(np.asarray(field)))
+        dtype = ft.dtype if ft.dtype in (torch.float32, torch.float64) else torch.float64
+        ncol = int(ft.shape[1])
+        nval = ncol - dim
+        # sorted samples and axes from a float64 interpolant of the raw value columns
+        kw = {} if nval == 1 else {"mode": "vector"}
+        base = type(self)(ft.to(dev, torch.float64), "quiet", precision="fp64", **kw)
+        n = base._n
+        vals = base._grid64.view(*reversed(n), nval)          # (t,) z, y, x, value
+        axes = [base._axes_dev[a].to(torch.float64) for a in range(dim)]
+        for a in range(dim):                                    # pad axis a (tensor dim dim-1-a)
+            d = dim - 1 - a
+            lo_i, hi_i = vals.narrow(d, 1, 1), vals.narrow(d, n[a] - 2, 1)
+            if bc == "neumann":
+                g_lo, g_hi = lo_i, hi_i
+            else:
+                g_lo = 2.0 * vals.narrow(d, 0, 1) - lo_i
+                g_hi = 2.0 * vals.narrow(d, n[a] - 1, 1) - hi_i
+            vals = torch.cat([g_lo, vals, g_hi], d)
+            ax = axes[a]
+            h = ax[1] - ax[0]
+            axes[a] = torch.cat([ax[:1] - h, ax, ax[-1:] + (ax[-1] - ax[-2])])
+        mesh = torch.meshgrid(*reversed(axes), indexing="ij")   # slowest first, x fastest
+        cols = [mesh[dim - 1 - a].reshape(-1) for a in range(dim)]
+        rows = torch.cat([torch.stack(cols, 1), vals.reshape(-1, nval)], 1).to(dtype)
+        del base
+        return rows if isinstance(field, torch.Tensor) else rows.cpu().numpy()
+
     def _ingest(self, field):
         L = lib()
         dim = self._dim

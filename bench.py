@@ -53,11 +53,12 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--kernel-only", action="store_true", help="time only the query kernel (profiling)")
-    p.add_argument("--workload", default=None, choices=["c0", "c2", "c3", "c4"],
+    p.add_argument("--workload", default=None, choices=["c0", "c2", "c3", "c4", "traj"],
                    help="measure one of the other seeded configurations and print its own JSON line: "
                         "c0 = 41^3 scalar, 1e5 queries; c2 = 4D 64^3x32 scalar, 1e7 queries; c3 = 512 batched "
                         "scalar fields in one persistent launch / CUDA graph; c4 = differentiable 128^3 "
-                        "float32 field, 1e6 queries, forward + backward")
+                        "float32 field, 1e6 queries, forward + backward; traj = 1e6 particles, 100 RK4 steps "
+                        "through the 256^3 'both' field")
     p.add_argument("--profile", default=None,
                    choices=["step", "small", "small-table", "small-fp64", "small-coef", "small-4d", "small-batched",
                             "small-adjoint"],
@@ -229,6 +230,40 @@ def run_workload(args):
                                 "precision": "mixed"},
                      "paths": out,
                      "per_field_max_rel_err_vs_fp64": {"max": max(per_field), "median": float(np.median(per_field))}})
+    elif args.workload == "traj":
+        field = synth.dipole_field3(n=GRID, seed=1, device=dev)
+        g0 = torch.Generator(device=dev).manual_seed(13)
+        res = {}
+        for prec in ("mixed", "fp64"):
+            o = tricubic(field, "quiet", mode="both", precision=prec)
+            lo = torch.tensor([float(v) for v in o._lo], device=dev)
+            hi = torch.tensor([float(v) for v in o._hi], device=dev)
+            x0 = lo + (hi - lo) * (0.25 + 0.5 * torch.rand((1_000_000, 3), generator=g0, device=dev,
+                                                          dtype=torch.float64))
+            v0 = 1e-3 * torch.randn((1_000_000, 3), generator=g0, device=dev, dtype=torch.float64)
+            nsteps, dt = 100, 0.05
+
+            def run():
+                return o.trajectories(x0, v0, dt, nsteps, coef=-1e-4)
+            with ClockSampler(gpu_index) as clk:
+                t = cuda_time(run, max(1, args.steps // 5), 1)
+            xs, _ = run()
+            res[prec] = {"value": 1_000_000 * nsteps * max(1, args.steps // 5) / t, "unit": "particle-steps/s",
+                         "ms_per_step": 1000 * t / max(1, args.steps // 5), "lost": o.lost, "clocks": clk.summary(),
+                         "_x": xs}
+        m = torch.isfinite(res["fp64"]["_x"]).all(1) & torch.isfinite(res["mixed"]["_x"]).all(1)
+        dd = (res["mixed"]["_x"][m] - res["fp64"]["_x"][m]).abs().amax(1)
+        # trajectories near the dipoles are chaotic (steep |B|): report quantiles, not just the worst
+        dx = {q_: float(torch.quantile(dd.float(), q_)) for q_ in (0.5, 0.9, 0.99)}
+        dx["max"] = float(dd.max())
+        for v in res.values():
+            v.pop("_x")
+        line.update({"metric": "traj: RK4 particle-steps/s (4 field evaluations per step)",
+                     "value": res["mixed"]["value"], "unit": "particle-steps/s",
+                     "ms_per_step": res["mixed"]["ms_per_step"], "dtype": "f32",
+                     "config": {"workload": "1e6 particles x 100 RK4 steps in the 256^3 dipole |B| field "
+                                            "(x'' = -1e-4 grad|B|)", "precision": "mixed"},
+                     "paths": res, "position_diff_mixed_vs_fp64_quantiles": dx})
     else:  # c4
         from arbinterp_gb300.autograd import TricubicField
         # float32 samples; both precisions get the same (float64) geometry
