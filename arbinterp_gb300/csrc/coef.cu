@@ -219,6 +219,8 @@ static int coef_solve_f32_simt(const arb_grid *g, int64_t cell0, int64_t ncells,
 }
 
 namespace arb {
+int coef4_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *table, int32_t *status,
+                   cudaStream_t s);
 int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *table, int32_t *status,
                    cudaStream_t s);
 }
@@ -228,13 +230,14 @@ int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *tabl
 static int coef_solve_mixed(const arb_grid *g, int64_t cell0, int64_t ncells, float *table,
                             int32_t *status, cudaStream_t s) {
   if (g->dim == 3 && g->grid32) return arb::coef3_solve_tc(g, cell0, ncells, table, status, s);
+  if (g->dim == 4 && g->grid32) return arb::coef4_solve_tc(g, cell0, ncells, table, status, s);
   return coef_solve_f32_simt(g, cell0, ncells, table, s);
 }
 
 extern "C" int arb_coef_solve(const arb_grid *g, int32_t precision, int64_t cell0, int64_t ncells,
                               void *table, int32_t *status, arb_stream_t stream) {
   // the 3D mixed solve reads only the float32 split; every other solve the float64 grid
-  const bool tc3 = precision == ARB_PREC_MIXED && g && g->dim == 3 && g->grid32;
+  const bool tc3 = precision == ARB_PREC_MIXED && g && g->grid32;   // 3D and 4D tensor-core solves
   if (!g || !table || (!tc3 && !g->grid64)) return ARB_ERR_INVALID;
   if (cell0 < 0 || ncells < 0 || cell0 + ncells > g->nc) return ARB_ERR_INVALID;
   if (ncells == 0) return ARB_OK;

@@ -40,6 +40,7 @@
 #include <cuda_fp16.h>
 
 #include <mutex>
+#include <vector>
 
 #include "arb_common.cuh"
 #include "tc_ptx.cuh"
@@ -78,7 +79,7 @@ __constant__ float kA1[4][4] = {{0.f, 1.f, 0.f, 0.f},
                                 {-0.5f, 1.5f, -1.5f, 0.5f}};
 
 // byte offset of element (row, k) in the no-swizzle K-major layout
-__device__ __forceinline__ uint32_t kmaj(int row, int k, int sbo) {
+__host__ __device__ __forceinline__ uint32_t kmaj(int row, int k, int sbo) {
   return (uint32_t)((row >> 3) * sbo + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
@@ -369,6 +370,382 @@ int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *tabl
       case 1: coef3_tc_kernel<1><<<(unsigned)grid, NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
       case 3: coef3_tc_kernel<3><<<(unsigned)grid, NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
       default: coef3_tc_kernel<4><<<(unsigned)grid, NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
+    }
+    const int rc = launch_status();
+    if (rc != ARB_OK) return rc;
+  }
+  return ARB_OK;
+}
+
+
+// ============================================================================
+// 4D: the 256x256 product (calcCoefficients1/2/3 and allCoeffs of quadcubic,
+// src/ARBInterp/ARBInterp.py:1260-1262, 1322-1355), rows = (cell, field),
+// K = the 256 block samples, B = 16 A4 (integers, |.| <= 624, exact in FP16;
+// row absolute sums <= 20740).  The same exact split with bounds for that
+// matrix: t = 2^9 d / S = h0 + h1 + 2^-20 h2, h0 and h2 integers with
+// |h| <= 512, h1 a multiple of 2^-10 with |h1| <= 1/2; then every part's
+// 256-term sum stays below 2^24 of its own unit and accumulates exactly.
+// Three parts x 256 monomials would need 768 TMEM columns (an SM has 512),
+// so each 128-row tile runs the monomials in two halves of 128 (3 x 128
+// columns) from an A tile kept whole in shared memory (128 rows x 768 FP16 =
+// 192 KB); B arrives in 16 KB chunks (128 monomials x 64 samples, already in
+// the core-matrix layout) by single bulk copies, double-buffered, and the two
+// chunk buffers double as the 128-byte-swizzled staging of the output boxes
+// (128 rows x 32 coefficients) drained by TMA tensor stores.  One CTA of 256
+// threads per SM (shared memory and TMEM both allow one).
+namespace {
+constexpr int T4_M = 128, T4_NT = 256, T4_KP = 256, T4_KT = 768, T4_NH = 128, T4_KC = 64;
+constexpr int T4_A_SBO = (T4_KT / 8) * 128;       // 12288
+constexpr int T4_A_BYTES = (T4_M / 8) * T4_A_SBO;  // 196608
+constexpr int T4_B_SBO = (T4_KC / 8) * 128;        // 1024
+constexpr int T4_B_BYTES = (T4_NH / 8) * T4_B_SBO; // 16384
+constexpr int T4_TMEM = 512;
+constexpr float kRound10 = 12288.0f;                // 1.5 * 2^13: rounds to a multiple of 2^-10
+
+struct Tc4Smem {
+  unsigned char a[T4_A_BYTES];
+  unsigned char b[2][T4_B_BYTES];
+  float amax[2][T4_M];
+  uint64_t mbar_b[2];
+  uint64_t mbar_mma[2];
+  uint32_t tmem_base;
+  int32_t bad;
+};
+
+// t -> (h0, h1, h2) with t = h0 + h1 + 2^-20 h2
+__device__ __forceinline__ void split3_4d(float t, float &h0, float &h1, float &h2) {
+  h0 = __fadd_rn(__fadd_rn(t, kRound0), -kRound0);
+  const float r = __fadd_rn(t, -h0);
+  h1 = __fadd_rn(__fadd_rn(r, kRound10), -kRound10);
+  h2 = __fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(r, -h1), 1048576.0f), kRound0), -kRound0);
+}
+}  // namespace
+
+// B = 16 A4 as FP16 in 8 chunks [half][K-chunk] of the no-swizzle K-major
+// core-matrix layout (filled once per device from the host).
+static __device__ __align__(256) unsigned short g_b4[8 * T4_B_BYTES / 2];
+
+template <int F>
+__global__ void __launch_bounds__(T4_NT, 1) coef4_tc_kernel(const __grid_constant__ CUtensorMap tmap, arb_grid g,
+                                                            int64_t cell0, int64_t ncells, int32_t *status) {
+  extern __shared__ unsigned char smem_raw[];
+  Tc4Smem &sm = *reinterpret_cast<Tc4Smem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (T4_M - 1), half = tid >> 7;
+  const int64_t rows = ncells * F;
+  const int64_t npts = grid_points(g);
+  const int64_t ntiles = (rows + T4_M - 1) / T4_M;
+  const int64_t sy = g.n[0], sz = g.n[0] * g.n[1], st = g.n[0] * g.n[1] * g.n[2];
+  constexpr int PW = F == 1 ? 2 : 4;
+  const unsigned char *b4 = reinterpret_cast<const unsigned char *>(g_b4);
+
+  if (warp == 0) {
+    tc::tmem_alloc(&sm.tmem_base, T4_TMEM);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&sm.mbar_b[i], 1);
+      tc::mbar_init(&sm.mbar_mma[i], 1);
+    }
+    sm.bad = 0;
+    tc::fence_mbar_init();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+  const uint32_t idesc = tc::idesc_f16(0u, 128u, 128u);
+  const uint32_t a_base = tc::smem_u32(sm.a);
+  const uint32_t t_lane = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  uint32_t pb[2] = {0u, 0u}, pm[2] = {0u, 0u};  // phases (meaningful in thread 0)
+
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t r = tile * T4_M + row;
+    float rhi = 0.f, rlo = 0.f, amax = 0.f;
+    const float *hb = nullptr, *lb = nullptr;
+    bool has_lo = false;
+    if (r < rows) {
+      const int64_t cell = cell0 + r / F;
+      const int f = F == 1 ? 0 : (int)(r % F);
+      has_lo = F == 1 || (F == 4 && f == 3);
+      int64_t c[4];
+      cell_coords<4>(cell, g, c);
+      const int64_t p0 = ((c[3] * g.n[2] + c[2]) * g.n[1] + c[1]) * g.n[0] + c[0];
+      hb = g.grid32 + p0 * PW + f;
+      lb = g.grid32 + npts * 4 + p0;
+      const int64_t corner = st + sz + sy + 1;
+      float vl = 0.f;
+      g32_load<F>(g.grid32, npts, p0 + corner, f, rhi, vl);
+      rlo = vl;
+      // pass 1: the row's largest |delta| over this thread's 128 samples
+#pragma unroll 1
+      for (int ot = 0; ot < 2; ++ot)
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz)
+#pragma unroll
+          for (int oy = 0; oy < 4; ++oy) {
+            const int64_t line = (2 * half + ot) * st + oz * sz + oy * sy;
+#pragma unroll
+            for (int ox = 0; ox < 4; ++ox) {
+              float vh, vl2 = 0.f;
+              if (F == 1) {
+                const float2 v = __ldg(reinterpret_cast<const float2 *>(hb) + line + ox);
+                vh = v.x;
+                vl2 = v.y;
+              } else {
+                vh = __ldg(hb + (line + ox) * 4);
+                if (has_lo) vl2 = __ldg(lb + line + ox);
+              }
+              amax = fmaxf(amax, fabsf((vh - rhi) + (vl2 - rlo)));
+            }
+          }
+    }
+    sm.amax[half][row] = amax;
+    __syncthreads();
+    const int E = scale_exp(fmaxf(amax, sm.amax[half ^ 1][row]));
+    const float c9 = __uint_as_float((uint32_t)(127 + 9 - E) << 23);  // 2^(9 - E)
+    // pass 2: split into the A tile (8 consecutive samples = two x-lines per store)
+#pragma unroll 1
+    for (int ot = 0; ot < 2; ++ot)
+#pragma unroll
+      for (int oz = 0; oz < 4; ++oz)
+#pragma unroll
+        for (int oy = 0; oy < 4; oy += 2) {
+          float d[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) d[u] = 0.f;
+          if (r < rows) {
+#pragma unroll
+            for (int l2 = 0; l2 < 2; ++l2) {
+              const int64_t line = (2 * half + ot) * st + oz * sz + (oy + l2) * sy;
+#pragma unroll
+              for (int ox = 0; ox < 4; ++ox) {
+                float vh, vl2 = 0.f;
+                if (F == 1) {
+                  const float2 v = __ldg(reinterpret_cast<const float2 *>(hb) + line + ox);
+                  vh = v.x;
+                  vl2 = v.y;
+                } else {
+                  vh = __ldg(hb + (line + ox) * 4);
+                  if (has_lo) vl2 = __ldg(lb + line + ox);
+                }
+                d[l2 * 4 + ox] = (vh - rhi) + (vl2 - rlo);
+              }
+            }
+          }
+          uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            float a0, a1, a2, b0, b1, b2;
+            split3_4d(__fmul_rn(d[2 * v], c9), a0, a1, a2);
+            split3_4d(__fmul_rn(d[2 * v + 1], c9), b0, b1, b2);
+            w0[v] = pack_h2(a0, b0);
+            w1[v] = pack_h2(a1, b1);
+            w2[v] = pack_h2(a2, b2);
+          }
+          const int k = half * 128 + ot * 64 + oz * 16 + oy * 4;  // sample index ox + 4oy + 16oz + 64ot
+          *reinterpret_cast<uint4 *>(sm.a + kmaj(row, k, T4_A_SBO)) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+          *reinterpret_cast<uint4 *>(sm.a + kmaj(row, T4_KP + k, T4_A_SBO)) =
+              make_uint4(w1[0], w1[1], w1[2], w1[3]);
+          *reinterpret_cast<uint4 *>(sm.a + kmaj(row, 2 * T4_KP + k, T4_A_SBO)) =
+              make_uint4(w2[0], w2[1], w2[2], w2[3]);
+        }
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    if (tid == 0) tc::bulk_wait_read0();  // staging boxes of the previous tile have been read
+    __syncthreads();
+    const float so = __uint_as_float((uint32_t)(E - 13 + 127) << 23);  // 2^(E - 13)
+
+    for (int nh = 0; nh < 2; ++nh) {
+      // ---- MMAs for monomials [128 nh, 128 nh + 128): 4 K-chunks x 3 parts x 4 ----
+      if (tid == 0) {
+        tc::tc_fence_after();
+        bool ok = true;
+        for (int i = 0; i < 2; ++i) {
+          tc::mbar_arrive_expect_tx(&sm.mbar_b[i], T4_B_BYTES);
+          tc::bulk_load(sm.b[i], b4 + (size_t)(nh * 4 + i) * T4_B_BYTES, T4_B_BYTES, &sm.mbar_b[i]);
+        }
+        for (int kc = 0; kc < 4 && ok; ++kc) {
+          const int buf = kc & 1;
+          ok = tc::mbar_wait_bounded(&sm.mbar_b[buf], pb[buf], WAIT_LIMIT);
+          pb[buf] ^= 1u;
+          if (!ok) break;
+          const uint32_t b_base = tc::smem_u32(sm.b[buf]);
+#pragma unroll
+          for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const uint32_t ka = (uint32_t)(p * T4_KP + kc * T4_KC + ks * 16);
+              const uint64_t ad = tc::smem_desc(a_base + (ka / 8) * 128u, 128u, (uint32_t)T4_A_SBO);
+              const uint64_t bd = tc::smem_desc(b_base + (uint32_t)ks * 256u, 128u, (uint32_t)T4_B_SBO);
+              tc::mma_f16(tmem + (uint32_t)(p * T4_NH), ad, bd, idesc, (kc | ks) ? 1u : 0u);
+            }
+          tc::mma_commit(&sm.mbar_mma[buf]);
+          if (kc >= 1 && kc + 1 < 4) {
+            // the previous chunk's MMAs release its buffer for chunk kc + 1
+            const int pbuf = buf ^ 1;
+            ok = tc::mbar_wait_bounded(&sm.mbar_mma[pbuf], pm[pbuf], WAIT_LIMIT);
+            pm[pbuf] ^= 1u;
+            if (ok) {
+              tc::mbar_arrive_expect_tx(&sm.mbar_b[pbuf], T4_B_BYTES);
+              tc::bulk_load(sm.b[pbuf], b4 + (size_t)(nh * 4 + kc + 1) * T4_B_BYTES, T4_B_BYTES, &sm.mbar_b[pbuf]);
+            }
+          }
+        }
+        // chunks 2 and 3 (buffers 0 and 1) are the last commits outstanding
+        for (int i = 0; i < 2 && ok; ++i) {
+          ok = tc::mbar_wait_bounded(&sm.mbar_mma[i], pm[i], WAIT_LIMIT);
+          pm[i] ^= 1u;
+        }
+        if (!ok) {
+          set_status(status, ARB_ERR_TIMEOUT);
+          sm.bad = 1;
+        }
+      }
+      tc::tc_fence_before();
+      __syncthreads();
+      tc::tc_fence_after();
+      if (sm.bad) break;
+      // ---- epilogue: thread (row, q) combines monomials 64 q .. 64 q + 63 of this half ----
+      const int q = half;
+#pragma unroll 1
+      for (int sub = 0; sub < 2; ++sub) {
+        const uint32_t col = (uint32_t)(q * 64 + sub * 32);
+        float a[32], t[32];
+        tc::tmem_ld16(t_lane + 2u * T4_NH + col, t);
+        tc::tmem_ld16(t_lane + 2u * T4_NH + col + 16u, t + 16);
+        tc::tmem_ld16(t_lane + T4_NH + col, a);
+        tc::tmem_ld16(t_lane + T4_NH + col + 16u, a + 16);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) t[j] = __fmaf_rn(t[j], 0x1p-20f, a[j]);
+        tc::tmem_ld16(t_lane + col, a);
+        tc::tmem_ld16(t_lane + col + 16u, a + 16);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) a[j] = __fmul_rn(__fadd_rn(a[j], t[j]), so);
+        if (nh == 0 && q == 0 && sub == 0) a[0] = rhi + (rlo + a[0]);
+        if (tid == 0) tc::bulk_wait_read0();  // the staging box is free again
+        __syncthreads();
+        unsigned char *st_row = sm.b[q] + row * 128;
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          *reinterpret_cast<float4 *>(st_row + 16 * (c ^ (row & 7))) =
+              make_float4(a[4 * c], a[4 * c + 1], a[4 * c + 2], a[4 * c + 3]);
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+          tc::tma_store_2d(&tmap, sm.b[0], nh * 128 + 0 * 64 + sub * 32, (int32_t)(tile * T4_M));
+          tc::tma_store_2d(&tmap, sm.b[1], nh * 128 + 1 * 64 + sub * 32, (int32_t)(tile * T4_M));
+          tc::bulk_commit();
+        }
+      }
+      // the next half's chunk copies land in the staging buffers: wait for the reads
+      tc::tc_fence_before();
+      if (tid == 0) tc::bulk_wait_read0();
+      __syncthreads();
+    }
+    if (sm.bad) break;
+  }
+  if (tid == 0) {
+    tc::bulk_wait0();
+    if (sm.bad) {
+      // after a timed-out wait: one more bounded wait for work still in flight
+      for (int i = 0; i < 2; ++i) {
+        (void)tc::mbar_wait_bounded(&sm.mbar_mma[i], pm[i], WAIT_LIMIT);
+        (void)tc::mbar_wait_bounded(&sm.mbar_b[i], pb[i], WAIT_LIMIT);
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  if (warp == 0) tc::tmem_dealloc(tmem, T4_TMEM);
+}
+
+// 16 A4 (the reference's 4D A scaled by 16: integers) in the chunked FP16 layout.
+static void build_b4_host(std::vector<__half> &out) {
+  static const double A1h[4][4] = {{0, 1, 0, 0}, {-0.5, 0, 0.5, 0}, {1, -2.5, 2, -0.5}, {-0.5, 1.5, -1.5, 0.5}};
+  static const double HB[2][4] = {{0, 1, -2, 1}, {0, 0, -1, 1}};  // t - 2t^2 + t^3, -t^2 + t^3
+  auto h_c = [&](int c, int n) {  // slope-Hermite tensor coefficient of monomial n for corner c (h_16 = 0)
+    if (c >= 16) return 0.0;
+    double v = 1.0;
+    for (int a = 0; a < 4; ++a) v *= HB[(c >> a) & 1][(n >> (2 * a)) & 3];
+    return v;
+  };
+  auto s_c = [&](int c, int k) {  // mixed fourth-difference stencil of corner c at block sample k
+    double v = 1.0;
+    for (int a = 0; a < 4; ++a) {
+      const int b = (c >> a) & 1, o = (k >> (2 * a)) & 3;
+      v *= o == b ? -0.5 : (o == b + 2 ? 0.5 : 0.0);
+    }
+    return v;
+  };
+  out.assign(8 * T4_B_BYTES / 2, __float2half(0.f));
+  for (int n = 0; n < 256; ++n)
+    for (int k = 0; k < 256; ++k) {
+      double v = 1.0;
+      for (int a = 0; a < 4; ++a) v *= A1h[(n >> (2 * a)) & 3][(k >> (2 * a)) & 3];
+      for (int c = 0; c < 16; ++c) v += (h_c(c + 1, n) - h_c(c, n)) * s_c(c, k);
+      const int nh = n >> 7, nl = n & 127, kc = k >> 6, kl = k & 63;
+      const size_t off = (size_t)(nh * 4 + kc) * T4_B_BYTES + kmaj(nl, kl, T4_B_SBO);
+      out[off / 2] = __float2half((float)(16.0 * v));
+    }
+}
+
+int coef4_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *table, int32_t *status,
+                   cudaStream_t s) {
+  if (!g->grid32 || ((uintptr_t)table & 15u)) return ARB_ERR_INVALID;
+  const EncodeTiled encode = encode_fn();
+  if (!encode) return ARB_ERR_CUDA;
+  const size_t smem = sizeof(Tc4Smem) + 1024;
+  static_assert(sizeof(Tc4Smem) + 1024 <= 232448, "shared memory above the per-CTA limit");
+  static std::mutex mu;
+  static bool filled[64] = {};
+  static bool attr = false;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ARB_ERR_CUDA;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!filled[dev]) {
+      std::vector<__half> host;
+      build_b4_host(host);
+      if (cudaMemcpyToSymbol(g_b4, host.data(), host.size() * sizeof(__half)) != cudaSuccess) return ARB_ERR_CUDA;
+      filled[dev] = true;
+    }
+    if (!attr) {
+      const void *ks[3] = {(const void *)coef4_tc_kernel<1>, (const void *)coef4_tc_kernel<3>,
+                           (const void *)coef4_tc_kernel<4>};
+      for (const void *k : ks)
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+          return ARB_ERR_CUDA;
+      attr = true;
+    }
+  }
+  const int F = g->nfield;
+  if (F != 1 && F != 3 && F != 4) return ARB_ERR_INVALID;
+  const int64_t max_cells = ((int64_t)1 << 31) / F;
+  for (int64_t done = 0; done < ncells; done += max_cells) {
+    const int64_t nc = ncells - done < max_cells ? ncells - done : max_cells;
+    const int64_t rows = nc * F;
+    CUtensorMap tmap;
+    const cuuint64_t dims[2] = {256, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {256 * sizeof(float)};
+    const cuuint32_t box[2] = {32, T4_M};
+    const cuuint32_t estr[2] = {1, 1};
+    if (encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, table + done * F * 256, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return ARB_ERR_CUDA;
+    const int64_t tiles = (rows + T4_M - 1) / T4_M;
+    int64_t grid = num_sms();
+    if (grid > tiles) grid = tiles;
+    switch (F) {
+      case 1: coef4_tc_kernel<1><<<(unsigned)grid, T4_NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
+      case 3: coef4_tc_kernel<3><<<(unsigned)grid, T4_NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
+      default: coef4_tc_kernel<4><<<(unsigned)grid, T4_NT, smem, s>>>(tmap, *g, cell0 + done, nc, status); break;
     }
     const int rc = launch_status();
     if (rc != ARB_OK) return rc;

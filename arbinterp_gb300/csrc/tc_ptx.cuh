@@ -37,6 +37,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *m, uint32_t parity, 
   return false;
 }
 
+// One arrival that also expects `bytes` of asynchronous transaction data.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *m, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes)
+               : "memory");
+}
+
+// Contiguous global -> shared bulk copy completing on an mbarrier
+// (addresses 16-byte aligned, size a multiple of 16).
+__device__ __forceinline__ void bulk_load(void *sdst, const void *gsrc, uint32_t bytes, uint64_t *m) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(sdst)),
+               "l"(gsrc), "r"(bytes), "r"(smem_u32(m))
+               : "memory");
+}
+
 // ---- proxy / tcgen05 ordering fences ----------------------------------------
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

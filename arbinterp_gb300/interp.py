@@ -347,7 +347,7 @@ class _Interpolant:
 
     def _solve(self, cell0, ncells):
         self._ensure_table()
-        if not (self.precision == "mixed" and self._dim == 3):
+        if self.precision != "mixed":
             self._grid64                      # the float64 grid (materialised if needed)
         L = lib()
         rc = L.arb_coef_solve(self._g, self._table_prec, cell0, ncells,

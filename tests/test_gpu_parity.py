@@ -330,6 +330,41 @@ def test_tensor_core_table_exact_from_deltas(mode):
         assert (err <= bound).all(), (key, (err / np.maximum(bound, 1e-300)).max())
 
 
+@pytest.mark.parametrize("mode", [None, "both"])
+def test_tensor_core_table_exact_from_deltas_4d(mode):
+    """4D tensor-core solve: every float32 coefficient equals alpha = A4 d
+    computed exactly from the kernel's float32 deltas, up to its own float32
+    rounding, the rounding of its three-part recombination, and the
+    fixed-point truncation of d (2^-30 of the row's power-of-two scale,
+    times the largest row abs-sum 1296.25 of A4)."""
+    _, quadcubic = _mods()
+    from arbinterp_gb300 import synth
+    from oracle.arb_oracle import OracleQuadcubic
+    f = synth.moving_gaussian_field4(n=(9, 8, 8, 7), h=(0.1, 0.12, 0.08, 0.1), seed=5).numpy()
+    if mode == "both":
+        f = np.hstack([f[:, :4], f[:, 4:5], np.sin(f[:, 4:5] + f[:, :1]), f[:, 4:5] * f[:, 1:2] + 0.5])
+    kw = {} if mode is None else {"mode": mode}
+    omx = quadcubic(f, "quiet", precision="mixed", **kw)
+    omx.allCoeffs()
+    o = OracleQuadcubic(f, **kw)
+    blocks = o.basePointInds[:, None] + o.block_offsets[None, :]
+    corner = 1 + 4 + 16 + 64
+    for key in o.fields:
+        v = o.fields[key]
+        hi = v.astype(np.float32)
+        lo = (v - hi).astype(np.float32) if key == "n" else np.zeros_like(hi)
+        rhi, rlo = hi[blocks[:, corner]], lo[blocks[:, corner]]
+        d = (hi[blocks] - rhi[:, None]) + (lo[blocks] - rlo[:, None])
+        want = d.astype(np.float64) @ o.A.T
+        want[:, 0] = (rhi + (rlo + np.float32(0))).astype(np.float64)
+        got = getattr(omx, "alpha" + key)[:, :o.nc].T.astype(np.float64)
+        amax = np.abs(d).max(axis=1).astype(np.float64)
+        scale = 2.0 ** np.ceil(np.log2(np.maximum(amax, 1e-300)) + 1e-12)
+        bound = 2.0 ** -23 * np.abs(want) + (2.0 ** -23 + 1296.25 * 2.0 ** -30) * 2 * scale[:, None]
+        err = np.abs(got - want)
+        assert (err <= bound).all(), (key, (err / np.maximum(bound, 1e-300)).max())
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_bin_once_evaluate_twice(prec):
     """arb_query_bin + arb_query_eval_binned equal the one-call sorted path,
