@@ -77,6 +77,11 @@ SIGNATURES = {
                                                 C.POINTER(ArbQueryOut), _P, _P]),
     "arb_rk4_trajectories": (C.c_int, [C.POINTER(ArbGrid), _I32, _P, _I64, C.c_double, _I64, C.c_double,
                                        C.POINTER(C.c_double), _P, _I64, _P, _P]),
+    "arb_csv_count_work_bytes": (C.c_size_t, [_I64]),
+    "arb_csv_count": (C.c_int, [_P, _I64, _P, C.c_size_t, _P, _P]),
+    "arb_csv_lines_work_bytes": (C.c_size_t, [_I64]),
+    "arb_csv_split": (C.c_int, [_P, _I64, _I64, _I32, _I32, _I64, _P, _P, C.c_size_t, _P, _P, _P]),
+    "arb_csv_parse": (C.c_int, [_P, _I64, _I64, _I32, _I32, _P, C.c_size_t, _P, _P, _I64, _I64, _P, _P]),
     "arb_status_fetch": (C.c_int, [_P, _P]),
     "arb_version": (C.c_char_p, []),
 }

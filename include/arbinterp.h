@@ -297,6 +297,49 @@ int arb_rk4_trajectories(const arb_grid *g, int32_t precision, double *state, in
                          int64_t nsteps, double coef, const double *gravity, double *path,
                          int64_t record_every, unsigned long long *lost, arb_stream_t stream);
 
+/* ---- field files: np.genfromtxt(path, delimiter=',') on the device
+ *      (examples/3D_ARBInterpExample.py:14,37 and
+ *      examples/4D_ARBInterpExample.py:14,38 load the N x 4..7 field tables
+ *      this way; README.md:64-72).  ASCII text, universal newlines, a
+ *      one-character delimiter and comment character, skip_header; every
+ *      token converted as Python's float() does (correctly rounded; an
+ *      empty or malformed token reads as NaN).  Three phases, each followed
+ *      by a read of the device-side arb_csv_info:
+ *        1. arb_csv_count  -> nlines (lines counted in byte chunks),
+ *                             first_nonascii;
+ *        2. arb_csv_split  -> line starts, values per line (nvals, the
+ *                             caller's int32[nlines]; 0 = skipped line),
+ *                             first_data_line, ncols, nrows, ninvalid;
+ *        3. arb_csv_parse  -> out[nrows][ncols] float64 (lines whose value
+ *                             count differs from ncols are not written).
+ *      text must be 16-byte aligned; delimiter in 1..127 (not CR/LF);
+ *      comment -1 (none) or 1..127 and != delimiter. ------------------- */
+typedef struct arb_csv_info {
+  int64_t nlines;          /* physical lines                                   */
+  int64_t first_nonascii;  /* offset of the first byte >= 0x80, or -1          */
+  int64_t first_data_line; /* first line with values (0-based), or -1          */
+  int64_t ncols;           /* values on that line                              */
+  int64_t nrows;           /* lines with exactly ncols values                  */
+  int64_t ninvalid;        /* lines with values, but not ncols of them         */
+  int64_t nexact;          /* tokens settled by the exact big-integer pass     */
+  int64_t nqueued;         /* lines queued for that pass                       */
+  int32_t error;           /* ARB_ERR_CAPACITY if a big integer overflowed     */
+  int32_t reserved;
+} arb_csv_info;
+
+size_t arb_csv_count_work_bytes(int64_t nbytes);
+int arb_csv_count(const uint8_t *text, int64_t nbytes, void *work, size_t work_bytes, arb_csv_info *info,
+                  arb_stream_t stream);
+/* lines_work: arb_csv_lines_work_bytes(nlines) bytes, 256-byte aligned;
+ * count_work is phase 1's work buffer (per-chunk line offsets). */
+size_t arb_csv_lines_work_bytes(int64_t nlines);
+int arb_csv_split(const uint8_t *text, int64_t nbytes, int64_t nlines, int32_t delimiter, int32_t comment,
+                  int64_t skip_header, const void *count_work, void *lines_work, size_t lines_work_bytes,
+                  int32_t *nvals, arb_csv_info *info, arb_stream_t stream);
+int arb_csv_parse(const uint8_t *text, int64_t nbytes, int64_t nlines, int32_t delimiter, int32_t comment,
+                  void *lines_work, size_t lines_work_bytes, const int32_t *nvals, double *out, int64_t nrows,
+                  int64_t ncols, arb_csv_info *info, arb_stream_t stream);
+
 /* Reads (and clears) the device status word after the stream's work is
  * done; returns ARB_OK, an arb_status bit set, or ARB_ERR_CUDA. */
 int arb_status_fetch(int32_t *status, arb_stream_t stream);
