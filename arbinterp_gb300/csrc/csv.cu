@@ -57,6 +57,53 @@ __device__ __forceinline__ bool is_ws(unsigned c) { return c == 32u || (c - 9u) 
 __device__ __forceinline__ bool is_digit(unsigned c) { return (c - 48u) < 10u; }
 __device__ __forceinline__ bool is_eol(unsigned c) { return c == 10u || c == 13u; }
 
+// ---- eight bytes at a time (SWAR on 64-bit words, byte 0 = lowest address) ------
+constexpr uint64_t ONES = 0x0101010101010101ull, HIGHS = 0x8080808080808080ull;
+
+// 0x80 in every byte of x equal to c, 0 elsewhere (exact: no carries between bytes)
+__device__ __forceinline__ uint64_t eq8(uint64_t x, unsigned c) {
+  const uint64_t y = x ^ (ONES * (uint64_t)c);
+  return ~(((y & 0x7f7f7f7f7f7f7f7full) + 0x7f7f7f7f7f7f7f7full) | y) & HIGHS;
+}
+__device__ __forceinline__ bool all_digits8(uint64_t x) {
+  return ((x & 0xf0f0f0f0f0f0f0f0ull) == 0x3030303030303030ull) &&
+         (((x + 0x0606060606060606ull) & 0xf0f0f0f0f0f0f0f0ull) == 0x3030303030303030ull);
+}
+// Value of 8 ASCII digits (first byte most significant): pairs, then quads,
+// then the octet, each step a multiply-add of adjacent lanes.
+__device__ __forceinline__ uint32_t digits8(uint64_t x) {
+  x -= 0x3030303030303030ull;
+  x = (x * 10u + (x >> 8)) & 0x00ff00ff00ff00ffull;
+  x = (x * 100u + (x >> 16)) & 0x0000ffff0000ffffull;
+  return (uint32_t)((x * 10000u + (x >> 32)) & 0xffffffffull);
+}
+// bytes 0..k-1 of a word (k in 0..8)
+__device__ __forceinline__ uint64_t below(int k) { return k >= 8 ? ~0ull : ((1ull << (8 * k)) - 1); }
+
+// Text byte x at p[x - off]: staged in shared memory (STAGED; the stage is
+// padded so an 8-byte read never leaves it) or read from global memory.
+template <bool STAGED>
+struct Src {
+  const uint8_t *p;
+  int64_t off;
+  __device__ __forceinline__ unsigned at(int64_t x) const { return p[x - off]; }
+  // bytes x .. x+7; callers keep x + 8 within the text
+  __device__ __forceinline__ uint64_t load8(int64_t x) const {
+    if constexpr (STAGED) {
+      const int64_t r = x - off;
+      const uint64_t *w = reinterpret_cast<const uint64_t *>(p + (r & ~(int64_t)7));
+      const int sh = (int)(r & 7) * 8;
+      const uint64_t lo = w[0];
+      return sh ? (lo >> sh) | (w[1] << (64 - sh)) : lo;
+    } else {
+      uint64_t v = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v |= (uint64_t)p[x - off + k] << (8 * k);
+      return v;
+    }
+  }
+};
+
 // ---- token grammar (Python float) --------------------------------------------
 struct Dec {
   uint64_t w;    // first 19 significant digits
@@ -65,31 +112,33 @@ struct Dec {
   uint8_t neg, trunc, kind;  // kind: 0 number, 1 inf, 2 nan, 3 invalid or empty
 };
 
-__device__ __forceinline__ bool word_is(const uint8_t *s, int64_t i, int64_t len, const char *w, int n) {
+template <bool ST>
+__device__ __forceinline__ bool word_is(const Src<ST> &s, int64_t i, int64_t len, const char *w, int n) {
   if (len != n) return false;
   for (int k = 0; k < n; ++k)
-    if ((unsigned)(s[i + k] | 0x20) != (unsigned)w[k]) return false;
+    if ((s.at(i + k) | 0x20u) != (unsigned)w[k]) return false;
   return true;
 }
 
 // Exponent part at s[i] (just past 'e'/'E'); returns the position after it,
 // or -1 if malformed.  e saturates at 1e9.
-__device__ __forceinline__ int64_t parse_exp(const uint8_t *s, int64_t i, int64_t j, int64_t &e) {
+template <bool ST>
+__device__ __forceinline__ int64_t parse_exp(const Src<ST> &s, int64_t i, int64_t j, int64_t &e) {
   bool eneg = false;
-  if (i < j && (s[i] == '+' || s[i] == '-')) {
-    eneg = s[i] == '-';
+  if (i < j && (s.at(i) == '+' || s.at(i) == '-')) {
+    eneg = s.at(i) == '-';
     ++i;
   }
   int64_t v = 0;
   int nd = 0;
   for (; i < j; ++i) {
-    const unsigned c = s[i];
+    const unsigned c = s.at(i);
     if (is_digit(c)) {
       v = v * 10 + (c - 48u);
       if (v > 1000000000) v = 1000000000;
       ++nd;
     } else if (c == '_') {
-      if (!(is_digit(s[i - 1]) && i + 1 < j && is_digit(s[i + 1]))) return -1;
+      if (!(is_digit(s.at(i - 1)) && i + 1 < j && is_digit(s.at(i + 1)))) return -1;
     } else {
       break;
     }
@@ -99,17 +148,18 @@ __device__ __forceinline__ int64_t parse_exp(const uint8_t *s, int64_t i, int64_
   return i;
 }
 
-__device__ Dec parse_token(const uint8_t *s, int64_t i, int64_t j) {
+template <bool ST>
+__device__ Dec parse_token(const Src<ST> &s, int64_t i, int64_t j) {
   Dec r{0, 0, 0, 0, 0, 3};
-  while (i < j && is_ws(s[i])) ++i;
-  while (j > i && is_ws(s[j - 1])) --j;
+  while (i < j && is_ws(s.at(i))) ++i;
+  while (j > i && is_ws(s.at(j - 1))) --j;
   if (i == j) return r;
   const int64_t i0 = i;
-  if (s[i] == '+' || s[i] == '-') {
-    r.neg = s[i] == '-';
+  if (s.at(i) == '+' || s.at(i) == '-') {
+    r.neg = s.at(i) == '-';
     ++i;
   }
-  if (i < j && ((s[i] | 0x20) == 'i' || (s[i] | 0x20) == 'n')) {
+  if (i < j && ((s.at(i) | 0x20u) == 'i' || (s.at(i) | 0x20u) == 'n')) {
     if (word_is(s, i, j - i, "inf", 3) || word_is(s, i, j - i, "infinity", 8)) r.kind = 1;
     else if (word_is(s, i, j - i, "nan", 3)) r.kind = 2;
     return r;
@@ -118,8 +168,28 @@ __device__ Dec parse_token(const uint8_t *s, int64_t i, int64_t j) {
   int nd = 0;
   int64_t q = 0, ndig = 0;
   bool seen = false, point = false, trunc = false;
-  for (; i < j; ++i) {
-    const unsigned c = s[i];
+  while (i < j) {
+    if (nd <= 11 && i + 8 <= j) {  // eight digits at once while w * 10^8 + v stays below 10^19
+      const uint64_t x = s.load8(i);
+      if (all_digits8(x)) {
+        const uint32_t v = digits8(x);
+        if (seen || v) {
+          int sig = 8;
+          if (!seen) {
+            const uint64_t nz = ~eq8(x, '0') & HIGHS;  // nonzero digits
+            sig = 8 - ((__ffsll((long long)nz) - 1) >> 3);
+            seen = true;
+          }
+          w = w * 100000000ull + v;
+          nd += sig;
+        }
+        q -= point ? 8 : 0;
+        ndig += 8;
+        i += 8;
+        continue;
+      }
+    }
+    const unsigned c = s.at(i);
     if (is_digit(c)) {
       const unsigned d = c - 48u;
       ++ndig;
@@ -137,16 +207,17 @@ __device__ Dec parse_token(const uint8_t *s, int64_t i, int64_t j) {
         q -= point;
       }
     } else if (c == '_') {
-      if (!(i > i0 && is_digit(s[i - 1]) && i + 1 < j && is_digit(s[i + 1]))) return r;
+      if (!(i > i0 && is_digit(s.at(i - 1)) && i + 1 < j && is_digit(s.at(i + 1)))) return r;
     } else if (c == '.') {
       if (point) return r;
       point = true;
     } else {
       break;
     }
+    ++i;
   }
   if (ndig == 0) return r;
-  if (i < j && (s[i] | 0x20) == 'e') {
+  if (i < j && (s.at(i) | 0x20u) == 'e') {
     int64_t e = 0;
     i = parse_exp(s, i + 1, j, e);
     if (i < 0) return r;
@@ -166,7 +237,7 @@ __device__ Dec parse_token(const uint8_t *s, int64_t i, int64_t j) {
 // the rounding of an exact integer, magnitude only.  carry: X overflowed
 // 192 bits (never for the table's T, reported as undecided).
 __device__ __forceinline__ uint64_t round_prod(uint64_t W, bool addW, uint64_t thi, uint64_t tlo, int b,
-                                               bool &carry) {
+                                               bool &carry, bool *same_plus_w = nullptr) {
   const int lz = __clzll((long long)W);
   const uint64_t Wn = W << lz;
   uint64_t x0 = Wn * tlo;
@@ -194,6 +265,10 @@ __device__ __forceinline__ uint64_t round_prod(uint64_t W, bool addW, uint64_t t
   uint64_t m = sh >= 64 ? 0 : (x2 >> sh);
   const uint64_t r = (x2 >> rs) & 1u;
   const uint64_t s = ((x2 & ((1ull << rs) - 1)) | x1 | x0) != 0;
+  // X + (W << lz) rounds the same way when the addition cannot carry into
+  // the top word (the round bit and mantissa live there) and X is already
+  // inexact below the round bit
+  if (same_plus_w) *same_plus_w = x1 != ~0ull && s;
   m += r & (s | (m & 1u));
   const uint64_t bits = ((uint64_t)(c + ebias + 1074) << 52) + m;
   return bits > INF_BITS ? INF_BITS : bits;
@@ -215,9 +290,10 @@ __device__ __forceinline__ uint64_t fast_convert(const Dec &d, bool &decided) {
   const uint64_t thi = kPow10T[k][0], tlo = kPow10T[k][1];
   const int b = kPow10B[k];
   const bool exact = d.q >= 0 && d.q <= 55;
-  bool cy;
-  const uint64_t lo = round_prod(d.w, false, thi, tlo, b, cy);
+  bool cy, same = false;
+  const uint64_t lo = round_prod(d.w, false, thi, tlo, b, cy, &same);
   if (exact && !d.trunc) return lo;
+  if (!d.trunc && same) return lo;  // the upper bound (W << lz) * (T + 1) rounds alike
   const uint64_t hi = round_prod(d.trunc ? d.w + 1 : d.w, !exact, thi, tlo, b, cy);
   if (cy || hi != lo) decided = false;
   return lo;
@@ -295,11 +371,11 @@ __device__ int big_cmp(const Big &a, const Big &b) {
 
 // Correctly rounded magnitude of the (valid, finite-number) token s[i, j),
 // starting from cand, a double no larger than the answer.
-__device__ uint64_t exact_convert(const uint8_t *s, int64_t i, int64_t j, uint64_t cand, uint32_t *scratch,
+__device__ uint64_t exact_convert(const Src<false> &s, int64_t i, int64_t j, uint64_t cand, uint32_t *scratch,
                                   int32_t *err) {
-  while (i < j && is_ws(s[i])) ++i;
-  while (j > i && is_ws(s[j - 1])) --j;
-  if (i < j && (s[i] == '+' || s[i] == '-')) ++i;
+  while (i < j && is_ws(s.at(i))) ++i;
+  while (j > i && is_ws(s.at(j - 1))) --j;
+  if (i < j && (s.at(i) == '+' || s.at(i) == '-')) ++i;
   Big D{scratch, 0};
   int nd = 0, chunk_n = 0;
   uint32_t chunk = 0;
@@ -307,7 +383,7 @@ __device__ uint64_t exact_convert(const uint8_t *s, int64_t i, int64_t j, uint64
   bool sticky = false, seen = false, point = false, ok = true;
   const uint32_t p10[10] = {1u, 10u, 100u, 1000u, 10000u, 100000u, 1000000u, 10000000u, 100000000u, 1000000000u};
   for (; i < j; ++i) {
-    const unsigned c = s[i];
+    const unsigned c = s.at(i);
     if ((c | 0x20) == 'e') break;
     if (is_digit(c)) {
       const unsigned d = c - 48u;
@@ -365,29 +441,51 @@ __device__ uint64_t exact_convert(const uint8_t *s, int64_t i, int64_t j, uint64
 }
 
 // ---- line walking --------------------------------------------------------------
-// Content of the line starting at p (bytes via s[x - off]), limited to lim:
-// [a, b) after the comment cut and the strip of spaces; nvals values.
+// Content of the line starting at p, limited to lim: [a, b) after the
+// comment cut and the strip of spaces; nvals values (0: nothing left).
 struct LineSpan {
   int64_t a, b;
   int32_t nvals;
 };
 
-__device__ __forceinline__ LineSpan line_span(const uint8_t *s, int64_t off, int64_t p, int64_t lim, int delim,
-                                              int comment) {
+template <bool ST>
+__device__ __forceinline__ LineSpan line_span(const Src<ST> &s, int64_t p, int64_t lim, int delim, int comment) {
   int64_t first = -1, last = -1;
   int32_t nd_all = 0, nd_first = 0, nd_last = 0;
-  for (; p < lim; ++p) {
-    const unsigned c = s[p - off];
-    if (is_eol(c) || (int)c == comment) break;
-    const bool isd = (int)c == delim;
-    nd_all += isd;
-    if (c != 32u) {
-      if (first < 0) {
-        first = p;
-        nd_first = nd_all - isd;
+  while (p < lim) {
+    if (p + 8 <= lim) {
+      const uint64_t x = s.load8(p);
+      uint64_t end = eq8(x, 10u) | eq8(x, 13u);
+      if (comment >= 0) end |= eq8(x, (unsigned)comment);
+      const uint64_t valid = end ? below((__ffsll((long long)end) - 1) >> 3) : ~0ull;
+      const uint64_t del = eq8(x, (unsigned)delim) & valid;
+      const uint64_t ns = ~eq8(x, 32u) & HIGHS & valid;
+      if (ns) {
+        const int fb = (__ffsll((long long)ns) - 1) >> 3, lb = (63 - __clzll((long long)ns)) >> 3;
+        if (first < 0) {
+          first = p + fb;
+          nd_first = nd_all + __popcll(del & below(fb));
+        }
+        last = p + lb;
+        nd_last = nd_all + __popcll(del & below(lb + 1));
       }
-      last = p;
-      nd_last = nd_all;
+      nd_all += __popcll(del);
+      if (end) break;
+      p += 8;
+    } else {
+      const unsigned c = s.at(p);
+      if (is_eol(c) || (int)c == comment) break;
+      const bool isd = (int)c == delim;
+      nd_all += isd;
+      if (c != 32u) {
+        if (first < 0) {
+          first = p;
+          nd_first = nd_all - isd;
+        }
+        last = p;
+        nd_last = nd_all;
+      }
+      ++p;
     }
   }
   LineSpan r;
@@ -397,16 +495,30 @@ __device__ __forceinline__ LineSpan line_span(const uint8_t *s, int64_t off, int
   return r;
 }
 
-// Bytes [a, b) of the text for the CTA's lines, staged into shared memory
-// when they fit; returns the (pointer, offset) pair to read text byte x at
-// ptr[x - off].
-__device__ __forceinline__ const uint8_t *stage_bytes(const uint8_t *t, int64_t n, int64_t a, int64_t b,
-                                                     uint8_t *sm, int64_t &off) {
-  const int64_t a16 = a & ~(int64_t)15;
-  if (b - a16 > STAGE_BYTES) {
-    off = 0;
-    return t;
+// Next delimiter at or after ts before b (b if none).
+template <bool ST>
+__device__ __forceinline__ int64_t next_delim(const Src<ST> &s, int64_t ts, int64_t b, int delim) {
+  while (ts < b) {
+    if (ts + 8 <= b) {
+      const uint64_t m = eq8(s.load8(ts), (unsigned)delim);
+      if (m) return ts + ((__ffsll((long long)m) - 1) >> 3);
+      ts += 8;
+    } else {
+      if ((int)s.at(ts) == delim) return ts;
+      ++ts;
+    }
   }
+  return b;
+}
+
+// Bytes [a, b) of the text for the CTA's lines, staged into shared memory
+// (16 bytes of padding past the stage) when they fit; returns whether they did
+// and sets off so that text byte x is at sm[x - off].
+__device__ __forceinline__ bool stage_bytes(const uint8_t *t, int64_t n, int64_t a, int64_t b, uint8_t *sm,
+                                            int64_t &off) {
+  const int64_t a16 = a & ~(int64_t)15;
+  off = a16;
+  if (b - a16 > STAGE_BYTES) return false;
   const int64_t nvec = (b - a16 + 15) >> 4;
   for (int64_t k = threadIdx.x; k < nvec; k += blockDim.x) {
     const int64_t p = a16 + 16 * k;
@@ -416,8 +528,7 @@ __device__ __forceinline__ const uint8_t *stage_bytes(const uint8_t *t, int64_t 
       for (int e = 0; e < 16; ++e) sm[16 * k + e] = p + e < n ? t[p + e] : (uint8_t)0;
     }
   }
-  off = a16;
-  return sm;
+  return true;
 }
 
 // ---- kernels -------------------------------------------------------------------
@@ -435,33 +546,34 @@ __global__ void init_kernel(arb_csv_info *info) {
 }
 
 // Terminators ('\n', or '\r' not followed by '\n') in t[p0, p1) in order;
-// records the first byte >= 0x80.
+// records the first byte >= 0x80.  p0 is a multiple of 16.
+// One 8-byte word at text position p of a chunk: its terminators in order.
+// next_lf: the byte after the word is '\n'.
+template <class F>
+__device__ __forceinline__ void word_terms(uint64_t x, int64_t p, bool next_lf, int64_t &nonascii, F &f) {
+  if ((x & HIGHS) && nonascii == NONE) nonascii = p + ((__ffsll((long long)(x & HIGHS)) - 1) >> 3);
+  const uint64_t lf = eq8(x, 10u);
+  uint64_t term = lf;
+  const uint64_t cr = eq8(x, 13u);
+  if (cr) term |= cr & ~((lf >> 8) | (next_lf ? (0x80ull << 56) : 0ull));  // CR not followed by LF
+  while (term) {
+    f(p + ((__ffsll((long long)term) - 1) >> 3));
+    term &= term - 1;
+  }
+}
+
+// Terminators ('\n', or '\r' not followed by '\n') in t[p0, p1) in order;
+// records the first byte >= 0x80.  p0 is a multiple of 16.
 template <class F>
 __device__ __forceinline__ void for_each_term(const uint8_t *t, int64_t n, int64_t p0, int64_t p1, int64_t &nonascii,
                                               F &&f) {
   for (int64_t p = p0; p < p1; p += 16) {
     if (p + 16 <= n) {
       const uint4 v = __ldg(reinterpret_cast<const uint4 *>(t + p));
-      const uint32_t wv[4] = {v.x, v.y, v.z, v.w};
-      uint32_t hit = 0, hi = 0;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        hit |= __vcmpeq4(wv[k], 0x0a0a0a0au) | __vcmpeq4(wv[k], 0x0d0d0d0du);
-        hi |= wv[k] & 0x80808080u;
-      }
-      if (hi && nonascii == NONE) {
-        for (int b = 0; b < 16; ++b)
-          if ((wv[b >> 2] >> (8 * (b & 3))) & 0x80u) {
-            nonascii = p + b;
-            break;
-          }
-      }
-      if (!hit) continue;
-#pragma unroll 1
-      for (int b = 0; b < 16; ++b) {
-        const unsigned c = (wv[b >> 2] >> (8 * (b & 3))) & 0xffu;
-        if (c == 10u || (c == 13u && (p + b + 1 >= n || t[p + b + 1] != 10u))) f(p + b);
-      }
+      const uint64_t x0 = (uint64_t)v.x | ((uint64_t)v.y << 32), x1 = (uint64_t)v.z | ((uint64_t)v.w << 32);
+      word_terms(x0, p, (x1 & 0xffu) == 10u, nonascii, f);
+      const bool lf16 = (x1 >> 56) == 13u && p + 16 < n && t[p + 16] == 10u;
+      word_terms(x1, p + 8, lf16, nonascii, f);
     } else {
       for (int64_t q = p; q < n && q < p + 16; ++q) {
         const unsigned c = t[q];
@@ -564,23 +676,48 @@ __global__ void __launch_bounds__(CHUNK_THREADS) starts_kernel(const uint8_t *t,
     });
 }
 
+template <bool ST>
+__device__ __forceinline__ void classify_line(const Src<ST> &s, int64_t l, int64_t start, int64_t lim, int delim,
+                                              int comment, int64_t skip_header, int32_t *nvals, uint2 *spans,
+                                              int64_t &first) {
+  const LineSpan sp = line_span(s, start, lim, delim, comment);
+  const int32_t nv = l < skip_header ? 0 : sp.nvals;
+  nvals[l] = nv;
+  if (nv > 0) {
+    const int64_t ra = sp.a - start, rb = sp.b - start;
+    spans[l] = rb < 0xffffffffll ? make_uint2((unsigned)ra, (unsigned)rb) : make_uint2(0xffffffffu, 0xffffffffu);
+    first = first < l ? first : l;
+  }
+}
+
 __global__ void __launch_bounds__(LINES_PER_CTA) classify_kernel(const uint8_t *t, int64_t n, const int64_t *starts,
                                                                  int64_t nlines, int delim, int comment,
-                                                                 int64_t skip_header, int32_t *nvals,
+                                                                 int64_t skip_header, int32_t *nvals, uint2 *spans,
                                                                  arb_csv_info *info) {
-  __shared__ __align__(16) uint8_t sm[STAGE_BYTES];
+  __shared__ __align__(16) uint8_t sm[STAGE_BYTES + 16];
+  __shared__ unsigned long long first_sm;
   const int64_t L0 = (int64_t)blockIdx.x * LINES_PER_CTA;
   const int64_t L1 = L0 + LINES_PER_CTA < nlines ? L0 + LINES_PER_CTA : nlines;
   const int64_t a = starts[L0], b = L1 < nlines ? starts[L1] : n;
   int64_t off;
-  const uint8_t *s = stage_bytes(t, n, a, b, sm, off);
+  const bool staged = stage_bytes(t, n, a, b, sm, off);
+  if (threadIdx.x == 0) first_sm = (unsigned long long)NONE;
   __syncthreads();
   const int64_t l = L0 + threadIdx.x;
-  if (l >= L1) return;
-  const LineSpan sp = line_span(s, off, starts[l], b, delim, comment);
-  const int32_t nv = l < skip_header ? 0 : sp.nvals;
-  nvals[l] = nv;
-  if (nv > 0) atomicMin(reinterpret_cast<unsigned long long *>(&info->first_data_line), (unsigned long long)l);
+  int64_t first = NONE;
+  if (l < L1) {
+    if (staged) classify_line(Src<true>{sm, off}, l, starts[l], b, delim, comment, skip_header, nvals, spans, first);
+    else classify_line(Src<false>{t, 0}, l, starts[l], b, delim, comment, skip_header, nvals, spans, first);
+  }
+  // one atomic per CTA: the first line with values
+  for (int o = 16; o > 0; o >>= 1) {
+    const int64_t y = __shfl_down_sync(0xffffffffu, first, o);
+    first = y < first ? y : first;
+  }
+  if ((threadIdx.x & 31) == 0 && first != NONE) atomicMin(&first_sm, (unsigned long long)first);
+  __syncthreads();
+  if (threadIdx.x == 0 && first_sm != (unsigned long long)NONE)
+    atomicMin(reinterpret_cast<unsigned long long *>(&info->first_data_line), first_sm);
 }
 
 __global__ void __launch_bounds__(LINES_PER_CTA) rows_kernel(const int32_t *nvals, int64_t nlines, int64_t *cta_count,
@@ -611,14 +748,14 @@ __global__ void __launch_bounds__(1024) row_scan_kernel(int64_t *cta, int64_t nc
 
 // Tokens of the content [a, b): each parsed and written to out_row[c];
 // returns true when every token was decided by the fast paths.
-__device__ __forceinline__ bool parse_line(const uint8_t *s, int64_t off, int64_t a, int64_t b, int delim,
-                                           int64_t ncols, double *out_row) {
+template <bool ST>
+__device__ __forceinline__ bool parse_line(const Src<ST> &s, int64_t a, int64_t b, int delim, int64_t ncols,
+                                           double *out_row) {
   bool all = true;
   int64_t ts = a;
   for (int64_t c = 0; c < ncols; ++c) {
-    int64_t te = ts;
-    while (te < b && (int)s[te - off] != delim) ++te;
-    const Dec d = parse_token(s + (ts - off), 0, te - ts);
+    const int64_t te = next_delim(s, ts, b, delim);
+    const Dec d = parse_token(s, ts, te);
     bool ok;
     out_row[c] = __longlong_as_double((long long)token_bits(d, ok));
     all &= ok;
@@ -627,26 +764,41 @@ __device__ __forceinline__ bool parse_line(const uint8_t *s, int64_t off, int64_
   return all;
 }
 
+template <bool ST>
+__device__ __forceinline__ bool parse_one(const Src<ST> &s, int64_t start, int64_t lim, uint2 sp, int delim,
+                                          int comment, int64_t ncols, double *out_row) {
+  int64_t a = start + sp.x, b = start + sp.y;
+  if (sp.x == 0xffffffffu) {  // a line longer than 4 GB: walk it again
+    const LineSpan r = line_span(s, start, lim, delim, comment);
+    a = r.a;
+    b = r.b;
+  }
+  return parse_line(s, a, b, delim, ncols, out_row);
+}
+
 __global__ void __launch_bounds__(LINES_PER_CTA) parse_kernel(const uint8_t *t, int64_t n, const int64_t *starts,
-                                                              int64_t nlines, const int32_t *nvals,
+                                                              int64_t nlines, const int32_t *nvals, const uint2 *spans,
                                                               const int64_t *cta_base, int delim, int comment,
                                                               int64_t ncols, double *out, int64_t *queue,
                                                               arb_csv_info *info) {
-  __shared__ __align__(16) uint8_t sm[STAGE_BYTES];
+  __shared__ __align__(16) uint8_t sm[STAGE_BYTES + 16];
   __shared__ int64_t red[LINES_PER_CTA / 32];
   __shared__ int64_t tot;
   const int64_t L0 = (int64_t)blockIdx.x * LINES_PER_CTA;
   const int64_t L1 = L0 + LINES_PER_CTA < nlines ? L0 + LINES_PER_CTA : nlines;
   const int64_t a = starts[L0], b = L1 < nlines ? starts[L1] : n;
   int64_t off;
-  const uint8_t *s = stage_bytes(t, n, a, b, sm, off);
+  const bool staged = stage_bytes(t, n, a, b, sm, off);
   const int64_t l = L0 + threadIdx.x;
   const int32_t nv = l < L1 ? nvals[l] : 0;
   const bool valid = nv > 0 && nv == ncols;
   const int64_t row = cta_base[blockIdx.x] + block_excl_i64(valid ? 1 : 0, red, &tot);  // also syncs the stage
   if (!valid) return;
-  const LineSpan sp = line_span(s, off, starts[l], b, delim, comment);
-  if (!parse_line(s, off, sp.a, sp.b, delim, ncols, out + row * ncols)) {
+  const uint2 sp = spans[l];
+  double *dst = out + row * ncols;
+  const bool ok = staged ? parse_one(Src<true>{sm, off}, starts[l], b, sp, delim, comment, ncols, dst)
+                         : parse_one(Src<false>{t, 0}, starts[l], b, sp, delim, comment, ncols, dst);
+  if (!ok) {
     const unsigned long long k = atomicAdd(reinterpret_cast<unsigned long long *>(&info->nqueued), 1ull);
     queue[2 * k] = l;
     queue[2 * k + 1] = row;
@@ -661,19 +813,19 @@ __global__ void __launch_bounds__(EXACT_THREADS) exact_kernel(const uint8_t *t, 
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   uint32_t *mine = scratch + tid * (3 * LIMBS);
   const int64_t nq = info->nqueued;
+  const Src<false> s{t, 0};
   for (int64_t k = tid; k < nq; k += nthreads) {
     const int64_t l = queue[2 * k], row = queue[2 * k + 1];
     const int64_t lim = l + 1 < nlines ? starts[l + 1] : n;
-    const LineSpan sp = line_span(t, 0, starts[l], lim, delim, comment);
+    const LineSpan sp = line_span(s, starts[l], lim, delim, comment);
     int64_t ts = sp.a;
     for (int64_t c = 0; c < ncols; ++c) {
-      int64_t te = ts;
-      while (te < sp.b && (int)t[te] != delim) ++te;
-      const Dec d = parse_token(t + ts, 0, te - ts);
+      const int64_t te = next_delim(s, ts, sp.b, delim);
+      const Dec d = parse_token(s, ts, te);
       bool ok;
       const uint64_t bits = token_bits(d, ok);
       if (!ok) {
-        const uint64_t m = exact_convert(t + ts, 0, te - ts, bits & ~SIGN, mine, &info->error);
+        const uint64_t m = exact_convert(s, ts, te, bits & ~SIGN, mine, &info->error);
         out[row * ncols + c] = __longlong_as_double((long long)(d.neg ? (m | SIGN) : m));
         atomicAdd(reinterpret_cast<unsigned long long *>(&info->nexact), 1ull);
       }
@@ -697,6 +849,7 @@ static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct LinesWork {
   int64_t *starts, *cta, *queue;
+  uint2 *spans;
   uint32_t *scratch;
 };
 
@@ -704,15 +857,17 @@ static size_t lines_layout(int64_t nlines, int grid, void *base, LinesWork *w) {
   const size_t s0 = align256((size_t)(nlines > 0 ? nlines : 1) * 8);
   const size_t s1 = align256((size_t)(nctas_of(nlines) + 1) * 8);
   const size_t s2 = align256((size_t)(nlines > 0 ? nlines : 1) * 16);
-  const size_t s3 = (size_t)grid * EXACT_THREADS * 3 * LIMBS * 4;
+  const size_t s3 = align256((size_t)(nlines > 0 ? nlines : 1) * 8);
+  const size_t s4 = (size_t)grid * EXACT_THREADS * 3 * LIMBS * 4;
   if (w) {
     char *p = static_cast<char *>(base);
     w->starts = reinterpret_cast<int64_t *>(p);
     w->cta = reinterpret_cast<int64_t *>(p + s0);
     w->queue = reinterpret_cast<int64_t *>(p + s0 + s1);
-    w->scratch = reinterpret_cast<uint32_t *>(p + s0 + s1 + s2);
+    w->spans = reinterpret_cast<uint2 *>(p + s0 + s1 + s2);
+    w->scratch = reinterpret_cast<uint32_t *>(p + s0 + s1 + s2 + s3);
   }
-  return s0 + s1 + s2 + s3;
+  return s0 + s1 + s2 + s3 + s4;
 }
 
 static bool args_ok(const uint8_t *text, int64_t nbytes, int delim, int comment) {
@@ -769,7 +924,7 @@ extern "C" int arb_csv_split(const uint8_t *text, int64_t nbytes, int64_t nlines
   starts_kernel<<<(unsigned)nch, CHUNK_THREADS, 0, s>>>(text, nbytes, static_cast<const int64_t *>(count_work),
                                                         w.starts, nlines);
   classify_kernel<<<(unsigned)nctas, LINES_PER_CTA, 0, s>>>(text, nbytes, w.starts, nlines, delimiter, comment,
-                                                            skip_header, nvals, info);
+                                                            skip_header, nvals, w.spans, info);
   rows_kernel<<<(unsigned)nctas, LINES_PER_CTA, 0, s>>>(nvals, nlines, w.cta, info);
   row_scan_kernel<<<1, 1024, 0, s>>>(w.cta, nctas, nvals, info);
   return arb::launch_status();
@@ -788,8 +943,8 @@ extern "C" int arb_csv_parse(const uint8_t *text, int64_t nbytes, int64_t nlines
   LinesWork w;
   lines_layout(nlines, grid, lines_work, &w);
   const int64_t nctas = nctas_of(nlines);
-  parse_kernel<<<(unsigned)nctas, LINES_PER_CTA, 0, s>>>(text, nbytes, w.starts, nlines, nvals, w.cta, delimiter,
-                                                         comment, ncols, out, w.queue, info);
+  parse_kernel<<<(unsigned)nctas, LINES_PER_CTA, 0, s>>>(text, nbytes, w.starts, nlines, nvals, w.spans, w.cta,
+                                                         delimiter, comment, ncols, out, w.queue, info);
   exact_kernel<<<(unsigned)grid, EXACT_THREADS, 0, s>>>(text, nbytes, w.starts, nlines, delimiter, comment, ncols,
                                                         out, w.queue, w.scratch, info);
   return arb::launch_status();

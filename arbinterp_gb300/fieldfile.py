@@ -76,46 +76,49 @@ def _padded(n: int) -> int:
     return max(16, (n + 15) & ~15)
 
 
-def file_to_device(path, device=None, stream=None):
-    """Bytes of ``path`` in a CUDA uint8 tensor (16-byte padded) and the
-    file size; the copy runs on ``stream`` and overlaps the reads."""
+def _to_device(size: int, fill, device, stream):
+    """A CUDA uint8 tensor (16-byte padded) holding ``size`` bytes that
+    ``fill(view, offset)`` writes into pinned staging buffers, chunk by chunk
+    on several threads; each chunk's host-to-device copy runs on ``stream``
+    while the next chunk is filled."""
     device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
     stream = torch.cuda.current_stream(device) if stream is None else stream
-    size = os.path.getsize(path)
     text = torch.empty(_padded(size), dtype=torch.uint8, device=device)
     if size == 0:
         return text, 0
     bufs, evs = _ring(device)
     pool = _readers()
+    for k, off in enumerate(range(0, size, CHUNK)):
+        n = min(CHUNK, size - off)
+        slot = k % RING
+        evs[slot].synchronize()               # the copy that last used this buffer is done
+        mv = memoryview(bufs[slot].numpy())[:n]
+        step = max(4 << 20, -(-n // READERS))
+        list(pool.map(lambda a: fill(mv[a:a + step], off + a), range(0, n, step)))
+        with torch.cuda.stream(stream):
+            text[off:off + n].copy_(bufs[slot][:n], non_blocking=True)
+            evs[slot].record(stream)
+    return text, size
+
+
+def file_to_device(path, device=None, stream=None):
+    """Bytes of the file at ``path`` in a CUDA uint8 tensor (16-byte padded)
+    and the file size; reads overlap the copies."""
+    size = os.path.getsize(path)
     fd = os.open(path, os.O_RDONLY)
     try:
-        for k, off in enumerate(range(0, size, CHUNK)):
-            n = min(CHUNK, size - off)
-            slot = k % RING
-            evs[slot].synchronize()           # the copy that last used this buffer is done
-            mv = memoryview(bufs[slot].numpy())[:n]
-            step = max(4 << 20, -(-n // READERS))
-            list(pool.map(lambda a: _pread_into(fd, mv[a:a + step], off + a), range(0, n, step)))
-            with torch.cuda.stream(stream):
-                text[off:off + n].copy_(bufs[slot][:n], non_blocking=True)
-                evs[slot].record(stream)
+        return _to_device(size, lambda mv, off: _pread_into(fd, mv, off), device, stream)
     finally:
         os.close(fd)
-    return text, size
 
 
 def bytes_to_device(data, device=None, stream=None):
     """A bytes-like object's contents in a CUDA uint8 tensor (16-byte padded)."""
-    device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
-    stream = torch.cuda.current_stream(device) if stream is None else stream
     src = np.frombuffer(memoryview(data).cast("B"), dtype=np.uint8)
-    text = torch.empty(_padded(src.size), dtype=torch.uint8, device=device)
-    if src.size:
-        host = torch.from_numpy(src.copy()).pin_memory()
-        with torch.cuda.stream(stream):
-            text[:src.size].copy_(host, non_blocking=True)
-        stream.synchronize()
-    return text, int(src.size)
+
+    def fill(mv, off):
+        np.copyto(np.frombuffer(mv, dtype=np.uint8), src[off:off + len(mv)])
+    return _to_device(int(src.size), fill, device, stream)
 
 
 def _char(v, what: str) -> int:
@@ -137,9 +140,12 @@ def _info(t: torch.Tensor) -> dict:
 
 
 def parse_device_text(text: torch.Tensor, nbytes: int, delimiter=",", comments="#", skip_header: int = 0,
-                      name: str = "<bytes>", stream=None, stats: dict | None = None) -> torch.Tensor:
+                      name: str = "<bytes>", stream=None, stats: dict | None = None,
+                      timing: dict | None = None) -> torch.Tensor:
     """Parse ``nbytes`` of CSV text already on the device (a 16-byte aligned
-    uint8 CUDA tensor) into a float64 table, as ``genfromtxt`` does."""
+    uint8 CUDA tensor) into a float64 table, as ``genfromtxt`` does.
+    ``timing``, when given, receives each phase's device time in ms (CUDA
+    events around the count, split and parse calls)."""
     L = _lib.lib()
     delim = _char(delimiter, "delimiter")
     if delim == -1:
@@ -153,11 +159,20 @@ def parse_device_text(text: torch.Tensor, nbytes: int, delimiter=",", comments="
     device = text.device
     stream = torch.cuda.current_stream(device) if stream is None else stream
     s = stream.cuda_stream
+    if text.data_ptr() % 16 or text.numel() < nbytes:
+        raise ValueError("text must be a 16-byte aligned uint8 tensor holding nbytes bytes")
     info = torch.zeros(_INFO_WORDS, dtype=torch.int64, device=device)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)] if timing is not None else None
+
+    def mark(k):
+        if ev is not None:
+            ev[k].record(stream)
     with torch.cuda.stream(stream):
         cw = torch.empty(L.arb_csv_count_work_bytes(nbytes), dtype=torch.uint8, device=device)
+        mark(0)
         _lib.check(L.arb_csv_count(text.data_ptr(), nbytes, cw.data_ptr(), cw.numel(), info.data_ptr(), s),
                    "arb_csv_count")
+        mark(1)
         h = _info(info)
         if h["first_nonascii"] >= 0:
             off = h["first_nonascii"]
@@ -168,9 +183,11 @@ def parse_device_text(text: torch.Tensor, nbytes: int, delimiter=",", comments="
             return _empty(name, device)
         lw = torch.empty(L.arb_csv_lines_work_bytes(nlines), dtype=torch.uint8, device=device)
         nvals = torch.empty(nlines, dtype=torch.int32, device=device)
+        mark(2)
         _lib.check(L.arb_csv_split(text.data_ptr(), nbytes, nlines, delim, comment, skip_header, cw.data_ptr(),
                                    lw.data_ptr(), lw.numel(), nvals.data_ptr(), info.data_ptr(), s),
                    "arb_csv_split")
+        mark(3)
         h = _info(info)
         if h["first_data_line"] < 0:
             return _empty(name, device)
@@ -178,10 +195,15 @@ def parse_device_text(text: torch.Tensor, nbytes: int, delimiter=",", comments="
         if h["ninvalid"]:
             raise ValueError(_invalid_message(nvals.cpu().numpy(), h["first_data_line"], ncols, skip_header))
         out = torch.empty((nrows, ncols), dtype=torch.float64, device=device)
+        mark(4)
         _lib.check(L.arb_csv_parse(text.data_ptr(), nbytes, nlines, delim, comment, lw.data_ptr(), lw.numel(),
                                    nvals.data_ptr(), out.data_ptr(), nrows, ncols, info.data_ptr(), s),
                    "arb_csv_parse")
+        mark(5)
         h = _info(info)
+    if ev is not None:
+        timing.update(count_ms=ev[0].elapsed_time(ev[1]), split_ms=ev[2].elapsed_time(ev[3]),
+                      parse_ms=ev[4].elapsed_time(ev[5]))
     if h["error"]:
         raise RuntimeError(f"arb_csv_parse: exact conversion ran out of big-integer capacity ({h['error']})")
     if stats is not None:
@@ -212,7 +234,8 @@ def genfromtxt(fname, delimiter=",", comments="#", skip_header: int = 0, *, devi
     computed on the GPU; returns a CUDA float64 tensor.
 
     ``fname``: a path (str / PathLike), a bytes-like object holding the
-    file's contents, or a file object (read whole).  ``stats``, when given,
+    file's contents, a file object (read whole), or the text already on the
+    device as a 1-D uint8 CUDA tensor.  ``stats``, when given,
     receives the reader's counters (lines, rows, tokens settled by the exact
     big-integer pass)."""
     if isinstance(fname, os.PathLike):
@@ -222,6 +245,12 @@ def genfromtxt(fname, delimiter=",", comments="#", skip_header: int = 0, *, devi
             raise NotImplementedError(f"{fname}: compressed files are not read by the GPU reader")
         text, n = file_to_device(fname, device)
         name = fname
+    elif isinstance(fname, torch.Tensor):
+        if not (fname.is_cuda and fname.dtype == torch.uint8 and fname.dim() == 1):
+            raise TypeError("a tensor input must be 1-D uint8 text on a CUDA device")
+        n = fname.numel()
+        text = fname if fname.data_ptr() % 16 == 0 else fname.clone()
+        name = "<device text>"
     elif isinstance(fname, (bytes, bytearray, memoryview)):
         text, n = bytes_to_device(fname, device)
         name = "<bytes>"

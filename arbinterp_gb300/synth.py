@@ -149,3 +149,44 @@ def batched_fields(n_fields=512, seed=4, edge_range=(16, 128), q_range=(1e3, 1e6
         nq = int(round(math.exp(rng.uniform(math.log(q_range[0]), math.log(q_range[1])))))
         f = gaussian_field3(n=(e, e, e), h=h, seed=int(rng.integers(1 << 30)), device=device)
         yield f, nq, int(rng.integers(1 << 30))
+
+
+
+def field_csv_text(n=(256, 256, 256), nfield=3, seed=5, origin=-1.0, inv_h=128, device="cpu"):
+    """A field file in the reference's layout (np.savetxt fmt '%.18e',
+    delimiter ','; README.md:64-72) as a 1-D uint8 tensor on ``device``: rows
+    x, y, z, then nfield values, x fastest.  Coordinates are the grid
+    origin + i / inv_h (exact decimals, formatted by Python); field values are
+    random 19-significant-digit decimals with random signs and exponents in
+    [-20, 20], so each value has the savetxt width of its sign (24 or 25
+    characters)."""
+    nx, ny, nz = n
+    rows = nx * ny * nz
+    ncol = 3 + nfield
+    W = 26                                   # sign slot + 24 characters + delimiter
+    gen = torch.Generator(device=device).manual_seed(seed)
+    u8 = dict(dtype=torch.uint8, device=device)
+    arr = torch.empty((rows, ncol * W), **u8)
+    keep = torch.ones((rows, ncol * W), dtype=torch.bool, device=device)
+    arr[:, W - 1::W] = ord(",")
+    arr[:, -1] = ord("\n")
+    r = torch.arange(rows, dtype=torch.int64, device=device)
+    idx = (r % nx, torch.div(r, nx, rounding_mode="floor") % ny, torch.div(r, nx * ny, rounding_mode="floor"))
+    for a, m in enumerate((nx, ny, nz)):
+        strs = ["%.18e" % (origin + i / inv_h) for i in range(m)]
+        tab = torch.tensor(list("".join(s.rjust(25) for s in strs).encode()), **u8).reshape(m, 25)
+        arr[:, a * W:a * W + 25] = tab[idx[a]]
+        keep[:, a * W] = tab[idx[a], 0] == ord("-")
+    for k in range(3, ncol):
+        o = k * W
+        arr[:, o] = ord("-")
+        keep[:, o] = torch.rand(rows, generator=gen, device=device) < 0.5
+        arr[:, o + 1] = torch.randint(ord("1"), ord("9") + 1, (rows,), generator=gen, **u8)
+        arr[:, o + 2] = ord(".")
+        arr[:, o + 3:o + 21] = torch.randint(ord("0"), ord("9") + 1, (rows, 18), generator=gen, **u8)
+        arr[:, o + 21] = ord("e")
+        e = torch.randint(-20, 21, (rows,), generator=gen, device=device)
+        arr[:, o + 22] = torch.where(e < 0, ord("-"), ord("+")).to(torch.uint8)
+        arr[:, o + 23] = (e.abs() // 10 + ord("0")).to(torch.uint8)
+        arr[:, o + 24] = (e.abs() % 10 + ord("0")).to(torch.uint8)
+    return arr[keep]

@@ -53,24 +53,28 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--kernel-only", action="store_true", help="time only the query kernel (profiling)")
-    p.add_argument("--workload", default=None, choices=["c0", "c2", "c3", "c4", "traj"],
+    p.add_argument("--workload", default=None, choices=["c0", "c2", "c3", "c4", "traj", "csv"],
                    help="measure one of the other seeded configurations and print its own JSON line: "
                         "c0 = 41^3 scalar, 1e5 queries; c2 = 4D 64^3x32 scalar, 1e7 queries; c3 = 512 batched "
                         "scalar fields in one persistent launch / CUDA graph; c4 = differentiable 128^3 "
                         "float32 field, 1e6 queries, forward + backward; traj = 1e6 particles, 100 RK4 steps "
-                        "through the 256^3 'both' field")
+                        "through the 256^3 'both' field; csv = the 256^3 'both' field as a savetxt '%%.18e' "
+                        "CSV file (2.6 GB) read as np.genfromtxt(delimiter=',') does")
     p.add_argument("--profile", default=None,
                    choices=["step", "small", "small-table", "small-fp64", "small-coef", "small-4d", "small-batched",
-                            "small-adjoint"],
+                            "small-adjoint", "small-csv"],
                    help="run a fixed workload for an ncu capture and exit (no timing, no JSON): "
                         "'step' = two full bench steps; 'small*' = 160^3 dipole field, 2.02e6 queries; "
                         "'small-coef' = 96^3 table solve; 'small-4d' = 40^3x12 scalar, 2e6 queries (on the fly "
                         "and table); 'small-batched' = 64 scalar fields; 'small-adjoint' = 96^3 scalar, 2e6 "
-                        "queries forward + backward")
+                        "queries forward + backward; 'small-csv' = the 128^3 'both' field file (324 MB) "
+                        "parsed twice")
     return p.parse_args()
 
 
 EVAL_SMALL_TRAFFIC = 249.86e6  # dram read + write of eval_bin_kernel<4> on the 160^3 case (ncu capture)
+# dram read + write of parse_kernel per byte of text: 444.0 MB for the 128^3 field file (324.0 MB; ncu capture)
+CSV_PARSE_TRAFFIC_PER_BYTE = (366.16e6 + 77.83e6) / 324.01e6
 
 
 def run_profile(args):
@@ -91,6 +95,11 @@ def run_profile(args):
                 q = synth.uniform_queries([float(v) for v in o._lo], [float(v) for v in o._hi], 2_000_000, 0,
                                           [float(v) for v in o._h], seed=3, device=dev)
                 o.Query(q)
+    elif args.profile == "small-csv":
+        from arbinterp_gb300 import fieldfile
+        text = synth.field_csv_text((128, 128, 128), 3, seed=5, device=dev)
+        for _ in range(2):
+            fieldfile.parse_device_text(text, text.numel())
     elif args.profile == "small-batched":
         from arbinterp_gb300.batched import BatchedTricubic
         fields, qs, counts = [], [], []
@@ -264,6 +273,8 @@ def run_workload(args):
                      "config": {"workload": "1e6 particles x 100 RK4 steps in the 256^3 dipole |B| field "
                                             "(x'' = -1e-4 grad|B|)", "precision": "mixed"},
                      "paths": res, "position_diff_mixed_vs_fp64_quantiles": dx})
+    elif args.workload == "csv":
+        line.update(csv_workload(args, dev, gpu_index))
     else:  # c4
         from arbinterp_gb300.autograd import TricubicField
         # float32 samples; both precisions get the same (float64) geometry
@@ -397,6 +408,92 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def csv_workload(args, dev, gpu_index):
+    """The 256^3 'both' field (16.8M rows x 6 values) as a savetxt '%.18e'
+    CSV file, parsed as np.genfromtxt(path, delimiter=',') does.  value:
+    text resident in HBM -> float64 table; e2e: host bytes -> pinned staging
+    -> device -> table -> host array; checked bit for bit against
+    np.genfromtxt on two 1e5-line samples, which also give the CPU baseline."""
+    import io
+
+    import numpy as np
+    import torch
+    from arbinterp_gb300 import fieldfile, genfromtxt, synth
+    t0 = time.perf_counter()
+    raw = synth.field_csv_text(GRID, 3, seed=5, device=dev)
+    nbytes = raw.numel()
+    text = torch.empty(fieldfile._padded(nbytes), dtype=torch.uint8, device=dev)
+    text[:nbytes] = raw
+    del raw
+    host = text[:nbytes].cpu().numpy().tobytes()
+    gen_s = time.perf_counter() - t0
+
+    def run():
+        return fieldfile.parse_device_text(text, nbytes)
+    with ClockSampler(gpu_index) as clk:
+        t = cuda_time(run, args.steps, args.warmup)
+    stats, phases = {}, []
+    for _ in range(3):
+        tm = {}
+        out = fieldfile.parse_device_text(text, nbytes, stats=stats, timing=tm)
+        phases.append(tm)
+    ph = {k: float(np.median([p[k] for p in phases])) for k in phases[0]}
+    nrows, ncols, nlines = stats["nrows"], stats["ncols"], stats["nlines"]
+    # bit-exact check against np.genfromtxt on two samples (first lines, middle of the file)
+    S = 100_000
+    checks, cpu_s, cpu_bytes = [], 0.0, 0
+    buf = np.frombuffer(host, dtype=np.uint8)
+    for start in (0, nbytes // 2):
+        if start:
+            start = host.index(b"\n", start) + 1
+        win = buf[start:start + 200 * S]
+        nl = np.flatnonzero(win == 10)
+        chunk = host[start:start + int(nl[S - 1]) + 1]
+        r0 = 0 if start == 0 else int(np.count_nonzero(buf[:start] == 10))
+        c0 = time.perf_counter()
+        ref = np.genfromtxt(io.BytesIO(chunk), delimiter=",")
+        cpu_s += time.perf_counter() - c0
+        cpu_bytes += len(chunk)
+        got = out[r0:r0 + S].cpu().numpy()
+        checks.append(bool(np.array_equal(got.view(np.uint64), ref.view(np.uint64))))
+    del buf
+    # end to end through the public API: host bytes in, host array out
+    ke = max(1, args.steps // 3)
+
+    def e2e():
+        return genfromtxt(host).cpu()
+    e2e()
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for _ in range(ke):
+        e2e()
+    torch.cuda.synchronize()
+    te = (time.perf_counter() - e0) / ke
+    peak, src = measured_peaks()
+    alg = nbytes + nrows * ncols * 8 + nlines * 12
+    achieved = alg / (ph["parse_ms"] / 1000.0) / 1e9
+    return {
+        "metric": "csv: field-file bytes/s parsed, np.genfromtxt(delimiter=',') drop-in (bit-exact)",
+        "value": nbytes * args.steps / t / 1e9, "unit": "GB/s", "ms_per_step": 1000 * t / args.steps,
+        "dtype": "u8->f64", "gpu_launches": 9 * args.steps,
+        "config": {"workload": f"256^3 'both' field file: {nrows} rows x {ncols} values, savetxt '%.18e' "
+                               f"({nbytes / 1e9:.2f} GB); text resident in HBM (larger than L2)",
+                   "rows_per_s": nrows * args.steps / t, "generate_s": gen_s},
+        "phases_ms": ph,
+        "exact_pass_tokens": stats["nexact"],
+        "bit_exact_vs_np_genfromtxt": {"samples": 2, "lines_per_sample": S, "all_equal": all(checks)},
+        "roofline": {"bound": "hbm", "kernel": "arb_csv_parse (parse_kernel + exact pass)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": CSV_PARSE_TRAFFIC_PER_BYTE * nbytes, "algorithmic_bytes": alg, "peak_source": src},
+        "cpu_baseline": {"value": cpu_bytes / cpu_s / 1e9, "unit": "GB/s", "cores": 1, "kind": "reference",
+                         "sample": f"np.genfromtxt(BytesIO, delimiter=',') on 2 x {S} lines "
+                                   f"({cpu_bytes / 1e6:.0f} MB) of the same file, one host core"},
+        "e2e": {"value": nbytes / te / 1e9, "unit": "GB/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nrows * ncols * 8, "ms_per_step": 1000 * te},
+        "clocks": clk.summary(),
+    }
 
 
 def measured_peaks():
