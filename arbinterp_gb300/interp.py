@@ -43,6 +43,20 @@ __version__ = "1.8"
 _F = {_lib.KIND_SCALAR: 1, _lib.KIND_VECTOR: 3, _lib.KIND_NORM: 1, _lib.KIND_BOTH: 4}
 _AXIS_CAP = 1 << 17
 _ORDERED_INGEST = True      # try the single-pass ingest for rows in meshgrid order first
+# host (NumPy) range queries of at least this many rows are uploaded, evaluated
+# and downloaded chunk by chunk on overlapping streams
+PIPELINE_MIN_ROWS = 1 << 21
+PIPELINE_MIN_CHUNK_ROWS = 1 << 20
+PIPELINE_MAX_CHUNKS = 8
+_COPY_STREAMS: dict = {}
+
+
+def _copy_streams(device):
+    """(copy-in, copy-out) side streams of a device, created once."""
+    key = torch.device(device).index
+    if key not in _COPY_STREAMS:
+        _COPY_STREAMS[key] = (torch.cuda.Stream(device), torch.cuda.Stream(device))
+    return _COPY_STREAMS[key]
 
 _BANNERS = {
     "scalar": "--- Scalar field, ignoring switches, interpolating for magnitude and gradient --- \n",
@@ -442,10 +456,20 @@ class _Interpolant:
             return 4, 0, None, None
         return (4 if dim == 3 else 8), None, 0, 1
 
-    def _outputs(self, n, want_oob):
+    def _packed_layout(self):
+        """Rows holding only what the caller receives (no padding column):
+        the layout downloaded to host arrays."""
+        dim, kind = self._dim, self._kind
+        if kind == _lib.KIND_BOTH:
+            return 3 + 1 + dim, 0, 3, 4
+        if kind == _lib.KIND_VECTOR:
+            return 3, 0, None, None
+        return 1 + dim, None, 0, 1
+
+    def _outputs(self, n, want_oob, packed=False):
         dev = self.device
         dim = self._dim
-        R, ci, ni, gi = self._row_layout()
+        R, ci, ni, gi = self._packed_layout() if packed else self._row_layout()
         rows = torch.empty((n, R), dtype=torch.float64, device=dev)
         comps = rows[:, ci:ci + 3] if ci is not None else None
         norms = rows[:, ni:ni + 1] if ni is not None else None
@@ -455,12 +479,14 @@ class _Interpolant:
         cnt = torch.zeros(1, dtype=torch.int64, device=dev) if want_oob else None
         return comps, norms, grads, inds, oob, cnt
 
-    def _launch(self, qd, n, qs, writeback, want_oob, plan):
-        """Launch one evaluation of device rows qd with a given plan."""
+    def _launch(self, qd, n, qs, writeback, want_oob, plan, res=None):
+        """Launch one evaluation of device rows qd with a given plan (into
+        the preallocated outputs res when given)."""
         L = lib()
-        res = self._outputs(n, want_oob)
+        if res is None:
+            res = self._outputs(n, want_oob)
         comps, norms, grads, inds, oob, cnt = res
-        R = self._row_layout()[0]
+        R = (comps if comps is not None else norms).stride(0)
         out = ArbQueryOut(_ptr(comps), _ptr(norms), _ptr(grads), _ptr(inds), _ptr(oob), _ptr(cnt), R, R, R)
         s = _stream()
         table = bool(plan["table"])
@@ -524,6 +550,8 @@ class _Interpolant:
         if qs < dim:
             raise IndexError("query rows need at least %d columns" % dim)
         qc = np.ascontiguousarray(qa, dtype=np.float64)
+        if n >= PIPELINE_MIN_ROWS:
+            return self._rquery_host_pipelined(qa, qc, n, qs)
         qd = torch.from_numpy(qc).to(self.device, non_blocking=True)
         comps, norms, grads, inds, oob, cnt = self._run(qd, n, qs, False, True)
         # one copy of the interleaved rows; the outputs are column views of it
@@ -541,6 +569,61 @@ class _Interpolant:
         if st & _lib.ARB_ERR_CELL_INDEX:
             raise IndexError("cell index beyond the coefficient table (query on an upper face)")
         out = [None if h is None else h.numpy() for h in host]
+        return self._pack(*out)
+
+    def _rquery_host_pipelined(self, qa, qc, n, qs):
+        """rQuery of a large host array in chunks: every chunk's upload is
+        queued on a copy-in stream, each chunk is binned and evaluated on the
+        current stream as soon as it has arrived, and its output rows go back
+        on a copy-out stream (the other direction of the link) while later
+        chunks upload and evaluate.  Results, in-place NaN rows and
+        queryInds are those of the single-shot path."""
+        dev = self.device
+        K = max(2, min(PIPELINE_MAX_CHUNKS, n // PIPELINE_MIN_CHUNK_ROWS))
+        bounds = [n * k // K for k in range(K + 1)]
+        src = torch.from_numpy(qc)
+        cur = torch.cuda.current_stream(dev)
+        s_in, s_out = _copy_streams(dev)
+        qd = torch.empty((n, qs), dtype=torch.float64, device=dev)
+        comps, norms, grads, inds, _, _ = self._outputs(n, False, packed=True)
+        rows = (comps if comps is not None else norms)._base
+        oob = torch.empty(n, dtype=torch.int64, device=dev)
+        cnts = torch.zeros(K, dtype=torch.int64, device=dev)
+        hrows = torch.empty(rows.shape, dtype=rows.dtype, pin_memory=True)
+        ev_in = [torch.cuda.Event() for _ in range(K)]
+        ev_done = [torch.cuda.Event() for _ in range(K)]
+        s_in.wait_stream(cur)                       # the buffers were allocated on the current stream
+        with torch.cuda.stream(s_in):
+            for k in range(K):
+                a, b = bounds[k], bounds[k + 1]
+                qd[a:b].copy_(src[a:b], non_blocking=True)
+                ev_in[k].record(s_in)
+        plan = None
+        sl = lambda t, a, b: None if t is None else t[a:b]  # noqa: E731
+        for k in range(K):
+            a, b = bounds[k], bounds[k + 1]
+            cur.wait_event(ev_in[k])
+            if plan is None:
+                plan = self._plan(qd[a:b], b - a, qs)
+                self.last_plan = plan
+            res = (sl(comps, a, b), sl(norms, a, b), sl(grads, a, b), inds[a:b], oob[a:b], cnts[k:k + 1])
+            self._launch(qd[a:b], b - a, qs, False, True, plan, res=res)
+            ev_done[k].record(cur)
+            s_out.wait_event(ev_done[k])
+            with torch.cuda.stream(s_out):
+                hrows[a:b].copy_(rows[a:b], non_blocking=True)
+        st = self._fetch_status()                   # synchronises the current stream
+        c = cnts.cpu().numpy()
+        if c.any():
+            bad = torch.cat([oob[bounds[k]:bounds[k] + int(c[k])] + bounds[k] for k in range(K) if c[k]])
+            qa[bad.cpu().numpy()] = np.nan          # in-place on the caller's array
+        s_out.synchronize()                         # every stream is idle before the buffers are released
+        self._last_inds = inds
+        if st & _lib.ARB_ERR_CELL_INDEX:
+            raise IndexError("cell index beyond the coefficient table (query on an upper face)")
+        R, ci, ni, gi = self._packed_layout()
+        dim = self._dim
+        out = [None if c_ is None else hrows[:, c_:c_ + w].numpy() for c_, w in ((ci, 3), (ni, 1), (gi, dim))]
         return self._pack(*out)
 
     def sQuery(self, query):

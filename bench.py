@@ -778,12 +778,14 @@ def main():
         def step_host():
             ob = tricubic(fnp, "quiet", mode="both", precision=prec, strategy=strat)
             last["out"] = ob.Query(qnp)
-            last["rows_bytes"] = ob._row_layout()[0] * 8 * qnp.shape[0]
+            from arbinterp_gb300 import interp as _ip
+            lay = ob._packed_layout() if qnp.shape[0] >= _ip.PIPELINE_MIN_ROWS else ob._row_layout()
+            last["rows_bytes"] = lay[0] * 8 * qnp.shape[0]
 
         te = cuda_time(step_host, max(3, args.steps // 2), 2, barrier)
         te = tmax(te)
         ksteps = max(3, args.steps // 2)
-        # the outputs are column views of one interleaved row buffer, copied whole
+        # the outputs are column views of one row buffer (packed: only the returned columns), copied whole
         d2h = last["rows_bytes"]
         e2e = {"value": world * nq * ksteps / te, "unit": "queries/s",
                "h2d_bytes_per_step": int(fnp.nbytes + qnp.nbytes), "d2h_bytes_per_step": int(d2h),

@@ -1,0 +1,46 @@
+"""Large host (NumPy) range queries run chunked on overlapping copy and
+compute streams; results, the in-place NaN rows of the caller's array and
+queryInds are bit-identical to the single-shot device-tensor path."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("mode", ["both", None])
+def test_pipelined_host_query_equals_device_query(prec, mode):
+    import torch
+    from arbinterp_gb300 import interp, synth, tricubic
+    f = synth.dipole_field3(n=(48, 40, 36), seed=3).numpy()
+    if mode is None:
+        f = np.hstack([f[:, :3], f[:, 3:4] * f[:, 4:5] + 1.0])
+    kw = {} if mode is None else {"mode": mode}
+    o = tricubic(f, "quiet", precision=prec, **kw)
+    n = interp.PIPELINE_MIN_ROWS + 12345
+    rng = np.random.default_rng(4)
+    lo, hi = np.array(o._lo, float), np.array(o._hi, float)
+    q = rng.uniform(lo - 0.02 * (hi - lo), hi + 0.02 * (hi - lo), (n, 3))   # some rows outside
+    q = np.hstack([q, rng.standard_normal((n, 1))])                          # and an extra column
+    qh = q.copy()
+    rh = o.Query(qh)
+    ih = o.queryInds.copy()
+    qd = torch.from_numpy(q.copy()).cuda()
+    rd = o.Query(qd)
+    idd = o.queryInds
+    rh = rh if isinstance(rh, tuple) else (rh,)
+    rd = rd if isinstance(rd, tuple) else (rd,)
+    for a, b in zip(rh, rd):
+        b = b.cpu().numpy()
+        assert a.shape == b.shape
+        assert np.array_equal(a.view(np.uint64), np.ascontiguousarray(b).view(np.uint64))
+    assert np.array_equal(np.isnan(qh), np.isnan(qd.cpu().numpy()))
+    assert np.isnan(qh).all(1).sum() > 1000
+    assert np.array_equal(ih, np.asarray(idd))
