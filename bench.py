@@ -73,6 +73,9 @@ def parse():
 
 
 EVAL_SMALL_TRAFFIC = 249.86e6  # dram read + write of eval_bin_kernel<4> on the 160^3 case (ncu capture)
+# dram read + write of eval_tab_coop_kernel<4, mixed> per query: 1.902 GB for 2.02e6 queries on the
+# 160^3 table (3.94M cells; ncu capture)
+TAB_SMALL_TRAFFIC_PER_QUERY = (1.777388e9 + 0.124713e9) / 2.02e6
 # dram read + write of parse_kernel per byte of text: 444.0 MB for the 128^3 field file (324.0 MB; ncu capture)
 CSV_PARSE_TRAFFIC_PER_BYTE = (366.16e6 + 77.83e6) / 324.01e6
 
@@ -754,6 +757,25 @@ def main():
         gemm_flops = 2.0 * 64 * 64 * 4 * cells
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if \
             os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        # the table evaluation kernel alone (queries binned once), against the
+        # compulsory bytes: each distinct cell's 1 KB block once, the record
+        # and the output row of every query
+        ws_t = torch.empty(int(L.arb_query_sorted_work_bytes(ot._g, pc, nq)), dtype=torch.uint8, device=dev)
+        ot._g.bin_shift = 0
+        LB.check(L.arb_query_bin(ot._g, pc, q.clone().data_ptr(), nq, 3, 0, qo, ws_t.data_ptr(), ws_t.numel(),
+                                 st.data_ptr(), sp), "arb_query_bin")
+        kt_tab = cuda_time(lambda: L.arb_query_eval_binned(ot._g, pc, 1, nq, qo, ws_t.data_ptr(), ws_t.numel(),
+                                                           sp), 5, 2) / 5
+        cells_hit = int(torch.unique(oi[oi < ot.nc]).numel())
+        tab_alg = cells_hit * 4 * 64 * 4 + nq * (32 + 7 * 8)
+        tab_ach = tab_alg / kt_tab / 1e9
+        del ws_t
+        extra["roofline_table_eval"] = {
+            "bound": "hbm", "kernel": "eval_tab_coop_kernel<4, mixed>", "kernel_ms": 1000 * kt_tab,
+            "achieved": tab_ach, "peak": peak, "unit": "GB/s", "frac": tab_ach / peak,
+            "traffic": nq * TAB_SMALL_TRAFFIC_PER_QUERY, "algorithmic_bytes": tab_alg, "peak_source": peak_src,
+            "distinct_cells": cells_hit,
+            "no_dedup_frac": nq * (4 * 64 * 4 + 32 + 7 * 8) / kt_tab / 1e9 / peak}
         extra["table_path"] = {
             "value": world * nq / (tg + tt), "unit": "queries/s",
             "coef_gemm_ms": 1000 * tg, "table_eval_ms": 1000 * tt,
