@@ -260,7 +260,8 @@ __device__ __forceinline__ void write_slot(const TF *row, int64_t dest, int64_t 
       // norm evaluates it: sqrt((bx*bx + by*by) + bz*bz).
       double nrm;
       if (sizeof(TF) == 8 && grid32 && norm_f32pair(out[0], out[1], out[2], nhi, nlo)) {
-        nrm = f2d_exact(nhi) + f2d_exact(nlo);
+        // the float64 value is needed only for grid64 (grid32 takes the pair)
+        nrm = grid64 ? f2d_exact(nhi) + f2d_exact(nlo) : 0.0;
         nsplit = true;
       } else if (sizeof(TF) == 8) {
         nrm = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn((double)bx, (double)bx), __dmul_rn((double)by, (double)by)),
@@ -292,10 +293,13 @@ __device__ __forceinline__ void write_slot(const TF *row, int64_t dest, int64_t 
   if (grid32) {
     float hi[4], lo[4];
 #pragma unroll
-    for (int f = 0; f < F; ++f) split_f32(out[f], hi[f], lo[f]);
-    if (nsplit) {
-      hi[F - 1] = nhi;
-      lo[F - 1] = nlo;
+    for (int f = 0; f < F; ++f) {
+      if (nsplit && f == F - 1) {
+        hi[f] = nhi;
+        lo[f] = nlo;
+      } else {
+        split_f32(out[f], hi[f], lo[f]);
+      }
     }
     if (F == 4) {
       reinterpret_cast<float4 *>(grid32)[dest] = make_float4(hi[0], hi[1 % F], hi[2 % F], hi[3 % F]);

@@ -590,73 +590,90 @@ static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, 
   bin_place_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, w);
 }
 
-// 3D table evaluation, 8 lanes per query.  A cell's block is F fields x 16
-// rows (ey + 4 ez) of 4 x-coefficients; lane j loads rows j and j + 8 of
-// every field (ey = j & 3, ez = j >> 2 and j >> 2 + 2), so each load
-// instruction of a group reads one contiguous 128-byte line (float table;
-// two with a double table) and a warp's four queries four lines.  Each lane
-// evaluates its rows along x (Horner) and weights them by y^ey z^ez (and the
-// derivative weights for the gradient field); the group reduces with three
-// butterfly shuffles and its first lane writes the row.  Each block walks
-// TAB_CHUNK consecutive sorted queries.
+// Table evaluation, 8 lanes per query.  A cell's block is F fields x R rows
+// (ey + 4 ez [+ 16 et]; R = 16 in 3D, 64 in 4D) of 4 x-coefficients; lane j
+// loads rows j + 8 i of every field (ey = j & 3, ez alternating between
+// j >> 2 and j >> 2 + 2, et = i >> 1), so each load instruction of a group
+// reads one contiguous 128-byte line (float table; two with a double table)
+// and a warp's four queries four lines.  Each lane evaluates its rows along x
+// (Horner) and weights them by y^ey z^ez t^et (and the derivative weights for
+// the gradient field); three butterfly shuffles reduce and the group's first
+// lane writes the row.  Each block walks TAB_CHUNK consecutive sorted queries.
 constexpr int TAB_CHUNK = 256;
 
-template <int F, bool MIXED>
+template <int DIM, int F, bool MIXED>
 __global__ void __launch_bounds__(256) eval_tab_coop_kernel(arb_grid g, KParams kp, int64_t nq, arb_query_out o,
                                                             SortedWork w) {
   using T = typename std::conditional<MIXED, float, double>::type;
+  constexpr int M = DIM == 3 ? 64 : 256, NR = M / 32;  // rows per lane and field
+  constexpr bool GRAD = F != 3;
   const int lane = threadIdx.x & 31, j = lane & 7;
   const unsigned gmask = 0xffu << (lane & 24);
   const int64_t t0 = (int64_t)blockIdx.x * TAB_CHUNK;
   const int64_t t1 = min(t0 + TAB_CHUNK, nq);
   const T *tab = reinterpret_cast<const T *>(g.table);
-  const int ey = j & 3, ez = j >> 2;
+  const int ey = j & 3, jz = j >> 2;
   for (int64_t t = t0 + (threadIdx.x >> 3); t < t1; t += blockDim.x >> 3) {
     const QRec<T> r = reinterpret_cast<const QRec<T> *>(w.rec)[t];
     const unsigned long long cw = r.cell;
     const int64_t i = r.row;
     if (cw & CELL_SPECIAL) {
-      if (j == 0) write_const<3, F>(o, i, (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
+      if (j == 0) write_const<DIM, F>(o, i, (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
       continue;
     }
-    int64_t c[3];
-    unpack_cell<3>(cw, c);
+    int64_t c[DIM];
+    unpack_cell<DIM>(cw, c);
     const T x = r.f[0], y = r.f[1], z = r.f[2];
-    // y^ey and d/dy; z^ez, z^(ez+2) and their d/dz (ez in {0, 1}); selects, not indexing
+    // y^ey, z^jz, z^(jz+2) and their derivatives: selects, not indexing
     const T y2 = y * y, z2 = z * z;
     const T wy = ey == 0 ? T(1) : ey == 1 ? y : ey == 2 ? y2 : y2 * y;
     const T dwy = ey == 0 ? T(0) : ey == 1 ? T(1) : ey == 2 ? T(2) * y : T(3) * y2;
-    const T wz0 = ez ? z : T(1), wz1 = ez ? z2 * z : z2;
-    const T dwz0 = ez ? T(1) : T(0), dwz1 = ez ? T(3) * z2 : T(2) * z;
-    const T *blk = tab + flat_cell<3>(c, g) * (int64_t)(F * 64);
-    T V[F], Gx = T(0), Gy = T(0), Gz = T(0);
+    const T wza = jz ? z : T(1), wzb = jz ? z2 * z : z2;
+    const T dwza = jz ? T(1) : T(0), dwzb = jz ? T(3) * z2 : T(2) * z;
+    T wt[4] = {T(1), T(1), T(1), T(1)}, dwt[4] = {T(0), T(0), T(0), T(0)};
+    if constexpr (DIM == 4) {
+      const T u = r.f[3], u2 = u * u;
+      wt[1] = u;
+      wt[2] = u2;
+      wt[3] = u2 * u;
+      dwt[1] = T(1);
+      dwt[2] = T(2) * u;
+      dwt[3] = T(3) * u2;
+    }
+    const T *blk = tab + flat_cell<DIM>(c, g) * (int64_t)(F * M);
+    T V[F], G[DIM];
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) G[d] = T(0);
 #pragma unroll
     for (int f = 0; f < F; ++f) {
-      T a0[4], a1[4], v0, d0, v1, d1;
-      load4<T>(blk + f * 64 + j * 4, a0);
-      load4<T>(blk + f * 64 + (j + 8) * 4, a1);
-      horner_x<T>(a0, x, v0, d0);
-      horner_x<T>(a1, x, v1, d1);
-      V[f] = v0 * (wy * wz0) + v1 * (wy * wz1);
-      if ((F != 3) && f == F - 1) {
-        Gx = d0 * (wy * wz0) + d1 * (wy * wz1);
-        Gy = v0 * (dwy * wz0) + v1 * (dwy * wz1);
-        Gz = v0 * (wy * dwz0) + v1 * (wy * dwz1);
+      V[f] = T(0);
+#pragma unroll
+      for (int k = 0; k < NR; ++k) {
+        T a[4], v, dx;
+        load4<T>(blk + f * M + (j + 8 * k) * 4, a);
+        horner_x<T>(a, x, v, dx);
+        const T wz = (k & 1) ? wzb : wza, dwz = (k & 1) ? dwzb : dwza;
+        const T wyz = wy * wz * wt[k >> 1];
+        V[f] += v * wyz;
+        if (GRAD && f == F - 1) {
+          G[0] += dx * wyz;
+          G[1] += v * (dwy * wz * wt[k >> 1]);
+          G[2] += v * (wy * dwz * wt[k >> 1]);
+          if constexpr (DIM == 4) G[3] += v * (wy * wz * dwt[k >> 1]);
+        }
       }
     }
 #pragma unroll
     for (int m = 1; m < 8; m <<= 1) {
 #pragma unroll
       for (int f = 0; f < F; ++f) V[f] += __shfl_xor_sync(gmask, V[f], m);
-      if (F != 3) {
-        Gx += __shfl_xor_sync(gmask, Gx, m);
-        Gy += __shfl_xor_sync(gmask, Gy, m);
-        Gz += __shfl_xor_sync(gmask, Gz, m);
+      if (GRAD) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) G[d] += __shfl_xor_sync(gmask, G[d], m);
       }
     }
     if (j == 0) {
-      double val[F], grad[3] = {0.0, 0.0, 0.0};
-      const T G[3] = {Gx, Gy, Gz};
+      double val[F], grad[DIM];
 #pragma unroll
       for (int f = 0; f < F; ++f) {
         if constexpr (MIXED)
@@ -664,16 +681,16 @@ __global__ void __launch_bounds__(256) eval_tab_coop_kernel(arb_grid g, KParams 
         else
           val[f] = V[f];
       }
-      if (F != 3) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          if constexpr (MIXED)
-            grad[d] = f2d_exact(G[d] * kp.inv_hf[d]);
-          else
-            grad[d] = (double)G[d] * kp.inv_h[d];
-        }
+      for (int d = 0; d < DIM; ++d) {
+        if (!GRAD)
+          grad[d] = 0.0;
+        else if constexpr (MIXED)
+          grad[d] = f2d_exact(G[d] * kp.inv_hf[d]);
+        else
+          grad[d] = (double)G[d] * kp.inv_h[d];
       }
-      write_vals<3, F>(o, i, val, grad);
+      write_vals<DIM, F>(o, i, val, grad);
     }
   }
 }
@@ -685,13 +702,11 @@ static void launch_eval(const arb_grid *g, const KParams &kp, int64_t nq, const 
   const int TE = DIM == 3 ? 256 : 128;
   const unsigned BE = (unsigned)((nq + TE - 1) / TE);
 #define ES(FF, TAB) eval_sorted_kernel<DIM, FF, MIXED, TAB><<<BE, TE, 0, s>>>(*g, kp, nq, *out, w)
-  if (table && DIM == 3) {
+  if (table) {
     const unsigned BT = (unsigned)((nq + TAB_CHUNK - 1) / TAB_CHUNK);
-#define ET(FF) eval_tab_coop_kernel<FF, MIXED><<<BT, 256, 0, s>>>(*g, kp, nq, *out, w)
+#define ET(FF) eval_tab_coop_kernel<DIM, FF, MIXED><<<BT, 256, 0, s>>>(*g, kp, nq, *out, w)
     switch (g->nfield) { case 1: ET(1); break; case 3: ET(3); break; default: ET(4); break; }
 #undef ET
-  } else if (table) {
-    switch (g->nfield) { case 1: ES(1, true); break; case 3: ES(3, true); break; default: ES(4, true); break; }
   } else if (DIM == 3 && MIXED && g->nfield == 4) {
     const unsigned BC = (unsigned)((nq + COOP_CHUNK - 1) / COOP_CHUNK);
     eval_sorted_coop4_kernel<<<BC, 256, 0, s>>>(*g, kp, nq, *out, w);
