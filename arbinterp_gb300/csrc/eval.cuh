@@ -399,6 +399,145 @@ __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, 
   }
 }
 
+// ---- 4D on-the-fly, mixed precision ------------------------------------------
+// The same contraction as eval_otf4 with float32 deltas taken hierarchically:
+// each x-row against its own x-offset-1 point, each row's reference against
+// the (1, 1, k, l) point (along y), those against (1, 1, 1, l) (along z) and
+// those against the cell corner (along t).  Every delta is a difference along
+// one axis, so the float32 rounding in a derivative along x, y or z no longer
+// carries the field's variation along the later axes (the corner deltas did:
+// a strongly t-dependent field cost its spatial gradient accuracy).  Rows,
+// lines and slabs run in the order 1, 0, 2, 3 so that each reference is
+// loaded before it is used; every grid point is loaded once.
+template <int F>
+__device__ __forceinline__ void eval_otf4_mixed(const arb_grid &g, const KParams &kp, const int64_t c[4],
+                                                const float frac[4], double val[F], double grad[4]) {
+  using T = float;
+  const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  T w[4][4], dw[4][4], hb[4][2], dhb[4][2];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    cr_weights<T>(frac[a], w[a]);
+    cr_dweights<T>(frac[a], dw[a]);
+    hermite_slope<T>(frac[a], hb[a], dhb[a]);
+  }
+  const int64_t npts = grid_points(g);
+  const int64_t pref = (((c[3] + 1) * nz + (c[2] + 1)) * ny + (c[1] + 1)) * nx + (c[0] + 1);
+#pragma unroll 1
+  for (int f = 0; f < F; ++f) {
+    const bool gradf = (F != 3) && (f == F - 1);
+    float rhi = 0.f, rlo = 0.f;
+    g32_load<F>(g.grid32, npts, pref, f, rhi, rlo);
+    T V = 0, Vg[4] = {0, 0, 0, 0};
+    T S[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) S[m] = 0;
+    float hl = 0.f, ll = 0.f;  // point (1, 1, 1, l): reference of the z-deltas of slab l
+#pragma unroll
+    for (int li = 0; li < 4; ++li) {
+      const int l = li == 0 ? 1 : (li == 1 ? 0 : li);
+      T Az = 0, Azg[3] = {0, 0, 0};
+      T E2[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) E2[m] = 0;
+#pragma unroll
+      for (int ki = 0; ki < 4; ++ki) {
+        const int k = ki == 0 ? 1 : (ki == 1 ? 0 : ki);
+        T Ay = 0, Ayx = 0, Ayy = 0;
+        T E1[4] = {0, 0, 0, 0};
+        float hj = 0.f, lj = 0.f;  // point (1, 1, k, l): reference of the y-deltas of line (k, l)
+#pragma unroll
+        for (int ji = 0; ji < 4; ++ji) {
+          const int j = ji == 0 ? 1 : (ji == 1 ? 0 : ji);
+          const int64_t p = (((c[3] + l) * nz + (c[2] + k)) * ny + (c[1] + j)) * nx + c[0];
+          float h_[4], l_[4];
+#pragma unroll
+          for (int ii = 0; ii < 4; ++ii) g32_load<F>(g.grid32, npts, p + ii, f, h_[ii], l_[ii]);
+          if (j == 1) {
+            hj = h_[1];
+            lj = l_[1];
+          }
+          T d[4];  // along x, against the row's point at x offset 1
+#pragma unroll
+          for (int ii = 0; ii < 4; ++ii) d[ii] = (h_[ii] - h_[1]) + (l_[ii] - l_[1]);
+          const T dy = (h_[1] - hj) + (l_[1] - lj);  // row reference against (1, 1, k, l)
+          const T ax = (w[0][0] * d[0] + w[0][2] * d[2] + w[0][3] * d[3]) + dy;
+          Ay += w[1][j] * ax;
+          if (gradf) {
+            const T axd = dw[0][0] * d[0] + dw[0][2] * d[2] + dw[0][3] * d[3];
+            Ayx += w[1][j] * axd;
+            Ayy += dw[1][j] * ax;
+          }
+          const T sj = (j >= 2) ? T(0.5) : T(-0.5);
+          E1[0 + 2 * (j & 1)] += sj * (T(0.5) * (d[2] - d[0]));
+          E1[1 + 2 * (j & 1)] += sj * (T(0.5) * d[3]);
+        }
+        if (k == 1) {
+          hl = hj;
+          ll = lj;
+        }
+        const T Ak = Ay + ((hj - hl) + (lj - ll));  // line reference against (1, 1, 1, l)
+        Az += w[2][k] * Ak;
+        if (gradf) {
+          Azg[0] += w[2][k] * Ayx;
+          Azg[1] += w[2][k] * Ayy;
+          Azg[2] += dw[2][k] * Ak;
+        }
+        const T sk = (k >= 2) ? T(0.5) : T(-0.5);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) E2[m + 4 * (k & 1)] += sk * E1[m];
+      }
+      const T Al = Az + ((hl - rhi) + (ll - rlo));  // slab reference against the corner
+      V += w[3][l] * Al;
+      if (gradf) {
+        Vg[0] += w[3][l] * Azg[0];
+        Vg[1] += w[3][l] * Azg[1];
+        Vg[2] += w[3][l] * Azg[2];
+        Vg[3] += dw[3][l] * Al;
+      }
+      const T sl = (l >= 2) ? T(0.5) : T(-0.5);
+#pragma unroll
+      for (int m = 0; m < 8; ++m) S[m + 8 * (l & 1)] += sl * E2[m];
+    }
+    // T_c = S_{c-1} - S_c, contracted with the slope-Hermite tensor
+    T Tc[16];
+    Tc[0] = -S[0];
+#pragma unroll
+    for (int m = 1; m < 16; ++m) Tc[m] = S[m - 1] - S[m];
+    T Cx[8], Cdx[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      Cx[m] = hb[0][0] * Tc[2 * m] + hb[0][1] * Tc[2 * m + 1];
+      Cdx[m] = dhb[0][0] * Tc[2 * m] + dhb[0][1] * Tc[2 * m + 1];
+    }
+    T Cy[4], Cyx[4], Cyy[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      Cy[m] = hb[1][0] * Cx[2 * m] + hb[1][1] * Cx[2 * m + 1];
+      Cyx[m] = hb[1][0] * Cdx[2 * m] + hb[1][1] * Cdx[2 * m + 1];
+      Cyy[m] = dhb[1][0] * Cx[2 * m] + dhb[1][1] * Cx[2 * m + 1];
+    }
+    T Cz[2], Czx[2], Czy[2], Czz[2];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      Cz[m] = hb[2][0] * Cy[2 * m] + hb[2][1] * Cy[2 * m + 1];
+      Czx[m] = hb[2][0] * Cyx[2 * m] + hb[2][1] * Cyx[2 * m + 1];
+      Czy[m] = hb[2][0] * Cyy[2 * m] + hb[2][1] * Cyy[2 * m + 1];
+      Czz[m] = dhb[2][0] * Cy[2 * m] + dhb[2][1] * Cy[2 * m + 1];
+    }
+    const T C = hb[3][0] * Cz[0] + hb[3][1] * Cz[1];
+    val[f] = f2d_exact(rhi + (rlo + (V + C)));
+    if (gradf) {
+      const T G[4] = {Vg[0] + (hb[3][0] * Czx[0] + hb[3][1] * Czx[1]),
+                      Vg[1] + (hb[3][0] * Czy[0] + hb[3][1] * Czy[1]),
+                      Vg[2] + (hb[3][0] * Czz[0] + hb[3][1] * Czz[1]),
+                      Vg[3] + (dhb[3][0] * Cz[0] + dhb[3][1] * Cz[1])};
+#pragma unroll
+      for (int a = 0; a < 4; ++a) grad[a] = f2d_exact(G[a] * kp.inv_hf[a]);
+    }
+  }
+}
+
 // ---- 4D on-the-fly ---------------------------------------------------------
 // value = sum_o W_o(x) f_o  +  sum_c (H_{c+1}(x) - H_c(x)) S_c
 // with W the 4-fold Catmull-Rom tensor, S_c the (1/16) mixed fourth
@@ -411,7 +550,10 @@ __device__ __forceinline__ void eval_otf4(const arb_grid &g, const KParams &kp, 
                                           const typename std::conditional<MIXED, float, double>::type frac[4],
                                           double val[F], double grad[4]) {
   using T = typename std::conditional<MIXED, float, double>::type;
-
+  if constexpr (MIXED) {
+    eval_otf4_mixed<F>(g, kp, c, frac, val, grad);
+    return;
+  }
   const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
   T w[4][4], dw[4][4], hb[4][2], dhb[4][2];
 #pragma unroll

@@ -365,6 +365,25 @@ def test_tensor_core_table_exact_from_deltas_4d(mode):
         assert (err <= bound).all(), (key, (err / np.maximum(bound, 1e-300)).max())
 
 
+def test_quadcubic_mixed_gradient_with_strong_time_variation():
+    """4D mixed on-the-fly gradients against the float64 path on a field that
+    varies far more along t than in space (moving Gaussians with a fast
+    cos(w t) amplitude): float32 deltas taken along one axis at a time keep
+    every component within 6e-7 normwise."""
+    _, quadcubic = _mods()
+    from arbinterp_gb300 import synth
+    f = synth.moving_gaussian_field4(n=(28, 26, 24, 20), h=(0.1, 0.1, 0.1, 0.1), seed=11)
+    o64 = quadcubic(f, "quiet", precision="fp64", strategy="otf")
+    omx = quadcubic(f, "quiet", precision="mixed", strategy="otf")
+    q = synth.uniform_queries([float(v) for v in o64._lo], [float(v) for v in o64._hi], 300_000, 0,
+                              [float(v) for v in o64._h], seed=12)
+    v64, g64 = o64.Query(q.numpy().copy())
+    vmx, gmx = omx.Query(q.numpy().copy())
+    assert (normwise(vmx, v64) <= 2e-7).all()
+    err = normwise(gmx, g64)
+    assert (err <= 6e-7).all(), err
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_bin_once_evaluate_twice(prec):
     """arb_query_bin + arb_query_eval_binned equal the one-call sorted path,
