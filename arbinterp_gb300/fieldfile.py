@@ -55,11 +55,13 @@ def _readers():
 
 
 def _ring(device: torch.device):
+    """(buffers, events, lock) of a device's staging ring; the lock is held
+    for a whole transfer so concurrent callers do not share buffers."""
     key = device.index
     with _ring_lock:
         if key not in _rings:
             bufs = [torch.empty(CHUNK, dtype=torch.uint8, pin_memory=True) for _ in range(RING)]
-            _rings[key] = (bufs, [torch.cuda.Event() for _ in range(RING)])
+            _rings[key] = (bufs, [torch.cuda.Event() for _ in range(RING)], threading.Lock())
         return _rings[key]
 
 
@@ -86,18 +88,21 @@ def _to_device(size: int, fill, device, stream):
     text = torch.empty(_padded(size), dtype=torch.uint8, device=device)
     if size == 0:
         return text, 0
-    bufs, evs = _ring(device)
+    bufs, evs, lock = _ring(device)
     pool = _readers()
-    for k, off in enumerate(range(0, size, CHUNK)):
-        n = min(CHUNK, size - off)
-        slot = k % RING
-        evs[slot].synchronize()               # the copy that last used this buffer is done
-        mv = memoryview(bufs[slot].numpy())[:n]
-        step = max(4 << 20, -(-n // READERS))
-        list(pool.map(lambda a: fill(mv[a:a + step], off + a), range(0, n, step)))
-        with torch.cuda.stream(stream):
-            text[off:off + n].copy_(bufs[slot][:n], non_blocking=True)
-            evs[slot].record(stream)
+    with lock:
+        for k, off in enumerate(range(0, size, CHUNK)):
+            n = min(CHUNK, size - off)
+            slot = k % RING
+            evs[slot].synchronize()           # the copy that last used this buffer is done
+            mv = memoryview(bufs[slot].numpy())[:n]
+            step = max(4 << 20, -(-n // READERS))
+            list(pool.map(lambda a: fill(mv[a:a + step], off + a), range(0, n, step)))
+            with torch.cuda.stream(stream):
+                text[off:off + n].copy_(bufs[slot][:n], non_blocking=True)
+                evs[slot].record(stream)
+        for e in evs:                         # buffers idle before another caller takes the ring
+            e.synchronize()
     return text, size
 
 

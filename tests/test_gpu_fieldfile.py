@@ -144,3 +144,25 @@ def test_non_ascii_and_unsupported_inputs_are_refused(tmp_path):
         genfromtxt(b"1 2\n", delimiter=None)
     with pytest.raises(NotImplementedError):
         genfromtxt(os.path.join(tmp_path, "f.csv.gz"))
+
+
+def test_concurrent_readers():
+    """Two threads reading texts longer than one staging chunk at the same
+    time get the same tables as reading from device-resident text."""
+    import threading
+    from arbinterp_gb300 import fieldfile, genfromtxt, synth
+    texts = [synth.field_csv_text((128, 128, 34), 3, seed=s, device="cuda") for s in (21, 22)]
+    assert all(t.numel() > fieldfile.CHUNK for t in texts)
+    host = [t.cpu().numpy().tobytes() for t in texts]
+    want = [fieldfile.parse_device_text(t, t.numel()).cpu().numpy() for t in texts]
+    got = [None, None]
+
+    def run(k):
+        got[k] = genfromtxt(host[k]).cpu().numpy()
+    th = [threading.Thread(target=run, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for g, w in zip(got, want):
+        _same_bits(g, w)
