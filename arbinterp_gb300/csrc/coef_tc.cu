@@ -94,31 +94,53 @@ __device__ __forceinline__ int scale_exp(float amax) {
   return min(max(eb - 126, -100), 126);
 }
 
-// t -> (h0, h1, h2) with t = h0 + h1 + 2^-22 h2 (see the file comment)
-__device__ __forceinline__ void split3(float t, float &h0, float &h1, float &h2) {
-  h0 = __fadd_rn(__fadd_rn(t, kRound0), -kRound0);
-  const float r = __fadd_rn(t, -h0);
-  h1 = __fadd_rn(__fadd_rn(r, kRound1), -kRound1);
-  h2 = __fmul_rn(__fadd_rn(r, -h1), 4194304.0f);
+// Packed float32 pairs (Blackwell .f32x2): one instruction rounds both
+// components exactly as the scalar operation does.
+#define ARB_F32X2(name, op)                                                                            \
+  __device__ __forceinline__ float2 name(float2 a, float2 b) {                                        \
+    float2 d;                                                                                          \
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t" op      \
+        " rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"                                                  \
+        : "=f"(d.x), "=f"(d.y)                                                                         \
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                                     \
+    return d;                                                                                          \
+  }
+ARB_F32X2(fadd2, "add.rn.f32x2")
+ARB_F32X2(fsub2, "sub.rn.f32x2")
+ARB_F32X2(fmul2, "mul.rn.f32x2")
+#undef ARB_F32X2
+
+// Two values at once: t -> (h0, h1, 2^-SH h2 parts) with t = h0 + h1 + 2^-SH h2;
+// R1 rounds to the h1 grid (3D: 2^-11, SH = 22; 4D: 2^-10, SH = 20).
+__device__ __forceinline__ void split3_pair(float2 t, float r1, float sh, float2 &h0, float2 &h1, float2 &h2) {
+  const float2 R0 = make_float2(kRound0, kRound0), R1 = make_float2(r1, r1);
+  h0 = fsub2(fadd2(t, R0), R0);
+  const float2 r = fsub2(t, h0);
+  h1 = fsub2(fadd2(r, R1), R1);
+  h2 = fmul2(fsub2(r, h1), make_float2(sh, sh));
 }
+
 
 // four points along x of one block line: component f of grid32 (+ lo)
 template <int F>
 __device__ __forceinline__ void load_line(const float *hp, const float *lp, bool has_lo, float rhi, float rlo,
                                           float *d, float &amax) {
 #pragma unroll
-  for (int ox = 0; ox < 4; ++ox) {
-    float vh, vl = 0.f;
+  for (int ox = 0; ox < 4; ox += 2) {
+    float2 vh, vl = make_float2(0.f, 0.f);
     if (F == 1) {
-      const float2 v = __ldg(reinterpret_cast<const float2 *>(hp) + ox);
-      vh = v.x;
-      vl = v.y;
+      const float2 v0 = __ldg(reinterpret_cast<const float2 *>(hp) + ox);  // (hi, lo) points: 8-byte aligned
+      const float2 v1 = __ldg(reinterpret_cast<const float2 *>(hp) + ox + 1);
+      vh = make_float2(v0.x, v1.x);
+      vl = make_float2(v0.y, v1.y);
     } else {
-      vh = __ldg(hp + 4 * ox);
-      if (has_lo) vl = __ldg(lp + ox);
+      vh = make_float2(__ldg(hp + 4 * ox), __ldg(hp + 4 * ox + 4));
+      if (has_lo) vl = make_float2(__ldg(lp + ox), __ldg(lp + ox + 1));
     }
-    d[ox] = (vh - rhi) + (vl - rlo);
-    amax = fmaxf(amax, fabsf(d[ox]));
+    const float2 dd = fadd2(fsub2(vh, make_float2(rhi, rhi)), fsub2(vl, make_float2(rlo, rlo)));
+    d[ox] = dd.x;
+    d[ox + 1] = dd.y;
+    amax = fmaxf(amax, fmaxf(fabsf(dd.x), fabsf(dd.y)));
   }
 }
 
@@ -211,12 +233,12 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
       uint32_t w0[4], w1[4], w2[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        float a0, a1, a2, b0, b1, b2;
-        split3(__fmul_rn(d[ch * 8 + v * 2], c10), a0, a1, a2);
-        split3(__fmul_rn(d[ch * 8 + v * 2 + 1], c10), b0, b1, b2);
-        w0[v] = pack_h2(a0, b0);
-        w1[v] = pack_h2(a1, b1);
-        w2[v] = pack_h2(a2, b2);
+        float2 h0, h1, h2;
+        split3_pair(fmul2(make_float2(d[ch * 8 + v * 2], d[ch * 8 + v * 2 + 1]), make_float2(c10, c10)), kRound1,
+                    4194304.0f, h0, h1, h2);
+        w0[v] = pack_h2(h0.x, h0.y);
+        w1[v] = pack_h2(h1.x, h1.y);
+        w2[v] = pack_h2(h2.x, h2.y);
       }
       const int k = half * 32 + ch * 8;
       *reinterpret_cast<uint4 *>(sm.a + kmaj(row, k, A_SBO)) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
@@ -413,13 +435,15 @@ struct Tc4Smem {
   int32_t bad;
 };
 
-// t -> (h0, h1, h2) with t = h0 + h1 + 2^-20 h2
-__device__ __forceinline__ void split3_4d(float t, float &h0, float &h1, float &h2) {
-  h0 = __fadd_rn(__fadd_rn(t, kRound0), -kRound0);
-  const float r = __fadd_rn(t, -h0);
-  h1 = __fadd_rn(__fadd_rn(r, kRound10), -kRound10);
-  h2 = __fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(r, -h1), 1048576.0f), kRound0), -kRound0);
+// Two values at once: t -> (h0, h1, h2) with t = h0 + h1 + 2^-20 h2, h2 an integer
+__device__ __forceinline__ void split3_4d_pair(float2 t, float2 &h0, float2 &h1, float2 &h2) {
+  const float2 R0 = make_float2(kRound0, kRound0), R10 = make_float2(kRound10, kRound10);
+  h0 = fsub2(fadd2(t, R0), R0);
+  const float2 r = fsub2(t, h0);
+  h1 = fsub2(fadd2(r, R10), R10);
+  h2 = fsub2(fadd2(fmul2(fsub2(r, h1), make_float2(1048576.0f, 1048576.0f)), R0), R0);
 }
+
 }  // namespace
 
 // B = 16 A4 as FP16 in 8 chunks [half][K-chunk] of the no-swizzle K-major
@@ -488,17 +512,19 @@ __global__ void __launch_bounds__(T4_NT, 1) coef4_tc_kernel(const __grid_constan
           for (int oy = 0; oy < 4; ++oy) {
             const int64_t line = (2 * half + ot) * st + oz * sz + oy * sy;
 #pragma unroll
-            for (int ox = 0; ox < 4; ++ox) {
-              float vh, vl2 = 0.f;
+            for (int ox = 0; ox < 4; ox += 2) {
+              float2 vh, vl2 = make_float2(0.f, 0.f);
               if (F == 1) {
-                const float2 v = __ldg(reinterpret_cast<const float2 *>(hb) + line + ox);
-                vh = v.x;
-                vl2 = v.y;
+                const float2 v0 = __ldg(reinterpret_cast<const float2 *>(hb) + line + ox);
+                const float2 v1 = __ldg(reinterpret_cast<const float2 *>(hb) + line + ox + 1);
+                vh = make_float2(v0.x, v1.x);
+                vl2 = make_float2(v0.y, v1.y);
               } else {
-                vh = __ldg(hb + (line + ox) * 4);
-                if (has_lo) vl2 = __ldg(lb + line + ox);
+                vh = make_float2(__ldg(hb + (line + ox) * 4), __ldg(hb + (line + ox + 1) * 4));
+                if (has_lo) vl2 = make_float2(__ldg(lb + line + ox), __ldg(lb + line + ox + 1));
               }
-              amax = fmaxf(amax, fabsf((vh - rhi) + (vl2 - rlo)));
+              const float2 dd = fadd2(fsub2(vh, make_float2(rhi, rhi)), fsub2(vl2, make_float2(rlo, rlo)));
+              amax = fmaxf(amax, fmaxf(fabsf(dd.x), fabsf(dd.y)));
             }
           }
     }
@@ -521,29 +547,31 @@ __global__ void __launch_bounds__(T4_NT, 1) coef4_tc_kernel(const __grid_constan
             for (int l2 = 0; l2 < 2; ++l2) {
               const int64_t line = (2 * half + ot) * st + oz * sz + (oy + l2) * sy;
 #pragma unroll
-              for (int ox = 0; ox < 4; ++ox) {
-                float vh, vl2 = 0.f;
+              for (int ox = 0; ox < 4; ox += 2) {
+                float2 vh, vl2 = make_float2(0.f, 0.f);
                 if (F == 1) {
-                  const float2 v = __ldg(reinterpret_cast<const float2 *>(hb) + line + ox);
-                  vh = v.x;
-                  vl2 = v.y;
+                  const float2 v0 = __ldg(reinterpret_cast<const float2 *>(hb) + line + ox);
+                  const float2 v1 = __ldg(reinterpret_cast<const float2 *>(hb) + line + ox + 1);
+                  vh = make_float2(v0.x, v1.x);
+                  vl2 = make_float2(v0.y, v1.y);
                 } else {
-                  vh = __ldg(hb + (line + ox) * 4);
-                  if (has_lo) vl2 = __ldg(lb + line + ox);
+                  vh = make_float2(__ldg(hb + (line + ox) * 4), __ldg(hb + (line + ox + 1) * 4));
+                  if (has_lo) vl2 = make_float2(__ldg(lb + line + ox), __ldg(lb + line + ox + 1));
                 }
-                d[l2 * 4 + ox] = (vh - rhi) + (vl2 - rlo);
+                const float2 dd = fadd2(fsub2(vh, make_float2(rhi, rhi)), fsub2(vl2, make_float2(rlo, rlo)));
+                d[l2 * 4 + ox] = dd.x;
+                d[l2 * 4 + ox + 1] = dd.y;
               }
             }
           }
           uint32_t w0[4], w1[4], w2[4];
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
-            float a0, a1, a2, b0, b1, b2;
-            split3_4d(__fmul_rn(d[2 * v], c9), a0, a1, a2);
-            split3_4d(__fmul_rn(d[2 * v + 1], c9), b0, b1, b2);
-            w0[v] = pack_h2(a0, b0);
-            w1[v] = pack_h2(a1, b1);
-            w2[v] = pack_h2(a2, b2);
+            float2 h0, h1, h2;
+            split3_4d_pair(fmul2(make_float2(d[2 * v], d[2 * v + 1]), make_float2(c9, c9)), h0, h1, h2);
+            w0[v] = pack_h2(h0.x, h0.y);
+            w1[v] = pack_h2(h1.x, h1.y);
+            w2[v] = pack_h2(h2.x, h2.y);
           }
           const int k = half * 128 + ot * 64 + oz * 16 + oy * 4;  // sample index ox + 4oy + 16oz + 64ot
           *reinterpret_cast<uint4 *>(sm.a + kmaj(row, k, T4_A_SBO)) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
