@@ -501,7 +501,10 @@ __global__ void __launch_bounds__(256) ordered_tile_kernel(const TF *field, int6
   constexpr int NC = DIM + (KIND == ARB_KIND_SCALAR ? 1 : 3);
   if (!w->ok || w->stride[0] == 1 || w->stride[0] == -1) return;
   extern __shared__ __align__(16) unsigned char ot_smem[];
-  TF(*tile)[OT + 1][NC] = reinterpret_cast<TF(*)[OT + 1][NC]>(ot_smem);
+  // one plane per column (structure of arrays): the load phase writes
+  // consecutive words, the write phase reads words 2 (OT + 1) / 2 apart,
+  // both without bank conflicts beyond the two wavefronts 8-byte values need
+  TF(*tile)[OT][OT + 1] = reinterpret_cast<TF(*)[OT][OT + 1]>(ot_smem);
   int64_t nn[DIM], st[DIM];
   int S = 1;
 #pragma unroll
@@ -537,7 +540,10 @@ __global__ void __launch_bounds__(256) ordered_tile_kernel(const TF *field, int6
         int64_t src = 0;
 #pragma unroll
         for (int a = 0; a < DIM; ++a) src += st[a] > 0 ? i[a] * st[a] : (nn[a] - 1 - i[a]) * (-st[a]);
-        load_field_row<TF, NC>(field + src * NC, tile[k][tx]);
+        TF v[NC];
+        load_field_row<TF, NC>(field + src * NC, v);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) tile[c][k][tx] = v[c];
       }
     }
     __syncthreads();
@@ -546,7 +552,9 @@ __global__ void __launch_bounds__(256) ordered_tile_kernel(const TF *field, int6
       i[0] = xt * OT + tx;
       i[S] = stile * OT + k;
       if (i[0] < nn[0] && i[S] < nn[S]) {
-        const TF *row = tile[tx][k];
+        TF row[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) row[c] = tile[c][tx][k];
         int64_t dest = 0;
         bool ok = true;
 #pragma unroll
