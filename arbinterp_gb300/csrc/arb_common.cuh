@@ -156,6 +156,51 @@ __host__ __device__ inline void fast_axis_pairs(FastAxis &f, double lo, double h
 // come from the product's bit pattern with integer operations.  Only when
 // the product lies within 8 ulps of an integer (where multiplying by 1/h
 // and dividing by h could floor differently) is the IEEE division redone.
+// The float64 step of one axis: (q - IntMin) * (1/h), floored, with the
+// reference's own division where the product lands within 8 ulps of an
+// integer.  Out of line, so the float32 fast path never issues these
+// float64-pipe instructions speculatively; it is the main path only for an
+// axis spanning more than 2^20 cells.
+struct AxisStep {
+  int64_t k;
+  float fr;
+};
+
+static __device__ __noinline__ AxisStep axis_step_f64(double q, const FastAxis &ax) {
+  const double d = q - ax.lo;
+  double iu = d * ax.inv_h;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(iu);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  int64_t kk = 0;
+  float fr = 0.f;
+  bool redo = (e > 30);
+  if (e >= -1 && e <= 30) {
+    const int nf = 52 - e;  // 22 .. 53 fraction bits
+    const unsigned long long m = (b & 0xfffffffffffffULL) | (1ULL << 52);
+    const unsigned long long one = 1ULL << nf;
+    const unsigned long long fb = m & (one - 1);
+    kk = (int64_t)(m >> nf);
+    redo = (fb < 8ULL) || (fb > one - 8ULL);
+    // top 24 bits of the fraction, converted exactly, times 2^-24
+    const unsigned f24 = (unsigned)(nf >= 24 ? (fb >> (nf - 24)) : (fb << (24 - nf)));
+    // f24 * 2^-24 exactly, without an int->float conversion instruction
+    const float f23 = __fsub_rn(__uint_as_float(0x4b000000u | (f24 >> 1)), 8388608.f);
+    fr = __fmaf_rn(f23, 2.f, (f24 & 1u) ? 1.f : 0.f) * 5.9604644775390625e-08f;
+  } else if (e < -1) {
+    fr = __double2float_rn(iu);  // iu < 0.5: floor is 0
+  }
+  if (redo) {
+    iu = d / ax.h;
+    const double kf = floor(iu);
+    kk = (int64_t)kf;
+    fr = (float)(iu - kf);
+  }
+  AxisStep r;
+  r.k = kk;
+  r.fr = fr;
+  return r;
+}
+
 template <int DIM>
 __device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const FastAxis *ax,
                                                      const arb_grid &g, float frac[DIM]) {
@@ -210,36 +255,9 @@ __device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const F
         continue;
       }
     }
-    const double d = q - ax[a].lo;
-    double iu = d * ax[a].inv_h;
-    const unsigned long long b = (unsigned long long)__double_as_longlong(iu);
-    const int e = (int)((b >> 52) & 0x7ff) - 1023;
-    int64_t kk = 0;
-    float fr = 0.f;
-    bool redo = (e > 30);
-    if (e >= -1 && e <= 30) {
-      const int nf = 52 - e;  // 22 .. 53 fraction bits
-      const unsigned long long m = (b & 0xfffffffffffffULL) | (1ULL << 52);
-      const unsigned long long one = 1ULL << nf;
-      const unsigned long long fb = m & (one - 1);
-      kk = (int64_t)(m >> nf);
-      redo = (fb < 8ULL) || (fb > one - 8ULL);
-      // top 24 bits of the fraction, converted exactly, times 2^-24
-      const unsigned f24 = (unsigned)(nf >= 24 ? (fb >> (nf - 24)) : (fb << (24 - nf)));
-      // f24 * 2^-24 exactly, without an int->float conversion instruction
-      const float f23 = __fsub_rn(__uint_as_float(0x4b000000u | (f24 >> 1)), 8388608.f);
-      fr = __fmaf_rn(f23, 2.f, (f24 & 1u) ? 1.f : 0.f) * 5.9604644775390625e-08f;
-    } else if (e < -1) {
-      fr = __double2float_rn(iu);  // iu < 0.5: floor is 0
-    }
-    if (redo) {
-      iu = d / ax[a].h;
-      const double kf = floor(iu);
-      kk = (int64_t)kf;
-      fr = (float)(iu - kf);
-    }
-    fl[a] = kk;
-    frac[a] = fr;
+    const AxisStep r = axis_step_f64(q, ax[a]);
+    fl[a] = r.k;
+    frac[a] = r.fr;
   }
 #pragma unroll
   for (int a = 0; a < DIM; ++a) s.fl[a] = fl[a];
@@ -364,11 +382,15 @@ __device__ __forceinline__ void g32_load(const float *g32, int64_t npts, int64_t
 
 // float -> double on the integer pipe (exact for normal numbers and zeros;
 // subnormals, infinities and NaN take the conversion instruction).
+// Rare conversions kept out of line: a call cannot be hoisted, so the common
+// path never issues the float64-pipe instruction speculatively.
+static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
+
 __device__ __forceinline__ double f2d_exact(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xffu;
   if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)u << 32));
-  if (e == 0u || e == 0xffu) return (double)f;
+  if (e == 0u || e == 0xffu) return f2d_slow(f);
   const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
                                ((unsigned long long)(e + 896u) << 52) |
                                ((unsigned long long)(u & 0x7fffffu) << 29);
@@ -378,12 +400,18 @@ __device__ __forceinline__ double f2d_exact(float f) {
 // Split a double into float32 hi = RN(v) and lo = RN(v - hi) with integer
 // operations (bit-identical to the float64-pipe conversions) for
 // 2^-45 <= |v| < 2^127; other magnitudes fall back to the conversions.
+static __device__ __noinline__ float2 split_f32_slow(double v) {
+  const float hi = __double2float_rn(v);
+  return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
 __device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
   const int E = (int)((b >> 52) & 0x7ff);
   if (E < 978 || E > 1023 + 126) {
-    hi = __double2float_rn(v);
-    lo = __double2float_rn(v - (double)hi);
+    const float2 r = split_f32_slow(v);  // out of line: never speculated
+    hi = r.x;
+    lo = r.y;
     return;
   }
   const unsigned long long m = b & 0xfffffffffffffULL;
@@ -392,8 +420,13 @@ __device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
   const bool up = (r > 0x10000000u) || (r == 0x10000000u && (top & 1u));
   const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
   hi = __uint_as_float(sign | ((((unsigned)(E - 1023 + 127)) << 23) + top + (up ? 1u : 0u)));
-  const int rs = up ? (int)r - 0x20000000 : (int)r;   // v - hi in units of 2^(E-1075)
-  const float l = __int2float_rn(rs) * __uint_as_float(((unsigned)(E - 948)) << 23);
+  const int rs = up ? (int)r - 0x20000000 : (int)r;   // v - hi in units of 2^(E-1075), |rs| <= 2^28
+  // RN(rs) without the int->float conversion instruction: rs = a 2^12 + b
+  // with both halves exact as magic-number floats, one rounded add
+  const int a = rs >> 12, bq = rs & 0xfff;
+  const float fa = __fsub_rn(__int_as_float(0x4b400000 + a), 12582912.f);
+  const float fb = __fsub_rn(__int_as_float(0x4b400000 + bq), 12582912.f);
+  const float l = __fadd_rn(__fmul_rn(fa, 4096.f), fb) * __uint_as_float(((unsigned)(E - 948)) << 23);
   lo = sign ? -l : l;
 }
 
