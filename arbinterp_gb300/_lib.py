@@ -67,7 +67,7 @@ SIGNATURES = {
                                         C.POINTER(ArbQueryOut), _P, C.c_size_t, _P, _P]),
     "arb_adjoint": (C.c_int, [C.POINTER(ArbGrid), _I32, _P, _I64, _I64, _P, _P, _P, _P, _P, _P]),
     "arb_grid_set_values": (C.c_int, [C.POINTER(ArbGrid), _P, _I32, _P, _P, _P]),
-    "arb_batched_launch": (C.c_int, [_P, _I32, _P, _P, _I64, _I32, _I32, _P, _I64, _I32,
+    "arb_batched_launch": (C.c_int, [_P, _I32, _I32, _P, _P, _I64, _I32, _I32, _P, _I64, _I32,
                                      C.POINTER(ArbQueryOut), _P, _P, _P]),
     "arb_query_bin": (C.c_int, [C.POINTER(ArbGrid), _I32, _P, _I64, _I64, _I32, C.POINTER(ArbQueryOut),
                                 _P, C.c_size_t, _P, _P]),

@@ -95,7 +95,7 @@ class BatchedTricubic:
         p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
         out = ArbQueryOut(p(comps), p(norms), p(grads), None, None, None)
         prec = _lib.PREC_MIXED if self.precision == "mixed" else _lib.PREC_FP64
-        check(lib().arb_batched_launch(self._desc.data_ptr(), len(self.interps), q_off.data_ptr(),
+        check(lib().arb_batched_launch(self._desc.data_ptr(), len(self.interps), self.F, q_off.data_ptr(),
                                        t_off.data_ptr(), ntiles, tile_rows, prec, q.data_ptr(), q.shape[1],
                                        0, out, self._counter.data_ptr(), self._status.data_ptr(), _stream()),
               "arb_batched_launch")

@@ -53,8 +53,12 @@ __device__ __forceinline__ void batched_rows(const arb_grid &g, const KParams &k
   }
 }
 
-template <bool MIXED>
-__global__ void __launch_bounds__(256) batched_kernel(const arb_grid *grids, int32_t nfields,
+// FF: the fields' common count (1, 3, 4), compiled alone (no registers or
+// spills for the other counts' paths); 0 dispatches on each descriptor's
+// count.  Mixed precision: two CTAs per SM (the register file caps the
+// on-the-fly evaluator at 16 warps per SM).
+template <bool MIXED, int FF>
+__global__ void __launch_bounds__(256, MIXED ? 2 : 1) batched_kernel(const arb_grid *grids, int32_t nfields,
                                                       const int64_t *q_off, const int64_t *tile_off,
                                                       int64_t ntiles, int32_t tile_rows, double *q,
                                                       int64_t qs, int wb, arb_query_out o,
@@ -87,10 +91,14 @@ __global__ void __launch_bounds__(256) batched_kernel(const arb_grid *grids, int
     const int32_t f = sfield;
     const int64_t q0 = q_off[f] + (tile - tile_off[f]) * tile_rows;
     const int64_t q1 = min(q0 + (int64_t)tile_rows, q_off[f + 1]);
-    switch (sg.nfield) {
-      case 1: batched_rows<1, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
-      case 3: batched_rows<3, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
-      default: batched_rows<4, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
+    if constexpr (FF != 0) {
+      batched_rows<FF, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status);
+    } else {
+      switch (sg.nfield) {
+        case 1: batched_rows<1, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
+        case 3: batched_rows<3, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
+        default: batched_rows<4, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
+      }
     }
     __syncthreads();  // the descriptor in shared memory is replaced next round
   }
@@ -111,13 +119,14 @@ static int sm_count() {
 
 using namespace arb;
 
-extern "C" int arb_batched_launch(const arb_grid *grids, int32_t nfields, const int64_t *q_off,
+extern "C" int arb_batched_launch(const arb_grid *grids, int32_t nfields, int32_t nfield, const int64_t *q_off,
                                   const int64_t *tile_off, int64_t ntiles, int32_t tile_rows,
                                   int32_t precision, double *q, int64_t q_stride, int32_t q_writeback,
                                   const arb_query_out *out, unsigned long long *counter, int32_t *status,
                                   arb_stream_t stream) {
   if (!grids || nfields <= 0 || !q_off || !tile_off || !out || !counter || tile_rows <= 0 || q_stride < 3)
     return ARB_ERR_INVALID;
+  if (nfield != 0 && nfield != 1 && nfield != 3 && nfield != 4) return ARB_ERR_INVALID;
   if (out->oob_rows && !out->oob_count) return ARB_ERR_INVALID;
   if (ntiles == 0) return ARB_OK;
   cudaStream_t s = (cudaStream_t)stream;
@@ -127,11 +136,16 @@ extern "C" int arb_batched_launch(const arb_grid *grids, int32_t nfields, const 
   const int per_sm = 8;
   int64_t grid = (int64_t)sm_count() * per_sm;
   if (grid > ntiles) grid = ntiles;
-  if (precision == ARB_PREC_MIXED)
-    batched_kernel<true><<<(unsigned)grid, 256, 0, s>>>(grids, nfields, q_off, tile_off, ntiles, tile_rows, q,
-                                                        q_stride, q_writeback, *out, counter, status);
-  else
-    batched_kernel<false><<<(unsigned)grid, 256, 0, s>>>(grids, nfields, q_off, tile_off, ntiles, tile_rows, q,
-                                                         q_stride, q_writeback, *out, counter, status);
+#define BK(MX, FF)                                                                                          \
+  batched_kernel<MX, FF><<<(unsigned)grid, 256, 0, s>>>(grids, nfields, q_off, tile_off, ntiles, tile_rows, q, \
+                                                        q_stride, q_writeback, *out, counter, status)
+  const bool mixed = precision == ARB_PREC_MIXED;
+  switch (nfield) {
+    case 1: if (mixed) BK(true, 1); else BK(false, 1); break;
+    case 3: if (mixed) BK(true, 3); else BK(false, 3); break;
+    case 4: if (mixed) BK(true, 4); else BK(false, 4); break;
+    default: if (mixed) BK(true, 0); else BK(false, 0); break;
+  }
+#undef BK
   return launch_status();
 }

@@ -234,8 +234,11 @@ int arb_grid_set_values(const arb_grid *g, const void *values, int32_t values_f3
  *      doubles per row); field f owns rows [q_off[f], q_off[f+1]) and tiles
  *      [tile_off[f], tile_off[f+1]) of tile_rows rows (device arrays of
  *      nfields+1).  Outputs are concatenated the same way.  counter is one
- *      device word of scratch (reset here).  Capturable in a CUDA graph. */
-int arb_batched_launch(const arb_grid *grids, int32_t nfields, const int64_t *q_off,
+ *      device word of scratch (reset here).  nfield: the fields' common
+ *      count F (1, 3 or 4) when every descriptor has it, which selects a
+ *      kernel compiled for that count alone (fewer registers, more CTAs per
+ *      SM); 0 when the counts differ.  Capturable in a CUDA graph. */
+int arb_batched_launch(const arb_grid *grids, int32_t nfields, int32_t nfield, const int64_t *q_off,
                        const int64_t *tile_off, int64_t ntiles, int32_t tile_rows, int32_t precision,
                        double *q, int64_t q_stride, int32_t q_writeback, const arb_query_out *out,
                        unsigned long long *counter, int32_t *status, arb_stream_t stream);
