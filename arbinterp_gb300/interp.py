@@ -656,7 +656,24 @@ class _Interpolant:
             return c, nv, gv
         return nv, gv
 
-    def trajectories(self, x0, v0, dt, nsteps, coef=-1.0, gravity=(0.0, 0.0, 0.0), record_every=0):
+    def _morton_order(self, x):
+        """Permutation sorting positions x (N, 3) along a Z-order curve over
+        the interpolation box (10 bits per axis): particles in a warp then
+        gather neighbouring grid points.  Non-finite rows sort last."""
+        lo = torch.tensor([float(v) for v in self._lo], dtype=torch.float64, device=x.device)
+        hi = torch.tensor([float(v) for v in self._hi], dtype=torch.float64, device=x.device)
+        u = ((x - lo) / (hi - lo)).clamp(0.0, 1.0)
+        u = torch.nan_to_num(u, nan=1.0)
+        k = (u * 1023.0).to(torch.int64)
+        key = torch.zeros(x.shape[0], dtype=torch.int64, device=x.device)
+        for b in range(10):
+            for a in range(3):
+                key |= ((k[:, a] >> b) & 1) << (3 * b + a)
+        key = torch.where(torch.isfinite(x).all(1), key, torch.full_like(key, 1 << 31))
+        return torch.argsort(key)
+
+    def trajectories(self, x0, v0, dt, nsteps, coef=-1.0, gravity=(0.0, 0.0, 0.0), record_every=0,
+                     spatial_sort=True):
         """Integrate particles through the field on the device (3D, scalar,
         norm or both mode): fourth-order Runge-Kutta on x' = v,
         v' = coef * grad f(x) + gravity, with f the interpolated scalar or |B|
@@ -666,7 +683,8 @@ class _Interpolant:
         nsteps steps of dt, and with record_every > 0 also the path
         (nsteps // record_every, N, 6) of (x, v) states; arrays of the input
         kind.  Particles that leave the interpolation volume come back NaN;
-        `self.lost` counts them."""
+        `self.lost` counts them.  spatial_sort: integrate in Z-order (the
+        results are returned in the caller's order either way)."""
         if self._dim != 3:
             raise NotImplementedError("trajectories are built for 3D fields")
         if self._kind == _lib.KIND_VECTOR:
@@ -678,7 +696,9 @@ class _Interpolant:
         if x.shape != v.shape:
             raise ValueError("x0 and v0 must have the same shape")
         n = x.shape[0]
-        state = torch.cat([x, v], 1).contiguous()
+        perm = self._morton_order(x) if spatial_sort and n > 1 else None
+        state = torch.cat([x, v], 1)
+        state = (state[perm] if perm is not None else state).contiguous()
         nrec = nsteps // record_every if record_every > 0 else 0
         path = torch.empty((nrec, n, 6), dtype=torch.float64, device=dev) if nrec else None
         lost = torch.zeros(1, dtype=torch.int64, device=dev)
@@ -688,6 +708,14 @@ class _Interpolant:
                                          grav, _ptr(path), int(record_every) if nrec else 0, lost.data_ptr(),
                                          _stream()), "arb_rk4_trajectories")
         self.lost = int(lost.item())
+        if perm is not None:  # back to the caller's order
+            st = torch.empty_like(state)
+            st[perm] = state
+            state = st
+            if nrec:
+                pt = torch.empty_like(path)
+                pt[:, perm] = path
+                path = pt
         out = [state[:, :3], state[:, 3:]] + ([path] if nrec else [])
         if not on_dev:
             out = [t.cpu().numpy() for t in out]

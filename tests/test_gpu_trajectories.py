@@ -95,3 +95,23 @@ def test_trajectories_device_tensors_and_vector_mode():
     gv = tricubic(f, "quiet", mode="vector")
     with pytest.raises(ValueError):
         gv.trajectories(x0.cpu().numpy(), v0.cpu().numpy(), 0.01, 5)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_spatial_sort_changes_nothing(prec):
+    """Integrating in Z-order returns the very same states, path and lost
+    count in the caller's order as integrating in the given order."""
+    from arbinterp_gb300 import tricubic
+    f, kw = _setup("both")
+    g = tricubic(f, "quiet", precision=prec, **kw)
+    rng = np.random.default_rng(9)
+    lo, hi = np.array(g._lo, float), np.array(g._hi, float)
+    x0 = lo + (hi - lo) * rng.uniform(0.05, 0.95, (3000, 3))
+    v0 = (hi - lo) * rng.uniform(-0.2, 0.2, (3000, 3))
+    x0[17] = np.nan
+    a = g.trajectories(x0, v0, 0.05, 30, coef=-1e-3, record_every=10)
+    la = g.lost
+    b = g.trajectories(x0, v0, 0.05, 30, coef=-1e-3, record_every=10, spatial_sort=False)
+    assert g.lost == la and la > 1
+    for p, q in zip(a, b):
+        assert np.array_equal(p, q, equal_nan=True)
