@@ -348,10 +348,15 @@ constexpr int TILE_PTS = TILE_EDGE * TILE_EDGE * TILE_EDGE;
 
 template <int F>
 struct BinTile;
+// hi planes are 124 points apart (121 used): 124 * 16 B = 1984 B is 64 B
+// modulo the 128-byte bank cycle, so a query's x-rows in planes k and k+1
+// (read by one 8-thread phase of a 128-bit load) fall on complementary banks.
+constexpr int HI_PLANE = 124;
+constexpr int HI_PTS = TILE_EDGE * HI_PLANE;
 template <>
 struct BinTile<4> {          // (hi_x, hi_y, hi_z, hi_n) and lo_n per point
-  float4 hi[TILE_PTS];
-  float lo[TILE_PTS];
+  float4 hi[HI_PTS];         // [z][HI_PLANE] with rows of TILE_EDGE points
+  float lo[TILE_PTS];        // [z][y][x], unpadded
 };
 template <>
 struct BinTile<1> {          // (hi, lo) per point
@@ -399,7 +404,8 @@ __device__ __forceinline__ void load_bin_tile(const arb_grid &g, const BinGeom &
     if (x >= nx || y >= ny || z >= nz) continue;
     const int64_t p = (z * ny + y) * nx + x;
     if (F == 4) {
-      cp_async16(&reinterpret_cast<BinTile<4> &>(t).hi[e], reinterpret_cast<const float4 *>(g.grid32) + p);
+      cp_async16(&reinterpret_cast<BinTile<4> &>(t).hi[lz * HI_PLANE + ly * TILE_EDGE + lx],
+                 reinterpret_cast<const float4 *>(g.grid32) + p);
       cp_async4(&reinterpret_cast<BinTile<4> &>(t).lo[e], g.grid32 + npts * 4 + p);
     } else {
       cp_async8(&reinterpret_cast<BinTile<1> &>(t).v[e], reinterpret_cast<const float2 *>(g.grid32) + p);
@@ -424,8 +430,10 @@ __global__ void __launch_bounds__(256, 4) eval_bin_kernel(arb_grid g, KParams kp
   extern __shared__ __align__(16) unsigned char bin_smem[];
   BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(bin_smem);
   const int lane = threadIdx.x & 31;
-  const int p = lane & 3;
-  const unsigned mask = 0xfu << (lane & 28);
+  const int g8 = lane & 7;        // lane within the query's group; also the output column it writes
+  const int p = lane & 3;         // x offset in the 4x4x4 block
+  const int h = g8 >> 2;          // z parity: this lane reads planes h and h + 2
+  const unsigned mask = 0xffu << (lane & 24);
   const int64_t nbins = bg.nbins;
   int stage = 0;
   int64_t b = blockIdx.x;
@@ -446,11 +454,13 @@ __global__ void __launch_bounds__(256, 4) eval_bin_kernel(arb_grid g, KParams kp
       int64_t og[3];
       bin_origin(b, bg, og);
       if (F == 4) {
-        // 4 lanes per query, lane p owning x offset p of every block row; the
-        // next record is loaded while this one is evaluated
+        // 8 lanes per query: lane (p, h) owns x offset p of the rows in
+        // planes h and h + 2, so each 8-thread phase of a 128-bit shared load
+        // reads one query's two x-rows on complementary banks.  The next
+        // record is loaded while this one is evaluated.
         const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
-        const int64_t tstep = blockDim.x >> 2;
-        int64_t t = t0 + (threadIdx.x >> 2);
+        const int64_t tstep = blockDim.x >> 3;
+        int64_t t = t0 + (threadIdx.x >> 3);
         QRec<float> rnext;
         if (t < t1) rnext = recs[t];
         for (; t < t1; t += tstep) {
@@ -459,7 +469,9 @@ __global__ void __launch_bounds__(256, 4) eval_bin_kernel(arb_grid g, KParams kp
           const int64_t i = r.row;
           int64_t c[3];
           unpack_cell<3>(r.cell, c);
-          const int lp = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));
+          const int cx = (int)(c[0] - og[0]), cy = (int)(c[1] - og[1]), cz = (int)(c[2] - og[2]);
+          const int lph = cz * HI_PLANE + cy * TILE_EDGE + cx;     // block corner in hi
+          const int lpl = (cz * TILE_EDGE + cy) * TILE_EDGE + cx;  // block corner in lo
           const float fx = r.f[0], fy = r.f[1], fz = r.f[2];
           float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
           cr_weights<float>(fx, wx);
@@ -468,70 +480,72 @@ __global__ void __launch_bounds__(256, 4) eval_bin_kernel(arb_grid g, KParams kp
           cr_dweights<float>(fy, dy);
           cr_weights<float>(fz, wz);
           cr_dweights<float>(fz, dz);
-          const int lref = lp + TILE_EDGE * TILE_EDGE + TILE_EDGE + 1;
-          const float nref = reinterpret_cast<const BinTile<4> &>(T).hi[lref].w;
-          const float rlo = reinterpret_cast<const BinTile<4> &>(T).lo[lref];
+          const float nref = reinterpret_cast<const BinTile<4> &>(T).hi[lph + HI_PLANE + TILE_EDGE + 1].w;
+          const float rlo = reinterpret_cast<const BinTile<4> &>(T).lo[lpl + TILE_EDGE * TILE_EDGE + TILE_EDGE + 1];
+          // this lane's weights, selected in registers
+          const float wzk[2] = {h ? wz[1] : wz[0], h ? wz[3] : wz[2]};
+          const float dzk[2] = {h ? dz[1] : dz[0], h ? dz[3] : dz[2]};
+          const float wxp = (p & 2) ? ((p & 1) ? wx[3] : wx[2]) : ((p & 1) ? wx[1] : wx[0]);
+          const float dxp = (p & 2) ? ((p & 1) ? dx[3] : dx[2]) : ((p & 1) ? dx[1] : dx[0]);
           // Components (values only) accumulate raw float32 values; |B|
           // accumulates deltas to the corner so its derivatives keep full
           // relative precision.  y first, then z: d/dz reuses the layer sums.
           float2 Sxy = make_float2(0.f, 0.f), Szn = make_float2(0.f, 0.f);
           float Gy = 0.f, Gz = 0.f;
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
+          for (int kk = 0; kk < 2; ++kk) {
+            const int k = 2 * kk + h;
             float2 axy = make_float2(0.f, 0.f), azn = make_float2(0.f, 0.f);
             float gy = 0.f;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-              const int e = lp + (k * TILE_EDGE + j) * TILE_EDGE + p;
-              const float4 v = reinterpret_cast<const BinTile<4> &>(T).hi[e];
-              const float dn = (v.w - nref) + (reinterpret_cast<const BinTile<4> &>(T).lo[e] - rlo);
+              const float4 v = reinterpret_cast<const BinTile<4> &>(T).hi[lph + k * HI_PLANE + j * TILE_EDGE + p];
+              const float lo = reinterpret_cast<const BinTile<4> &>(T).lo[lpl + (k * TILE_EDGE + j) * TILE_EDGE + p];
+              const float dn = (v.w - nref) + (lo - rlo);
               const float2 wj = make_float2(wy[j], wy[j]);
               axy = ffma2(wj, make_float2(v.x, v.y), axy);
               azn = ffma2(wj, make_float2(v.z, dn), azn);
               gy += dy[j] * dn;
             }
-            const float2 wk = make_float2(wz[k], wz[k]);
+            const float2 wk = make_float2(wzk[kk], wzk[kk]);
             Sxy = ffma2(wk, axy, Sxy);
             Szn = ffma2(wk, azn, Szn);
-            Gy += wz[k] * gy;
-            Gz += dz[k] * azn.y;
+            Gy += wzk[kk] * gy;
+            Gz += dzk[kk] * azn.y;
           }
-          const float Sn = Szn.y;
-          float Vx = wx[p] * Sxy.x, Vy = wx[p] * Sxy.y, Vz = wx[p] * Szn.x, Vn = wx[p] * Sn;
-          float Gx = dx[p] * Sn;
-          Gy *= wx[p];
-          Gz *= wx[p];
+          // Reduce-scatter over the 8 lanes of the group (butterfly on lane
+          // bits 2, 1, 0): lane g8 ends with the sum of output column g8 of
+          // (Vx, Vy, Vz, Vn, Gx, Gy, Gz, 0).
+          float u[4];
+          {
+            const float v8[8] = {wxp * Sxy.x, wxp * Sxy.y, wxp * Szn.x, wxp * Szn.y,
+                                 dxp * Szn.y, wxp * Gy, wxp * Gz, 0.f};
 #pragma unroll
-          for (int off = 1; off <= 2; off <<= 1) {
-            Vx += __shfl_xor_sync(mask, Vx, off);
-            Vy += __shfl_xor_sync(mask, Vy, off);
-            Vz += __shfl_xor_sync(mask, Vz, off);
-            Vn += __shfl_xor_sync(mask, Vn, off);
-            Gx += __shfl_xor_sync(mask, Gx, off);
-            Gy += __shfl_xor_sync(mask, Gy, off);
-            Gz += __shfl_xor_sync(mask, Gz, off);
+            for (int m = 0; m < 4; ++m) {
+              const float send = h ? v8[m] : v8[m + 4];
+              u[m] = (h ? v8[m + 4] : v8[m]) + __shfl_xor_sync(mask, send, 4);
+            }
           }
-          const double nv = f2d_exact(nref + (rlo + Vn));
+          const bool b1 = (p & 2) != 0, b0 = (p & 1) != 0;
+          float u2[2];
+#pragma unroll
+          for (int m = 0; m < 2; ++m) {
+            const float send = b1 ? u[m] : u[m + 2];
+            u2[m] = (b1 ? u[m + 2] : u[m]) + __shfl_xor_sync(mask, send, 2);
+          }
+          const float val = (b0 ? u2[1] : u2[0]) + __shfl_xor_sync(mask, b0 ? u2[0] : u2[1], 1);
+          // column g8 as the caller's float64
+          const float ih = g8 == 4 ? kp.inv_hf[0] : (g8 == 5 ? kp.inv_hf[1] : kp.inv_hf[2]);
+          const float x = g8 == 3 ? nref + (rlo + val) : (g8 >= 4 ? val * ih : val);
+          const double out = g8 == 7 ? 0.0 : f2d_exact(x);
           if (interleaved_rows<3, 4>(o)) {
-            if (p == 0)
-              st_v4(o.comps + i * 8, f2d_exact(Vx), f2d_exact(Vy), f2d_exact(Vz), nv);
-            else if (p == 2)
-              st_v4(o.comps + i * 8 + 4, f2d_exact(Gx * kp.inv_hf[0]), f2d_exact(Gy * kp.inv_hf[1]),
-                    f2d_exact(Gz * kp.inv_hf[2]), 0.0);
-          } else if (p == 0) {
-            if (o.comps) {
-              o.comps[i * o.comps_stride + 0] = f2d_exact(Vx);
-              o.comps[i * o.comps_stride + 1] = f2d_exact(Vy);
-              o.comps[i * o.comps_stride + 2] = f2d_exact(Vz);
-            }
-          } else if (p == 1) {
-            if (o.norms) o.norms[i * o.norms_stride] = nv;
-          } else if (p == 2) {
-            if (o.grads) {
-              o.grads[i * o.grads_stride + 0] = f2d_exact(Gx * kp.inv_hf[0]);
-              o.grads[i * o.grads_stride + 1] = f2d_exact(Gy * kp.inv_hf[1]);
-              o.grads[i * o.grads_stride + 2] = f2d_exact(Gz * kp.inv_hf[2]);
-            }
+            o.comps[i * 8 + g8] = out;      // a group writes its 64-byte row
+          } else if (g8 < 3) {
+            if (o.comps) o.comps[i * o.comps_stride + g8] = out;
+          } else if (g8 == 3) {
+            if (o.norms) o.norms[i * o.norms_stride] = out;
+          } else if (g8 < 7) {
+            if (o.grads) o.grads[i * o.grads_stride + (g8 - 4)] = out;
           }
         }
       }
