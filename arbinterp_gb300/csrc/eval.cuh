@@ -408,12 +408,25 @@ __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, 
 // carries the field's variation along the later axes (the corner deltas did:
 // a strongly t-dependent field cost its spatial gradient accuracy).  Rows,
 // lines and slabs run in the order 1, 0, 2, 3 so that each reference is
-// loaded before it is used; every grid point is loaded once.
-template <int F>
-__device__ __forceinline__ void eval_otf4_mixed(const arb_grid &g, const KParams &kp, const int64_t c[4],
-                                                const float frac[4], double val[F], double grad[4]) {
+// loaded before it is used; every grid point is loaded once.  BLK says where
+// the 4x4x4x4 block is read from: at(i, j, k, l) is the index of block point
+// (i, j, k, l) and load<F>(index, f, hi, lo) its (hi, lo) of field f.
+struct Grid32Block {  // the mixed grid in global memory
+  const float *g32;
+  int64_t npts, sy, sz, st, base;  // strides of y, z, t; index of the block corner
+  __device__ __forceinline__ int64_t at(int i, int j, int k, int l) const {
+    return base + l * st + k * sz + j * sy + i;
+  }
+  template <int F>
+  __device__ __forceinline__ void load(int64_t p, int f, float &hi, float &lo) const {
+    g32_load<F>(g32, npts, p, f, hi, lo);
+  }
+};
+
+template <int F, class BLK>
+__device__ __forceinline__ void eval_otf4_mixed_block(const BLK &blk, const KParams &kp, const float frac[4],
+                                                      double val[F], double grad[4]) {
   using T = float;
-  const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
   T w[4][4], dw[4][4], hb[4][2], dhb[4][2];
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
@@ -421,13 +434,12 @@ __device__ __forceinline__ void eval_otf4_mixed(const arb_grid &g, const KParams
     cr_dweights<T>(frac[a], dw[a]);
     hermite_slope<T>(frac[a], hb[a], dhb[a]);
   }
-  const int64_t npts = grid_points(g);
-  const int64_t pref = (((c[3] + 1) * nz + (c[2] + 1)) * ny + (c[1] + 1)) * nx + (c[0] + 1);
+  const auto pref = blk.at(1, 1, 1, 1);
 #pragma unroll 1
   for (int f = 0; f < F; ++f) {
     const bool gradf = (F != 3) && (f == F - 1);
     float rhi = 0.f, rlo = 0.f;
-    g32_load<F>(g.grid32, npts, pref, f, rhi, rlo);
+    blk.template load<F>(pref, f, rhi, rlo);
     T V = 0, Vg[4] = {0, 0, 0, 0};
     T S[16];
 #pragma unroll
@@ -449,10 +461,10 @@ __device__ __forceinline__ void eval_otf4_mixed(const arb_grid &g, const KParams
 #pragma unroll
         for (int ji = 0; ji < 4; ++ji) {
           const int j = ji == 0 ? 1 : (ji == 1 ? 0 : ji);
-          const int64_t p = (((c[3] + l) * nz + (c[2] + k)) * ny + (c[1] + j)) * nx + c[0];
+          const auto p = blk.at(0, j, k, l);
           float h_[4], l_[4];
 #pragma unroll
-          for (int ii = 0; ii < 4; ++ii) g32_load<F>(g.grid32, npts, p + ii, f, h_[ii], l_[ii]);
+          for (int ii = 0; ii < 4; ++ii) blk.template load<F>(p + ii, f, h_[ii], l_[ii]);
           if (j == 1) {
             hj = h_[1];
             lj = l_[1];
@@ -536,6 +548,20 @@ __device__ __forceinline__ void eval_otf4_mixed(const arb_grid &g, const KParams
       for (int a = 0; a < 4; ++a) grad[a] = f2d_exact(G[a] * kp.inv_hf[a]);
     }
   }
+}
+
+template <int F>
+__device__ __forceinline__ void eval_otf4_mixed(const arb_grid &g, const KParams &kp, const int64_t c[4],
+                                                const float frac[4], double val[F], double grad[4]) {
+  const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
+  Grid32Block blk;
+  blk.g32 = g.grid32;
+  blk.npts = grid_points(g);
+  blk.sy = nx;
+  blk.sz = nx * ny;
+  blk.st = nx * ny * nz;
+  blk.base = ((c[3] * nz + c[2]) * ny + c[1]) * nx + c[0];
+  eval_otf4_mixed_block<F>(blk, kp, frac, val, grad);
 }
 
 // ---- 4D on-the-fly ---------------------------------------------------------

@@ -592,6 +592,136 @@ static bool launch_eval_bin(const arb_grid *g, const KParams &kp, const BinGeom 
   return true;
 }
 
+// ---- bin-staged evaluation (4D, mixed, one scalar field, 4^4-cell bins) -------
+// As eval_bin in 3D: one CTA per bin (round-robin), the bin's 7^4-point
+// footprint of (hi, lo) pairs copied into shared memory with cp.async and
+// double-buffered, one thread per query evaluating eval_otf4_mixed_block on
+// the staged block.  From global memory each thread's 8-byte loads touch a
+// different 128-byte line per instruction and the kernel was L1-bound; shared
+// memory serves a warp's 32 scattered 8-byte loads in a few wavefronts.
+constexpr int BIN4_EDGE = 4;
+constexpr int TILE4_EDGE = BIN4_EDGE + 3;
+constexpr int TILE4_PTS = TILE4_EDGE * TILE4_EDGE * TILE4_EDGE * TILE4_EDGE;
+constexpr int BIN4_THREADS = 128;
+
+struct BinTile4 {
+  float2 v[TILE4_PTS];  // [t][z][y][x] (hi, lo)
+};
+
+struct TileBlock4 {  // a 4x4x4x4 block inside a staged tile
+  const float2 *v;
+  int base;  // tile index of the block corner
+  __device__ __forceinline__ int at(int i, int j, int k, int l) const {
+    return base + ((l * TILE4_EDGE + k) * TILE4_EDGE + j) * TILE4_EDGE + i;
+  }
+  template <int F>
+  __device__ __forceinline__ void load(int p, int, float &hi, float &lo) const {
+    const float2 x = v[p];
+    hi = x.x;
+    lo = x.y;
+  }
+};
+
+__device__ __forceinline__ void bin_origin4(int64_t b, const BinGeom &bg, int64_t o[4]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    o[a] = (b % bg.nb[a]) * BIN4_EDGE;
+    b /= bg.nb[a];
+  }
+  o[3] = b * BIN4_EDGE;
+}
+
+__device__ __forceinline__ void load_bin_tile4(const arb_grid &g, const BinGeom &bg, int64_t b, BinTile4 &t) {
+  int64_t o[4];
+  bin_origin4(b, bg, o);
+  const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2], nt = g.n[3];
+  const float2 *g2 = reinterpret_cast<const float2 *>(g.grid32);
+  for (int e = threadIdx.x; e < TILE4_PTS; e += blockDim.x) {
+    int r = e;
+    const int lx = r % TILE4_EDGE;
+    r /= TILE4_EDGE;
+    const int ly = r % TILE4_EDGE;
+    r /= TILE4_EDGE;
+    const int lz = r % TILE4_EDGE, lt = r / TILE4_EDGE;
+    const int64_t x = o[0] + lx, y = o[1] + ly, z = o[2] + lz, tt = o[3] + lt;
+    if (x >= nx || y >= ny || z >= nz || tt >= nt) continue;
+    cp_async8(&t.v[e], g2 + ((tt * nz + z) * ny + y) * nx + x);
+  }
+}
+
+__global__ void __launch_bounds__(BIN4_THREADS) eval_bin4_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
+                                                                 arb_query_out o, SortedWork w) {
+  extern __shared__ __align__(16) unsigned char bin4_smem[];
+  BinTile4 *tiles = reinterpret_cast<BinTile4 *>(bin4_smem);
+  const int64_t nbins = bg.nbins;
+  const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
+  int stage = 0;
+  int64_t b = blockIdx.x;
+  // after placement hist[b] is the end of bin b; bins with no query need no copy
+  auto bin_begin = [&](int64_t bb) { return bb > 0 ? (int64_t)w.hist[bb - 1] : (int64_t)0; };
+  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb] - bin_begin(bb) : 0; };
+  if (count(b) > 0) load_bin_tile4(g, bg, b, tiles[0]);
+  cp_async_commit();
+  for (; b < nbins; b += gridDim.x) {
+    const int64_t bn = b + gridDim.x;
+    if (count(bn) > 0) load_bin_tile4(g, bg, bn, tiles[stage ^ 1]);
+    cp_async_commit();
+    const int64_t t0 = bin_begin(b), t1 = w.hist[b];
+    cp_async_wait1();
+    __syncthreads();
+    if (t1 > t0) {
+      int64_t og[4];
+      bin_origin4(b, bg, og);
+      for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+        const QRec<float> r = recs[t];
+        int64_t c[4];
+        unpack_cell<4>(r.cell, c);
+        TileBlock4 blk;
+        blk.v = tiles[stage].v;
+        blk.base = (int)((((c[3] - og[3]) * TILE4_EDGE + (c[2] - og[2])) * TILE4_EDGE + (c[1] - og[1])) *
+                             TILE4_EDGE +
+                         (c[0] - og[0]));
+        const float fr[4] = {r.f[0], r.f[1], r.f[2], r.f[3]};
+        double val[1], grad[4];
+        eval_otf4_mixed_block<1>(blk, kp, fr, val, grad);
+        write_vals<4, 1>(o, r.row, val, grad);
+      }
+    }
+    __syncthreads();  // this stage is refilled two bins later
+    stage ^= 1;
+  }
+  // records that need no evaluation (out of volume, NaN, sentinel column)
+  for (int64_t t = bin_begin(nbins) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const QRec<float> r = recs[t];
+    write_const<4, 1>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
+  }
+}
+
+// Launches the 4D bin-staged kernel when it applies (4D, mixed, one scalar
+// field, 4^4-cell bins); returns false otherwise.
+static bool launch_eval_bin4(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
+                             const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
+  if (g->dim != 4 || g->nfield != 1 || bg.shift != 2) return false;
+  const size_t smem = 2 * sizeof(BinTile4);
+  static int per_sm = 0;
+  if (!per_sm) {
+    if (cudaFuncSetAttribute(eval_bin4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return false;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, eval_bin4_kernel, BIN4_THREADS, smem) != cudaSuccess ||
+        n < 1)
+      return false;
+    per_sm = n;
+  }
+  int64_t grid = (int64_t)sm_count_sorted() * per_sm;
+  if (grid > bg.nbins) grid = bg.nbins;
+  if (grid < 1) grid = 1;
+  eval_bin4_kernel<<<(unsigned)grid, BIN4_THREADS, smem, s>>>(*g, kp, bg, nq, *out, w);
+  return true;
+}
+
 template <int DIM, bool MIXED>
 static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, double *q, int64_t nq,
                        int64_t qs, int wb, const arb_query_out *out, int32_t *status, const SortedWork &w,
@@ -713,6 +843,7 @@ template <int DIM, bool MIXED>
 static void launch_eval(const arb_grid *g, const KParams &kp, int64_t nq, const arb_query_out *out,
                         const SortedWork &w, bool table, cudaStream_t s) {
   if (DIM == 3 && MIXED && !table && launch_eval_bin(g, kp, bin_geom(g), nq, out, w, s)) return;
+  if (DIM == 4 && MIXED && !table && launch_eval_bin4(g, kp, bin_geom(g), nq, out, w, s)) return;
   const int TE = DIM == 3 ? 256 : 128;
   const unsigned BE = (unsigned)((nq + TE - 1) / TE);
 #define ES(FF, TAB) eval_sorted_kernel<DIM, FF, MIXED, TAB><<<BE, TE, 0, s>>>(*g, kp, nq, *out, w)
