@@ -593,6 +593,7 @@ static bool launch_eval_bin(const arb_grid *g, const KParams &kp, const BinGeom 
 }
 
 // ---- bin-staged evaluation (4D, mixed, one scalar field, 4^4-cell bins) -------
+// rQuery2 of the 4D class (ARBInterp.py:1129-1189) on the fly.
 // As eval_bin in 3D: one CTA per bin (round-robin), the bin's 7^4-point
 // footprint of (hi, lo) pairs copied into shared memory with cp.async and
 // double-buffered, one thread per query evaluating eval_otf4_mixed_block on
