@@ -22,6 +22,30 @@ static inline int launch_status() {
   return e == cudaSuccess ? ARB_OK : ARB_ERR_CUDA;
 }
 
+// -- per-device host caches -----------------------------------------------------
+// Function attributes (shared-memory limits) and __device__ constants are
+// per device, so launchers keep their one-time setup per device index.
+constexpr int MAX_DEVICES = 64;
+
+// The current device's index, or -1 when there is none (or it is out of range).
+static inline int current_device() {
+  int d = -1;
+  return (cudaGetDevice(&d) == cudaSuccess && d >= 0 && d < MAX_DEVICES) ? d : -1;
+}
+
+// Streaming multiprocessors of the current device (cached per device).
+static inline int device_sms() {
+  static int n[MAX_DEVICES] = {};
+  const int d = current_device();
+  if (d < 0) return 148;
+  if (!n[d]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, d);
+    n[d] = v > 0 ? v : 148;
+  }
+  return n[d];
+}
+
 // -- Catmull-Rom weights ------------------------------------------------------
 // The reference's 3D A = inv(B) D is exactly kron(A1, A1, A1) with A1 the
 // 4x4 Catmull-Rom matrix (cubic Hermite with central-difference slopes), so

@@ -104,16 +104,7 @@ __global__ void __launch_bounds__(256, MIXED ? 2 : 1) batched_kernel(const arb_g
   }
 }
 
-static int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 148;
-  }
-  return n;
-}
+static int sm_count() { return device_sms(); }
 
 }  // namespace arb
 

@@ -312,14 +312,7 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
 }
 
 static int num_sms() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 148;
-  }
-  return n;
+  return device_sms();
 }
 
 using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -351,24 +344,28 @@ int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *tabl
   const size_t smem = sizeof(TcSmem) + 1024;
   static_assert(3 * (sizeof(TcSmem) + 1024 + 1024) > 228 * 1024, "a third CTA per SM would oversubscribe TMEM");
   static_assert(offsetof(TcSmem, stage) % 1024 == 0, "swizzled boxes need 1 KB alignment");
-  static int per_sm = 0;
-  static std::once_flag once;
-  static cudaError_t attr_err = cudaSuccess;
-  std::call_once(once, [&] {
+  // one-time setup per device (function attributes are per device)
+  static std::once_flag once[MAX_DEVICES];
+  static int per_sm_dev[MAX_DEVICES];
+  static cudaError_t attr_err[MAX_DEVICES];
+  const int dev = current_device();
+  if (dev < 0) return ARB_ERR_CUDA;
+  std::call_once(once[dev], [&] {
+    attr_err[dev] = cudaSuccess;
     const void *ks[3] = {(const void *)coef3_tc_kernel<1>, (const void *)coef3_tc_kernel<3>,
                          (const void *)coef3_tc_kernel<4>};
     for (const void *k : ks) {
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-      if (e != cudaSuccess) attr_err = e;
+      if (e != cudaSuccess) attr_err[dev] = e;
     }
-    int dev = 0, smem_sm = 0;
-    cudaGetDevice(&dev);
+    int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    per_sm = (int)(smem_sm / (int64_t)(smem + 1024));
-    per_sm = per_sm < 1 ? 1 : (per_sm > 2 ? 2 : per_sm);
+    int n = (int)(smem_sm / (int64_t)(smem + 1024));
+    per_sm_dev[dev] = n < 1 ? 1 : (n > 2 ? 2 : n);
   });
-  if (attr_err != cudaSuccess) return ARB_ERR_CUDA;
+  if (attr_err[dev] != cudaSuccess) return ARB_ERR_CUDA;
+  const int per_sm = per_sm_dev[dev];
   const int F = g->nfield;
   if (F != 1 && F != 3 && F != 4) return ARB_ERR_INVALID;
   // one tensor map covers at most 2^31 rows; larger solves go in chunks
@@ -731,10 +728,10 @@ int coef4_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *tabl
   const size_t smem = sizeof(Tc4Smem) + 1024;
   static_assert(sizeof(Tc4Smem) + 1024 <= 232448, "shared memory above the per-CTA limit");
   static std::mutex mu;
-  static bool filled[64] = {};
-  static bool attr = false;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ARB_ERR_CUDA;
+  static bool filled[MAX_DEVICES] = {};
+  static bool attr[MAX_DEVICES] = {};
+  const int dev = current_device();
+  if (dev < 0) return ARB_ERR_CUDA;
   {
     std::lock_guard<std::mutex> lock(mu);
     if (!filled[dev]) {
@@ -743,13 +740,13 @@ int coef4_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *tabl
       if (cudaMemcpyToSymbol(g_b4, host.data(), host.size() * sizeof(__half)) != cudaSuccess) return ARB_ERR_CUDA;
       filled[dev] = true;
     }
-    if (!attr) {
+    if (!attr[dev]) {
       const void *ks[3] = {(const void *)coef4_tc_kernel<1>, (const void *)coef4_tc_kernel<3>,
                            (const void *)coef4_tc_kernel<4>};
       for (const void *k : ks)
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
           return ARB_ERR_CUDA;
-      attr = true;
+      attr[dev] = true;
     }
   }
   const int F = g->nfield;

@@ -576,15 +576,14 @@ static void launch_ordered_tile(const void *field, int64_t npts, const double *a
                                 cudaStream_t s) {
   constexpr int NC = DIM + (KIND == ARB_KIND_SCALAR ? 1 : 3);
   const size_t smem = sizeof(TF) * OT * (OT + 1) * NC;
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[MAX_DEVICES] = {};
+  const int dev = current_device();
+  if (dev >= 0 && !attr[dev]) {
     cudaFuncSetAttribute(ordered_tile_kernel<TF, KIND, DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
-    attr = true;
+    attr[dev] = true;
   }
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sms();
   int64_t grid = (int64_t)sms * 4, tiles_max = npts / (OT * 4) + 1;  // tiles >= npts / 1024 when a tile is full
   if (grid > tiles_max) grid = tiles_max;
   ordered_tile_kernel<TF, KIND, DIM><<<(unsigned)grid, 256, smem, s>>>((const TF *)field, npts, axes, cap, w,

@@ -561,16 +561,7 @@ __global__ void __launch_bounds__(256, 4) eval_bin_kernel(arb_grid g, KParams kp
   }
 }
 
-static int sm_count_sorted() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 148;
-  }
-  return n;
-}
+static int sm_count_sorted() { return device_sms(); }
 
 // Launches the bin-staged kernel when it applies (3D, mixed, 'both' fields,
 // 8^3-cell bins); returns false otherwise.
@@ -578,12 +569,14 @@ static bool launch_eval_bin(const arb_grid *g, const KParams &kp, const BinGeom 
                             const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
   if (g->dim != 3 || g->nfield != 4 || bg.shift != 3) return false;
   const size_t smem = 2 * sizeof(BinTile<4>);
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[MAX_DEVICES] = {};
+  const int dev = current_device();
+  if (dev < 0) return false;
+  if (!attr[dev]) {
     if (cudaFuncSetAttribute(eval_bin_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
       return false;
-    attr = true;
+    attr[dev] = true;
   }
   int64_t grid = (int64_t)sm_count_sorted() * 4;  // 4 resident per SM (64 registers)
   if (grid > bg.nbins) grid = bg.nbins;
@@ -705,8 +698,10 @@ static bool launch_eval_bin4(const arb_grid *g, const KParams &kp, const BinGeom
                              const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
   if (g->dim != 4 || g->nfield != 1 || bg.shift != 2) return false;
   const size_t smem = 2 * sizeof(BinTile4);
-  static int per_sm = 0;
-  if (!per_sm) {
+  static int per_sm[MAX_DEVICES] = {};
+  const int dev = current_device();
+  if (dev < 0) return false;
+  if (!per_sm[dev]) {
     if (cudaFuncSetAttribute(eval_bin4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
       return false;
@@ -714,9 +709,9 @@ static bool launch_eval_bin4(const arb_grid *g, const KParams &kp, const BinGeom
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, eval_bin4_kernel, BIN4_THREADS, smem) != cudaSuccess ||
         n < 1)
       return false;
-    per_sm = n;
+    per_sm[dev] = n;
   }
-  int64_t grid = (int64_t)sm_count_sorted() * per_sm;
+  int64_t grid = (int64_t)sm_count_sorted() * per_sm[dev];
   if (grid > bg.nbins) grid = bg.nbins;
   if (grid < 1) grid = 1;
   eval_bin4_kernel<<<(unsigned)grid, BIN4_THREADS, smem, s>>>(*g, kp, bg, nq, *out, w);
