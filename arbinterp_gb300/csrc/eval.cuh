@@ -208,12 +208,26 @@ __device__ __forceinline__ void load_row(const arb_grid &g, int64_t npts, int64_
 // then smoothed over the other two axes (positive-dominated weights, no
 // cancellation).  Values use corner deltas as before.  Layers and lines are
 // visited in the order 1, 0, 2, 3 so the local references are loaded first.
-template <int F>
-__device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KParams &kp, const int64_t c[3],
-                                                     const float frac[3], double val[F], double grad[3]) {
+// BLK says where the 4x4x4 block is read from: at(i, j, k) is the index of
+// block point (i, j, k); with F = 1, hl(index) is its (hi, lo) pair; with
+// F = 4, hi4(index) its float4 (hi_x, hi_y, hi_z, hi_n) and lo(index) lo_n.
+struct Grid32Block3 {  // the mixed grid in global memory
+  const float *g32;
+  int64_t npts, sy, sz, base;  // strides of y, z; index of the block corner
+  __device__ __forceinline__ int64_t at(int i, int j, int k) const { return base + k * sz + j * sy + i; }
+  __device__ __forceinline__ float2 hl(int64_t p) const { return __ldg(reinterpret_cast<const float2 *>(g32) + p); }
+  __device__ __forceinline__ float4 hi4(int64_t p) const { return __ldg(reinterpret_cast<const float4 *>(g32) + p); }
+  __device__ __forceinline__ float lo(int64_t p) const { return __ldg(g32 + npts * 4 + p); }
+  template <int F>
+  __device__ __forceinline__ void load(int64_t p, int f, float &h, float &l) const {
+    g32_load<F>(g32, npts, p, f, h, l);
+  }
+};
+
+template <int F, class BLK>
+__device__ __forceinline__ void eval_otf3_mixed_block(const BLK &blk, const KParams &kp, const float frac[3],
+                                                      double val[F], double grad[3]) {
   constexpr int G = F - 1;  // the field whose gradient is returned (scalar or |B|)
-  const int64_t nx = g.n[0], ny = g.n[1];
-  const int64_t npts = grid_points(g);
   float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
   cr_weights<float>(frac[0], wx);
   cr_weights<float>(frac[1], wy);
@@ -222,9 +236,9 @@ __device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KP
   cr_dweights<float>(frac[1], dy);
   cr_dweights<float>(frac[2], dz);
   float rhi[F], rlo[F];
-  const int64_t pr = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
+  const auto pr = blk.at(1, 1, 1);
 #pragma unroll
-  for (int f = 0; f < F; ++f) g32_load<F>(g.grid32, npts, pr, f, rhi[f], rlo[f]);
+  for (int f = 0; f < F; ++f) blk.template load<F>(pr, f, rhi[f], rlo[f]);
   float zh[4][4], zl[4][4], yh[4], yl[4];
   float acc[F], gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
@@ -239,26 +253,24 @@ __device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KP
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) {
       const int j = ORD[jj];
-      const int64_t p = ((c[2] + k) * ny + (c[1] + j)) * nx + c[0];
+      const auto p = blk.at(0, j, k);
       float h[4], l[4], vv[4][3];
-      if (F == 1) {
-        const float2 *r = reinterpret_cast<const float2 *>(g.grid32) + p;
+      if constexpr (F == 1) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          const float2 a = __ldg(r + i);
+          const float2 a = blk.hl(p + i);
           h[i] = a.x;
           l[i] = a.y;
         }
       } else {
-        const float4 *r4 = reinterpret_cast<const float4 *>(g.grid32) + p;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          const float4 a = __ldg(r4 + i);
+          const float4 a = blk.hi4(p + i);
           vv[i][0] = a.x - rhi[0];
           vv[i][1] = a.y - rhi[1 % F];
           vv[i][2] = a.z - rhi[2 % F];
           h[i] = a.w;
-          l[i] = __ldg(g.grid32 + npts * 4 + p + i);
+          l[i] = blk.lo(p + i);
         }
       }
       if (k == 1) {
@@ -315,6 +327,19 @@ __device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KP
   grad[0] = f2d_exact(gx * kp.inv_hf[0]);
   grad[1] = f2d_exact(gy * kp.inv_hf[1]);
   grad[2] = f2d_exact(gz * kp.inv_hf[2]);
+}
+
+template <int F>
+__device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KParams &kp, const int64_t c[3],
+                                                     const float frac[3], double val[F], double grad[3]) {
+  const int64_t nx = g.n[0], ny = g.n[1];
+  Grid32Block3 blk;
+  blk.g32 = g.grid32;
+  blk.npts = grid_points(g);
+  blk.sy = nx;
+  blk.sz = nx * ny;
+  blk.base = (c[2] * ny + c[1]) * nx + c[0];
+  eval_otf3_mixed_block<F>(blk, kp, frac, val, grad);
 }
 
 // ---- 3D on-the-fly ---------------------------------------------------------

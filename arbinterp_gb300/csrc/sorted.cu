@@ -585,6 +585,98 @@ static bool launch_eval_bin(const arb_grid *g, const KParams &kp, const BinGeom 
   return true;
 }
 
+// ---- bin-staged evaluation (3D, mixed, one scalar field, 8^3-cell bins) -------
+// rQuery2 (ARBInterp.py:399-455) on the fly for scalar / norm fields: the
+// bin's 11^3 (hi, lo) pairs staged in shared memory as in eval_bin, one query
+// per thread evaluating eval_otf3_mixed_block on the staged block (the same
+// contraction as the global-memory kernel, so the same bits).
+constexpr int BIN1_THREADS = 128;
+
+struct TileBlock3 {  // a 4x4x4 block inside a staged (hi, lo) tile
+  const float2 *v;
+  int base;  // tile index of the block corner
+  __device__ __forceinline__ int at(int i, int j, int k) const {
+    return base + (k * TILE_EDGE + j) * TILE_EDGE + i;
+  }
+  __device__ __forceinline__ float2 hl(int p) const { return v[p]; }
+  template <int F>
+  __device__ __forceinline__ void load(int p, int, float &hi, float &lo) const {
+    const float2 x = v[p];
+    hi = x.x;
+    lo = x.y;
+  }
+};
+
+__global__ void __launch_bounds__(BIN1_THREADS) eval_bin1_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
+                                                                 arb_query_out o, SortedWork w) {
+  extern __shared__ __align__(16) unsigned char bin1_smem[];
+  BinTile<1> *tiles = reinterpret_cast<BinTile<1> *>(bin1_smem);
+  const int64_t nbins = bg.nbins;
+  const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
+  int stage = 0;
+  int64_t b = blockIdx.x;
+  // after placement hist[b] is the end of bin b; bins with no query need no copy
+  auto bin_begin = [&](int64_t bb) { return bb > 0 ? (int64_t)w.hist[bb - 1] : (int64_t)0; };
+  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb] - bin_begin(bb) : 0; };
+  if (count(b) > 0) load_bin_tile<1>(g, bg, b, tiles[0]);
+  cp_async_commit();
+  for (; b < nbins; b += gridDim.x) {
+    const int64_t bn = b + gridDim.x;
+    if (count(bn) > 0) load_bin_tile<1>(g, bg, bn, tiles[stage ^ 1]);
+    cp_async_commit();
+    const int64_t t0 = bin_begin(b), t1 = w.hist[b];
+    cp_async_wait1();
+    __syncthreads();
+    if (t1 > t0) {
+      int64_t og[3];
+      bin_origin(b, bg, og);
+      for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+        const QRec<float> r = recs[t];
+        int64_t c[3];
+        unpack_cell<3>(r.cell, c);
+        TileBlock3 blk;
+        blk.v = tiles[stage].v;
+        blk.base = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));
+        const float fr[3] = {r.f[0], r.f[1], r.f[2]};
+        double val[1], grad[3];
+        eval_otf3_mixed_block<1>(blk, kp, fr, val, grad);
+        write_vals<3, 1>(o, r.row, val, grad);
+      }
+    }
+    __syncthreads();  // this stage is refilled two bins later
+    stage ^= 1;
+  }
+  // records that need no evaluation (out of volume, NaN, sentinel column)
+  for (int64_t t = bin_begin(nbins) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const QRec<float> r = recs[t];
+    write_const<3, 1>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
+  }
+}
+
+// Launches the 3D scalar bin-staged kernel when it applies (3D, mixed, one
+// field, 8^3-cell bins); returns false otherwise.
+static bool launch_eval_bin1(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
+                             const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
+  if (g->dim != 3 || g->nfield != 1 || bg.shift != 3) return false;
+  const size_t smem = 2 * sizeof(BinTile<1>);
+  static int per_sm[MAX_DEVICES] = {};
+  const int dev = current_device();
+  if (dev < 0) return false;
+  if (!per_sm[dev]) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, eval_bin1_kernel, BIN1_THREADS, smem) != cudaSuccess ||
+        n < 1)
+      return false;
+    per_sm[dev] = n;
+  }
+  int64_t grid = (int64_t)sm_count_sorted() * per_sm[dev];
+  if (grid > bg.nbins) grid = bg.nbins;
+  if (grid < 1) grid = 1;
+  eval_bin1_kernel<<<(unsigned)grid, BIN1_THREADS, smem, s>>>(*g, kp, bg, nq, *out, w);
+  return true;
+}
+
 // ---- bin-staged evaluation (4D, mixed, one scalar field, 4^4-cell bins) -------
 // rQuery2 of the 4D class (ARBInterp.py:1129-1189) on the fly.
 // As eval_bin in 3D: one CTA per bin (round-robin), the bin's 7^4-point
@@ -839,6 +931,7 @@ template <int DIM, bool MIXED>
 static void launch_eval(const arb_grid *g, const KParams &kp, int64_t nq, const arb_query_out *out,
                         const SortedWork &w, bool table, cudaStream_t s) {
   if (DIM == 3 && MIXED && !table && launch_eval_bin(g, kp, bin_geom(g), nq, out, w, s)) return;
+  if (DIM == 3 && MIXED && !table && launch_eval_bin1(g, kp, bin_geom(g), nq, out, w, s)) return;
   if (DIM == 4 && MIXED && !table && launch_eval_bin4(g, kp, bin_geom(g), nq, out, w, s)) return;
   const int TE = DIM == 3 ? 256 : 128;
   const unsigned BE = (unsigned)((nq + TE - 1) / TE);
