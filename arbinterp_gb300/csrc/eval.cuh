@@ -342,6 +342,42 @@ __device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KP
   eval_otf3_mixed_block<F>(blk, kp, frac, val, grad);
 }
 
+// Vector fields (values only) in float32: corner deltas of the three
+// components; BLK as for eval_otf3_mixed_block (hi4 and at).
+template <class BLK>
+__device__ __forceinline__ void eval_otf3_vec_block(const BLK &blk, const float frac[3], double val[3]) {
+  float wx[4], wy[4], wz[4];
+  cr_weights<float>(frac[0], wx);
+  cr_weights<float>(frac[1], wy);
+  cr_weights<float>(frac[2], wz);
+  const float4 r = blk.hi4(blk.at(1, 1, 1));  // reference point: the cell's own corner
+  const float rhi[3] = {r.x, r.y, r.z};
+  float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    float ay[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const auto p = blk.at(0, j, k);
+      float v[4][3];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float4 a = blk.hi4(p + i);
+        v[i][0] = a.x - rhi[0];
+        v[i][1] = a.y - rhi[1];
+        v[i][2] = a.z - rhi[2];
+      }
+#pragma unroll
+      for (int f = 0; f < 3; ++f)
+        ay[f] += wy[j] * (wx[0] * v[0][f] + wx[1] * v[1][f] + wx[2] * v[2][f] + wx[3] * v[3][f]);
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) acc[f] += wz[k] * ay[f];
+  }
+#pragma unroll
+  for (int f = 0; f < 3; ++f) val[f] = f2d_exact(rhi[f] + (0.f + acc[f]));
+}
+
 // ---- 3D on-the-fly ---------------------------------------------------------
 template <int F, bool MIXED>
 __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, const int64_t c[3],
@@ -351,6 +387,16 @@ __device__ __forceinline__ void eval_otf3(const arb_grid &g, const KParams &kp, 
   constexpr bool GRAD = (F != 3);
   if constexpr (MIXED && GRAD) {
     eval_otf3_mixed_grad<F>(g, kp, c, frac, val, grad);
+    return;
+  }
+  if constexpr (MIXED && F == 3) {
+    Grid32Block3 blk;
+    blk.g32 = g.grid32;
+    blk.npts = grid_points(g);
+    blk.sy = g.n[0];
+    blk.sz = g.n[0] * g.n[1];
+    blk.base = (c[2] * g.n[1] + c[1]) * g.n[0] + c[0];
+    eval_otf3_vec_block(blk, frac, val);
     return;
   }
   const int64_t nx = g.n[0], ny = g.n[1];

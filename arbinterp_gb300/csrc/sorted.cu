@@ -362,6 +362,10 @@ template <>
 struct BinTile<1> {          // (hi, lo) per point
   float2 v[TILE_PTS];
 };
+template <>
+struct BinTile<3> {          // (hi_x, hi_y, hi_z, 0) per point
+  float4 v[TILE_PTS];
+};
 
 __device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
@@ -407,6 +411,8 @@ __device__ __forceinline__ void load_bin_tile(const arb_grid &g, const BinGeom &
       cp_async16(&reinterpret_cast<BinTile<4> &>(t).hi[lz * HI_PLANE + ly * TILE_EDGE + lx],
                  reinterpret_cast<const float4 *>(g.grid32) + p);
       cp_async4(&reinterpret_cast<BinTile<4> &>(t).lo[e], g.grid32 + npts * 4 + p);
+    } else if (F == 3) {
+      cp_async16(&reinterpret_cast<BinTile<3> &>(t).v[e], reinterpret_cast<const float4 *>(g.grid32) + p);
     } else {
       cp_async8(&reinterpret_cast<BinTile<1> &>(t).v[e], reinterpret_cast<const float2 *>(g.grid32) + p);
     }
@@ -585,21 +591,25 @@ static bool launch_eval_bin(const arb_grid *g, const KParams &kp, const BinGeom 
   return true;
 }
 
-// ---- bin-staged evaluation (3D, mixed, one scalar field, 8^3-cell bins) -------
-// rQuery2 (ARBInterp.py:399-455) on the fly for scalar / norm fields: the
-// bin's 11^3 (hi, lo) pairs staged in shared memory as in eval_bin, one query
-// per thread evaluating eval_otf3_mixed_block on the staged block (the same
-// contraction as the global-memory kernel, so the same bits).
-constexpr int BIN1_THREADS = 128;
+// ---- bin-staged evaluation (3D, mixed, scalar / norm or vector fields) -------
+// rQuery2 (ARBInterp.py:399-455, scalar and norm fields: one (hi, lo) field)
+// and rQuery1 (ARBInterp.py:344-397, vector fields: three components, values
+// only) on the fly: the bin's 11^3 points staged in shared memory as in
+// eval_bin, one query per thread evaluating eval_otf3_mixed_block /
+// eval_otf3_vec_block on the staged block (the code the global-memory kernel
+// runs, so the same bits).
+constexpr int BINF_THREADS = 128;
 
-struct TileBlock3 {  // a 4x4x4 block inside a staged (hi, lo) tile
-  const float2 *v;
+template <int F>
+struct TileBlock3 {  // a 4x4x4 block inside a staged tile
+  const typename std::conditional<F == 1, float2, float4>::type *v;
   int base;  // tile index of the block corner
   __device__ __forceinline__ int at(int i, int j, int k) const {
     return base + (k * TILE_EDGE + j) * TILE_EDGE + i;
   }
   __device__ __forceinline__ float2 hl(int p) const { return v[p]; }
-  template <int F>
+  __device__ __forceinline__ float4 hi4(int p) const { return v[p]; }
+  template <int FF>
   __device__ __forceinline__ void load(int p, int, float &hi, float &lo) const {
     const float2 x = v[p];
     hi = x.x;
@@ -607,10 +617,11 @@ struct TileBlock3 {  // a 4x4x4 block inside a staged (hi, lo) tile
   }
 };
 
-__global__ void __launch_bounds__(BIN1_THREADS) eval_bin1_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
+template <int F>
+__global__ void __launch_bounds__(BINF_THREADS) eval_binf_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
                                                                  arb_query_out o, SortedWork w) {
-  extern __shared__ __align__(16) unsigned char bin1_smem[];
-  BinTile<1> *tiles = reinterpret_cast<BinTile<1> *>(bin1_smem);
+  extern __shared__ __align__(16) unsigned char binf_smem[];
+  BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(binf_smem);
   const int64_t nbins = bg.nbins;
   const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
   int stage = 0;
@@ -618,11 +629,11 @@ __global__ void __launch_bounds__(BIN1_THREADS) eval_bin1_kernel(arb_grid g, KPa
   // after placement hist[b] is the end of bin b; bins with no query need no copy
   auto bin_begin = [&](int64_t bb) { return bb > 0 ? (int64_t)w.hist[bb - 1] : (int64_t)0; };
   auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb] - bin_begin(bb) : 0; };
-  if (count(b) > 0) load_bin_tile<1>(g, bg, b, tiles[0]);
+  if (count(b) > 0) load_bin_tile<F>(g, bg, b, tiles[0]);
   cp_async_commit();
   for (; b < nbins; b += gridDim.x) {
     const int64_t bn = b + gridDim.x;
-    if (count(bn) > 0) load_bin_tile<1>(g, bg, bn, tiles[stage ^ 1]);
+    if (count(bn) > 0) load_bin_tile<F>(g, bg, bn, tiles[stage ^ 1]);
     cp_async_commit();
     const int64_t t0 = bin_begin(b), t1 = w.hist[b];
     cp_async_wait1();
@@ -634,13 +645,16 @@ __global__ void __launch_bounds__(BIN1_THREADS) eval_bin1_kernel(arb_grid g, KPa
         const QRec<float> r = recs[t];
         int64_t c[3];
         unpack_cell<3>(r.cell, c);
-        TileBlock3 blk;
+        TileBlock3<F> blk;
         blk.v = tiles[stage].v;
         blk.base = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));
         const float fr[3] = {r.f[0], r.f[1], r.f[2]};
-        double val[1], grad[3];
-        eval_otf3_mixed_block<1>(blk, kp, fr, val, grad);
-        write_vals<3, 1>(o, r.row, val, grad);
+        double val[F], grad[3] = {0.0, 0.0, 0.0};
+        if constexpr (F == 1)
+          eval_otf3_mixed_block<1>(blk, kp, fr, val, grad);
+        else
+          eval_otf3_vec_block(blk, fr, val);
+        write_vals<3, F>(o, r.row, val, grad);
       }
     }
     __syncthreads();  // this stage is refilled two bins later
@@ -650,22 +664,23 @@ __global__ void __launch_bounds__(BIN1_THREADS) eval_bin1_kernel(arb_grid g, KPa
   for (int64_t t = bin_begin(nbins) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
        t += (int64_t)gridDim.x * blockDim.x) {
     const QRec<float> r = recs[t];
-    write_const<3, 1>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
+    write_const<3, F>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
   }
 }
 
-// Launches the 3D scalar bin-staged kernel when it applies (3D, mixed, one
-// field, 8^3-cell bins); returns false otherwise.
-static bool launch_eval_bin1(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
+// Launches the 3D one-field / vector bin-staged kernel when it applies (3D,
+// mixed, F = 1 or 3, 8^3-cell bins); returns false otherwise.
+template <int F>
+static bool launch_eval_binf(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
                              const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
-  if (g->dim != 3 || g->nfield != 1 || bg.shift != 3) return false;
-  const size_t smem = 2 * sizeof(BinTile<1>);
+  const size_t smem = 2 * sizeof(BinTile<F>);
   static int per_sm[MAX_DEVICES] = {};
   const int dev = current_device();
   if (dev < 0) return false;
   if (!per_sm[dev]) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, eval_bin1_kernel, BIN1_THREADS, smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, eval_binf_kernel<F>, BINF_THREADS, smem) !=
+            cudaSuccess ||
         n < 1)
       return false;
     per_sm[dev] = n;
@@ -673,8 +688,16 @@ static bool launch_eval_bin1(const arb_grid *g, const KParams &kp, const BinGeom
   int64_t grid = (int64_t)sm_count_sorted() * per_sm[dev];
   if (grid > bg.nbins) grid = bg.nbins;
   if (grid < 1) grid = 1;
-  eval_bin1_kernel<<<(unsigned)grid, BIN1_THREADS, smem, s>>>(*g, kp, bg, nq, *out, w);
+  eval_binf_kernel<F><<<(unsigned)grid, BINF_THREADS, smem, s>>>(*g, kp, bg, nq, *out, w);
   return true;
+}
+
+static bool launch_eval_bin1(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
+                             const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
+  if (g->dim != 3 || bg.shift != 3) return false;
+  if (g->nfield == 1) return launch_eval_binf<1>(g, kp, bg, nq, out, w, s);
+  if (g->nfield == 3) return launch_eval_binf<3>(g, kp, bg, nq, out, w, s);
+  return false;
 }
 
 // ---- bin-staged evaluation (4D, mixed, one scalar field, 4^4-cell bins) -------

@@ -544,13 +544,14 @@ def test_quadcubic_bin_tiles_equal_global_gathers():
     assert torch.isnan(outs[0][1]).any() and not torch.isnan(outs[0][1]).all()
 
 
-@pytest.mark.parametrize("mode", [None, "norm"])
+@pytest.mark.parametrize("mode", [None, "norm", "vector"])
 def test_tricubic_scalar_bin_tiles_equal_global_gathers(mode):
-    """3D mixed on the fly, one field (a scalar field, or |B| in norm mode):
-    the bin-staged kernel (8^3-cell bins, blocks read from shared memory)
-    returns the same bits as the kernel gathering from global memory (4^3-cell
-    bins), on a grid whose cell counts are not multiples of 8, with queries
-    outside the volume and in the last cells."""
+    """3D mixed on the fly, one field (a scalar field, or |B| in norm mode)
+    or the three components (vector mode): the bin-staged kernel (8^3-cell
+    bins, blocks read from shared memory) returns the same bits as the kernel
+    gathering from global memory (4^3-cell bins), on a grid whose cell counts
+    are not multiples of 8, with queries outside the volume and in the last
+    cells."""
     import torch
     tricubic, _ = _mods()
     from arbinterp_gb300 import synth
@@ -559,7 +560,7 @@ def test_tricubic_scalar_bin_tiles_equal_global_gathers(mode):
         kw = {}
     else:
         f = synth.dipole_field3(n=(37, 30, 42), seed=34)
-        kw = {"mode": "norm"}
+        kw = {"mode": mode}
     o = tricubic(f, "quiet", precision="mixed", strategy="otf", **kw)
     lo, hi = np.array([float(v) for v in o._lo]), np.array([float(v) for v in o._hi])
     rng = np.random.default_rng(35)
@@ -577,4 +578,5 @@ def test_tricubic_scalar_bin_tiles_equal_global_gathers(mode):
             continue
         assert torch.equal(torch.isnan(a), torch.isnan(b))
         assert torch.equal(torch.nan_to_num(a), torch.nan_to_num(b))
-    assert torch.isnan(outs[0][1]).any() and not torch.isnan(outs[0][1]).all()
+    first = next(t for t in outs[0][:3] if t is not None)
+    assert torch.isnan(first).any() and not torch.isnan(first).all()
