@@ -602,6 +602,8 @@ constexpr int BINF_THREADS = 128;
 
 template <int F>
 struct TileBlock3 {  // a 4x4x4 block inside a staged tile
+  // F = 1: (hi, lo) pairs, read by hl and load; F = 3: float4 components,
+  // read by hi4 (the accessors of the other layout are never instantiated)
   const typename std::conditional<F == 1, float2, float4>::type *v;
   int base;  // tile index of the block corner
   __device__ __forceinline__ int at(int i, int j, int k) const {
