@@ -62,13 +62,14 @@ def parse():
                         "CSV file (2.6 GB) read as np.genfromtxt(delimiter=',') does")
     p.add_argument("--profile", default=None,
                    choices=["step", "small", "small-table", "small-fp64", "small-coef", "small-4d", "small-batched",
-                            "small-adjoint", "small-csv"],
+                            "small-adjoint", "small-csv", "small-scalar", "small-traj"],
                    help="run a fixed workload for an ncu capture and exit (no timing, no JSON): "
                         "'step' = two full bench steps; 'small*' = 160^3 dipole field, 2.02e6 queries; "
                         "'small-coef' = 96^3 table solve; 'small-4d' = 40^3x12 scalar, 2e6 queries (on the fly "
                         "and table); 'small-batched' = 64 scalar fields; 'small-adjoint' = 96^3 scalar, 2e6 "
                         "queries forward + backward; 'small-csv' = the 128^3 'both' field file (324 MB) "
-                        "parsed twice")
+                        "parsed twice; 'small-scalar' = 160^3 scalar and 160^3 vector fields, 2e6 queries "
+                        "each; 'small-traj' = 2e5 particles x 20 RK4 steps in the 160^3 'both' field")
     return p.parse_args()
 
 
@@ -129,6 +130,25 @@ def run_profile(args):
             qq = q.clone().requires_grad_(True)
             val, _ = fld(v, qq)
             torch.nan_to_num(val).sum().backward()
+    elif args.profile == "small-scalar":
+        # one (hi, lo) field and three float32 components: the 3D one-field / vector bin tiles
+        for field, kw in ((synth.gaussian_field3(n=(160, 160, 160), h=(0.01, 0.012, 0.008), seed=5, device=dev), {}),
+                          (synth.dipole_field3(n=(160, 160, 160), seed=1, device=dev), {"mode": "vector"})):
+            o = tricubic(field, "quiet", precision="mixed", strategy="otf", **kw)
+            q = synth.uniform_queries([float(v) for v in o._lo], [float(v) for v in o._hi], 2_000_000, 20_000,
+                                      [float(v) for v in o._h], seed=3, device=dev)
+            for _ in range(2):
+                o.Query(q.clone())
+    elif args.profile == "small-traj":
+        field = synth.dipole_field3(n=(160, 160, 160), seed=1, device=dev)
+        o = tricubic(field, "quiet", mode="both", precision="mixed")
+        g0 = torch.Generator(device=dev).manual_seed(13)
+        lo = torch.tensor([float(v) for v in o._lo], device=dev)
+        hi = torch.tensor([float(v) for v in o._hi], device=dev)
+        x0 = lo + (hi - lo) * (0.25 + 0.5 * torch.rand((200_000, 3), generator=g0, device=dev, dtype=torch.float64))
+        v0 = 1e-3 * torch.randn((200_000, 3), generator=g0, device=dev, dtype=torch.float64)
+        for _ in range(2):
+            o.trajectories(x0, v0, 0.05, 20, coef=-1e-4)
     elif args.profile == "small-coef":
         # 96^3 'both' field: 804k cells x 4 fields x 64 float32 coefficients = 0.82 GB table
         field = synth.dipole_field3(n=(96, 96, 96), seed=1, device=dev)
