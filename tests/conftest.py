@@ -36,3 +36,30 @@ def normwise(a, b):
     d = np.abs(a[m] - b[m]).max(axis=0)
     s = np.abs(b[m]).max(axis=0)
     return d / np.where(s == 0, 1, s)
+
+
+GOLDEN_SCALE = os.path.join(ROOT, "tests", "golden", "golden_scale.npz")
+
+
+@pytest.fixture(scope="session")
+def golden_scale():
+    """Reference outputs on a 48^3 dipole field ('both', 'norm', 'vector')
+    and a 16^3 x 12 4D scalar field, 49,500 queries each (tests/golden/
+    make_golden.py --scale)."""
+    return dict(np.load(GOLDEN_SCALE))
+
+
+def grid_rows(axes, values):
+    """Field rows in meshgrid(indexing='ij') order from stored axes and value
+    columns (the generators are not bit-stable across CPU architectures)."""
+    G = np.meshgrid(*axes, indexing="ij")
+    vals = np.asarray(values).reshape(len(G[0].ravel()), -1)
+    return np.hstack([np.stack([g.ravel() for g in G], 1), vals])
+
+
+def c1s_field(g):
+    return grid_rows([g[f"c1_ax{a}"] for a in range(3)], g["c1_B"])
+
+
+def c2s_field(g):
+    return grid_rows([g[f"c2_ax{a}"] for a in range(4)], g["c2_U"])

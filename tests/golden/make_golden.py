@@ -42,7 +42,7 @@ def run_range(obj, q):
     out = obj.Query(qq)
     # the reference writes NaN over whole out-of-volume rows in place
     nanrows = np.isnan(qq).all(axis=1)
-    assert np.array_equal(qq[~nanrows], q[~nanrows])
+    assert np.array_equal(qq[~nanrows], q[~nanrows], equal_nan=True)
     res = {"nanrows": nanrows, "inds": np.asarray(obj.queryInds)}
     if isinstance(out, tuple) and len(out) == 3:
         res.update(comps=out[0], norms=out[1], grads=out[2])
@@ -245,6 +245,140 @@ def main(ref_path):
     print(f"wrote golden.npz ({sz / 1e6:.2f} MB, {len(out)} arrays)")
 
 
+def ref_index(q, lo, hi, h, npos):
+    """The reference's flat cell index of range-query rows (rQuery3,
+    ARBInterp.py:463-485; 4D rQuery2, ARBInterp.py:1138-1160), computed with the
+    same float64 operations (out-of-volume rows NaN), so candidate rows that
+    would make it raise IndexError (index > nc) can be dropped before the
+    reference runs."""
+    q = q.copy()
+    d = len(lo)
+    for a in range(d):
+        q[(q[:, a] < lo[a]) | (q[:, a] > hi[a])] = np.nan
+    idx = np.zeros(len(q))
+    stride = 1.0
+    for a in range(d):
+        ia = np.floor((q[:, a] - lo[a]) / h[a])
+        idx = idx + ia * stride
+        stride = stride * npos[a]
+    return idx
+
+
+def face_rows(rng, axes, lo, hi, h, npos, nc, n_faces, n_upper, n_nan):
+    """Special query rows: coordinates exactly on grid planes (cell faces,
+    IntMin and IntMax included), rows on each upper face (x = IntMax aliases
+    to the next row of cells, ARBInterp.py:481-483), rows on the last axis'
+    upper face inside the first cell column (index == nc: the sentinel
+    column), and rows with one NaN coordinate."""
+    d = len(lo)
+    rows = []
+    base = lambda m: lo + (hi - lo) * rng.random((m, d))  # noqa: E731
+    q = base(n_faces)
+    for r in q:
+        for a in rng.choice(d, rng.integers(1, d + 1), replace=False):
+            r[a] = axes[a][rng.integers(1, len(axes[a]) - 1)]
+    rows.append(q)
+    for a in range(d - 1):
+        q = base(n_upper)
+        q[:, a] = hi[a]
+        rows.append(q)
+    q = base(n_upper)
+    q[:, 0] = hi[0]
+    q[:, 1] = hi[1]
+    rows.append(q)
+    q = lo + rng.random((n_upper // 4, d)) * h * 0.999
+    q[:, d - 1] = hi[d - 1]
+    rows.append(q)
+    q = base(n_nan)
+    q[np.arange(n_nan), rng.integers(0, d, n_nan)] = np.nan
+    rows.append(q)
+    q = np.vstack(rows)
+    idx = ref_index(q, lo, hi, h, npos)
+    keep = ~(idx > nc)
+    return q[keep]
+
+
+def main_scale(ref_path):
+    """Reduced-size versions of the 256^3 'both' workload and the 4D
+    64^3 x 32 scalar workload, at sizes where the binned query path runs
+    (5e4 queries, above the default sort threshold), written to
+    golden_scale.npz."""
+    R = load_reference(ref_path)
+    out = {}
+    rng = np.random.default_rng(77)
+
+    # -- 48^3 dipole field, 'both' / 'norm' / 'vector' -----------------------
+    n = (48, 48, 48)
+    f = synth.dipole_field3(n=n, seed=1).numpy()
+    axes = [np.unique(f[:, a]) for a in range(3)]
+    out["c1_B"] = f[:, 3:]
+    for a in range(3):
+        out[f"c1_ax{a}"] = axes[a]
+    ob = quiet_call(R.tricubic, f, "quiet", mode="both")
+    lo = np.array([ob.xIntMin, ob.yIntMin, ob.zIntMin])
+    hi = np.array([ob.xIntMax, ob.yIntMax, ob.zIntMax])
+    h = np.array([ob.hx, ob.hy, ob.hz])
+    q = synth.uniform_queries(lo, hi, 49000, 500, h, seed=41).numpy()
+    special = face_rows(rng, axes, lo, hi, h, ob.nPos, ob.nc, 300, 60, 20)
+    q[rng.choice(len(q), len(special), replace=False)] = special
+    assert not (ref_index(q, lo, hi, h, ob.nPos) > ob.nc).any()
+    out["c1_q"] = q
+    res = run_range(ob, q)
+    pack("c1_both_", res, out)
+    out["c1_both_inds"] = res["inds"].astype(np.int32)
+    pack("c1_p_", params3(ob), out)
+    out["c1_p_basePointInds"] = ob.basePointInds.astype(np.int32)
+    on = quiet_call(R.tricubic, f, "quiet", mode="norm")
+    rn = run_range(on, q)
+    # rQuery2 evaluates alphan exactly as rQuery3 does: the same bits
+    assert np.array_equal(rn["norms"], res["norms"], equal_nan=True)
+    assert np.array_equal(rn["grads"], res["grads"], equal_nan=True)
+    ov = quiet_call(R.tricubic, f, "quiet", mode="vector")
+    rv = run_range(ov, q)
+    out["c1_vector_comps"] = rv["comps"]
+    assert np.array_equal(rv["inds"], res["inds"])
+    cells = [0, 1, ob.nPos[0] - 1, ob.nPos[0] * (ob.nPos[1] - 1), ob.nPos[0] * ob.nPos[1] - 1,
+             ob.nc - ob.nPos[0] * ob.nPos[1], ob.nc - ob.nPos[0], ob.nc - 1]
+    cells += list(rng.choice(ob.nc, 12, replace=False))
+    out["c1_nb_cells"] = np.array(cells)
+    out["c1_nb_inds"] = np.array([ob.neighbourInd(ob.basePointInds[c]) for c in cells])
+
+    # -- 16^3 x 12 moving-Gaussian scalar field (4D) --------------------------
+    n4 = (16, 16, 16, 12)
+    f4 = synth.moving_gaussian_field4(n=n4, seed=2).numpy()
+    axes4 = [np.unique(f4[:, a]) for a in range(4)]
+    out["c2_U"] = f4[:, 4]
+    for a in range(4):
+        out[f"c2_ax{a}"] = axes4[a]
+    o4 = quiet_call(R.quadcubic, f4, "quiet")
+    lo4 = np.array([o4.xIntMin, o4.yIntMin, o4.zIntMin, o4.tIntMin])
+    hi4 = np.array([o4.xIntMax, o4.yIntMax, o4.zIntMax, o4.tIntMax])
+    h4 = np.array([o4.hx, o4.hy, o4.hz, o4.ht])
+    np4 = np.array([o4.nPosx - 3, o4.nPosy - 3, o4.nPosz - 3, o4.nPost - 3])
+    q4 = synth.uniform_queries(lo4, hi4, 49000, 500, h4, seed=42).numpy()
+    special = face_rows(rng, axes4, lo4, hi4, h4, np4, o4.nc, 300, 60, 20)
+    q4[rng.choice(len(q4), len(special), replace=False)] = special
+    assert not (ref_index(q4, lo4, hi4, h4, np4) > o4.nc).any()
+    out["c2_q"] = q4
+    r4 = run_range(o4, q4)
+    pack("c2_", r4, out)
+    out["c2_inds"] = r4["inds"].astype(np.int32)
+    pack("c2_p_", params4(o4), out)
+    del out["c2_p_basePointInds"]
+    cells = [0, 1, np4[0] - 1, o4.nc - 1, o4.nc - np4[0], o4.nc - np4[0] * np4[1] * np4[2]]
+    cells += list(rng.choice(o4.nc, 10, replace=False))
+    out["c2_nb_cells"] = np.array(cells)
+    out["c2_nb_inds"] = np.array([o4.neighbourInd(o4.basePointInds[c]) for c in cells])
+
+    path = os.path.join(HERE, "golden_scale.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote golden_scale.npz ({os.path.getsize(path) / 1e6:.2f} MB, {len(out)} arrays)")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else
-         os.path.join(os.sep, "root", "reference", "src", "ARBInterp", "ARBInterp.py"))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    path = args[0] if args else os.path.join(os.sep, "root", "reference", "src", "ARBInterp", "ARBInterp.py")
+    if "--scale" in sys.argv:
+        main_scale(path)
+    else:
+        main(path)

@@ -138,3 +138,33 @@ def test_quadcubic_kat_fingerprint(golden):
     exact = np.prod(g["kat4_q"], axis=1)
     err = np.abs(r["norms"][:, 0] - exact).max()
     assert err > 1e-9     # a correct quadcubic reproduces x*y*z*t; the row-240 D bug does not
+
+
+def test_scale_both_norm_vector(golden_scale):
+    """48^3 dipole field, 49,500 queries (faces, upper faces, sentinel rows,
+    NaN coordinates): the oracle against the reference in every vector mode."""
+    from conftest import c1s_field
+    g = golden_scale
+    f = c1s_field(g)
+    o = O.OracleTricubic(f, mode="both")
+    assert np.array_equal(o.nPos, g["c1_p_nPos"]) and o.nc == g["c1_p_nc"]
+    assert np.array_equal(np.array(o.h), g["c1_p_h"])
+    assert np.array_equal(o.basePointInds, g["c1_p_basePointInds"])
+    _check_range(o, g, "c1_both_", g["c1_q"])
+    r = O.OracleTricubic(f, mode="norm").query(g["c1_q"].copy())
+    for k in ("norms", "grads"):
+        assert (normwise(r[k], g["c1_both_" + k]) <= 1e-13).all()
+    r = O.OracleTricubic(f, mode="vector").query(g["c1_q"].copy())
+    ref = g["c1_vector_comps"]
+    assert np.array_equal(np.isnan(r["comps"]), np.isnan(ref))
+    assert (normwise(r["comps"], ref) <= 1e-13).all()
+
+
+def test_scale_quadcubic(golden_scale):
+    from conftest import c2s_field
+    g = golden_scale
+    o = O.OracleQuadcubic(c2s_field(g))
+    assert o.nc == g["c2_p_nc"]
+    # 256-term sums in another order than the reference's (ARBInterp.py:1180-1188):
+    # gradients agree to ~2e-13 normwise on this grid, well inside the 1e-12 bar
+    _check_range(o, g, "c2_", g["c2_q"], tol=5e-13)
