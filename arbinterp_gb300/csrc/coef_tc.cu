@@ -146,6 +146,12 @@ __device__ __forceinline__ void load_line(const float *hp, const float *lp, bool
 
 }  // namespace
 
+// Poll limit of the MMA-completion wait in coef3_tc's tile loop.  It is
+// WAIT_LIMIT unless a test lowers it (arb_test_set_mma_wait_limit) to make
+// that wait run out; the drain wait before the accumulator columns are
+// released always keeps WAIT_LIMIT, so no MMA is in flight at kernel exit.
+static __device__ uint32_t g_mma_wait_limit = WAIT_LIMIT;
+
 template <int F>
 __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__ CUtensorMap tmap, arb_grid g,
                                                          int64_t cell0, int64_t ncells, int32_t *status) {
@@ -184,6 +190,7 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
   unsigned char *st_row = sm.stage[half] + row * 128;
   uint32_t parity = 0;
   bool timed_out = false;
+  const uint32_t mma_wait_limit = g_mma_wait_limit;
 
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t r = tile * TM + row;
@@ -263,7 +270,7 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
         }
       tc::mma_commit(&sm.mbar);
     }
-    const bool ok = tc::mbar_wait_bounded(&sm.mbar, parity, WAIT_LIMIT);
+    const bool ok = tc::mbar_wait_bounded(&sm.mbar, parity, mma_wait_limit);
     parity ^= 1u;
     if (!ok) set_status(status, ARB_ERR_TIMEOUT);
     tc::tc_fence_after();
@@ -331,6 +338,13 @@ static EncodeTiled encode_fn() {
       fn = reinterpret_cast<EncodeTiled>(p);
   });
   return fn;
+}
+
+// Test hook: sets the poll limit of coef3_tc's MMA-completion wait on the
+// current device (limit < 0 restores the default).
+extern "C" int arb_test_set_mma_wait_limit(int64_t limit) {
+  const uint32_t v = limit < 0 ? WAIT_LIMIT : (limit > (int64_t)WAIT_LIMIT ? WAIT_LIMIT : (uint32_t)limit);
+  return cudaMemcpyToSymbol(g_mma_wait_limit, &v, sizeof(v)) == cudaSuccess ? ARB_OK : ARB_ERR_CUDA;
 }
 
 // Host launcher used by arb_coef_solve for 3D mixed precision.  The table is

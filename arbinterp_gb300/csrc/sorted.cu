@@ -22,6 +22,8 @@
 // pass cost three partial-sector writes per query, the record one full one.
 // The evaluation pass does no float64 arithmetic and no integer division in
 // mixed precision.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "eval.cuh"
@@ -983,29 +985,55 @@ using namespace arb;
 // Scratch of arb_query_eval_sorted_noalloc: a file-scope device array that
 // every GPU which loads this library holds until the process exits.  Host code
 // must not pass the symbol itself to a kernel (on the host it is only a
-// stand-in); its device address is looked up once per device.
+// stand-in); its device address is looked up with cudaGetSymbolAddress, with
+// the device current, the first time that device's context calls, and again
+// only if the device's context has changed since (a cudaDeviceReset loads the
+// module anew, at a possibly different address).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[ARB_NOALLOC_SCRATCH_BYTES];
+
+// Unique id of the calling thread's current context (0 if none or unknown).
+static unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult r;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &r) == cudaSuccess &&
+        r == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(p);
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &r) == cudaSuccess &&
+        r == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(p);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) != CUDA_SUCCESS)
+    id = 0;
+  return id;
+}
 
 static void *noalloc_scratch(int *rc) {
   static std::mutex mu;
-  static void *ptrs[64] = {};
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) {
+  static void *ptrs[MAX_DEVICES] = {};
+  static unsigned long long ctx_ids[MAX_DEVICES] = {};
+  const int dev = current_device();
+  if (dev < 0) {
     *rc = ARB_ERR_CUDA;
     return nullptr;
   }
-  if (dev < 0 || dev >= 64) {
-    *rc = ARB_ERR_UNSUPPORTED;
-    return nullptr;
-  }
+  const unsigned long long id = current_context_id();
   std::lock_guard<std::mutex> lock(mu);
-  if (!ptrs[dev]) {
+  if (!ptrs[dev] || ctx_ids[dev] != id) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
       *rc = ARB_ERR_CUDA;
       return nullptr;
     }
     ptrs[dev] = p;
+    ctx_ids[dev] = current_context_id();  // the lookup may have made the primary context current
   }
   return ptrs[dev];
 }
@@ -1128,12 +1156,13 @@ extern "C" int arb_query_eval_sorted_noalloc(const arb_grid *g, int32_t precisio
                                              double *q, int64_t nq, int64_t q_stride, int32_t q_writeback,
                                              const arb_query_out *out, int32_t *status,
                                              arb_stream_t stream) {
-  if (!g || nq < 0) return ARB_ERR_INVALID;
+  int rc = check_query_args(g, q, nq, q_stride, out);
+  if (rc) return rc;
   if (nq == 0) return ARB_OK;
+  if (!status) return ARB_ERR_INVALID;
   const size_t need = arb_query_sorted_work_bytes(g, precision, nq);
   if (need == 0) return ARB_ERR_INVALID;
   if (need > (size_t)ARB_NOALLOC_SCRATCH_BYTES) return ARB_ERR_CAPACITY;
-  int rc = ARB_OK;
   void *ws = noalloc_scratch(&rc);
   if (!ws) return rc;
   return arb_query_eval_sorted(g, precision, use_table, q, nq, q_stride, q_writeback, out, ws, need,

@@ -368,6 +368,12 @@ class _Interpolant:
                               self._table.data_ptr() + cell0 * self._F * self._M * self._table.element_size(),
                               self._status.data_ptr(), _stream())
         check(rc, "arb_coef_solve")
+        if self.precision == "mixed":
+            # the tensor-core solve reports a bounded device wait that ran out
+            # in the status word; its rows are then not trustworthy
+            st = self._fetch_status()
+            if st & _lib.ARB_ERR_TIMEOUT:
+                raise RuntimeError("arb_coef_solve: " + _lib.describe(st))
         self._solved[cell0:cell0 + ncells] = True
 
     def allCoeffs(self):

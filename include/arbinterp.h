@@ -268,13 +268,16 @@ int arb_query_eval_binned(const arb_grid *g, int32_t precision, int32_t use_tabl
  *      scratch is a fixed array inside the library: ARB_NOALLOC_SCRATCH_BYTES
  *      on every GPU that loads the library, held until the process exits.
  *      Calls whose scratch need (arb_query_sorted_work_bytes) exceeds it
- *      return ARB_ERR_CAPACITY without touching the GPU — about 2e5 query
- *      rows per call in float64 and 3e5 in mixed precision on a 256^3 grid;
- *      split larger query sets into several calls.
+ *      return ARB_ERR_CAPACITY without touching the GPU — on a 256^3 grid
+ *      (32768 bins) at most 346,789 query rows per call in float64 and
+ *      520,184 in mixed precision (48- and 32-byte records); split larger
+ *      query sets into several calls.  Arguments are checked first, as
+ *      arb_query_eval_sorted checks them.
  *
  *      The first call on a device looks up the array's device address (once
  *      per device, with that device current); make that first call before
- *      any stream capture.  Nothing is allocated: no cudaMalloc, no
+ *      any stream capture.  The lookup is repeated only if the device's
+ *      context changed since (after a cudaDeviceReset).  Nothing is allocated: no cudaMalloc, no
  *      cudaFree, no allocating library call.  Every call shares the one
  *      array and leaves its contents behind; each call clears what must start
  *      at zero.  Calls that overlap on the GPU (other streams, other host
@@ -342,6 +345,15 @@ int arb_csv_split(const uint8_t *text, int64_t nbytes, int64_t nlines, int32_t d
 int arb_csv_parse(const uint8_t *text, int64_t nbytes, int64_t nlines, int32_t delimiter, int32_t comment,
                   void *lines_work, size_t lines_work_bytes, const int32_t *nvals, double *out, int64_t nrows,
                   int64_t ncols, arb_csv_info *info, arb_stream_t stream);
+
+/* Test hook, no counterpart in the reference: sets the poll limit of the
+ * 3D tensor-core solve's MMA-completion wait (arb_coef_solve, mixed
+ * precision) on the current device; limit < 0 restores the default (2^22
+ * polls).  With a limit of 0 that wait gives up at once: the kernel ORs
+ * ARB_ERR_TIMEOUT into the status word, waits (with the full limit) for the
+ * MMAs it issued, releases its tensor memory and returns.  Tests use it to
+ * exercise the timeout path without faulting or hanging the GPU. */
+int arb_test_set_mma_wait_limit(int64_t limit);
 
 /* Reads (and clears) the device status word after the stream's work is
  * done; returns ARB_OK, an arb_status bit set, or ARB_ERR_CUDA. */

@@ -58,3 +58,25 @@ def test_import_paths():
     from ARBTools.ARBInterp import tricubic as T
     assert A.__version__ == "1.8" and A.tricubic is T
     assert A.tricubic.__version__ == "1.8" and A.quadcubic.__version__ == "1.8"
+
+
+def test_noalloc_capacity_stated_in_header():
+    """The per-call row limits that include/arbinterp.h states for the
+    allocation-free entry point on a 256^3 grid are the real ones: the last
+    stated row count fits ARB_NOALLOC_SCRATCH_BYTES and one more does not
+    (a host-side size computation; no CUDA call)."""
+    from arbinterp_gb300 import _lib
+    src = open(os.path.join(ROOT, "include", "arbinterp.h")).read()
+    cap = eval(re.search(r"#define ARB_NOALLOC_SCRATCH_BYTES \((\d+)u << (\d+)\)", src).expand(r"\1 << \2"))
+    m = re.search(r"at most ([\d,]+) query[\s*]+rows per call in float64 and[\s*]+([\d,]+) in mixed", src)
+    assert m, "row limits not found in the header"
+    stated = [int(m.group(1).replace(",", "")), int(m.group(2).replace(",", ""))]
+    L = _lib.lib()
+    g = _lib.ArbGrid()
+    g.dim, g.kind, g.nfield = 3, _lib.KIND_BOTH, 4
+    for a in range(3):
+        g.n[a] = 256
+    g.n[3] = 1
+    g.nc = 253 ** 3
+    for prec, rows in zip((_lib.PREC_FP64, _lib.PREC_MIXED), stated):
+        assert L.arb_query_sorted_work_bytes(g, prec, rows) <= cap < L.arb_query_sorted_work_bytes(g, prec, rows + 1)

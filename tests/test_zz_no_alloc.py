@@ -8,6 +8,8 @@ ARB_NOALLOC_SCRATCH_BYTES per GPU.  This test calls that entry point through
 the C ABI twice in a row, on different query sets, and checks each result
 against the workspace entry point (arb_query_eval_sorted) on the same
 inputs: identical cell indices, out-of-volume rows, NaN masks and values.
+It covers 3D vector ('both'), 3D scalar and 4D scalar fields, evaluating on
+the fly and from a coefficient table.
 
 It sits in a file of its own, collected last, and works alone in a fresh
 process as well as after the other tests."""
@@ -27,12 +29,12 @@ def _setup():
     return torch, _lib, _lib.lib()
 
 
-def _run(torch, _lib, L, o, q, entry, ws=None):
-    n = q.shape[0]
+def _run(torch, _lib, L, o, q, entry, use_table):
+    n, d = q.shape[0], o._dim
     f64 = dict(dtype=torch.float64, device="cuda")
     comps = torch.full((n, 3), -7.0, **f64)
     norms = torch.full((n, 1), -7.0, **f64)
-    grads = torch.full((n, 3), -7.0, **f64)
+    grads = torch.full((n, d), -7.0, **f64)
     inds = torch.full((n,), -7, dtype=torch.int64, device="cuda")
     oob = torch.full((n,), -1, dtype=torch.int64, device="cuda")
     cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
@@ -45,10 +47,10 @@ def _run(torch, _lib, L, o, q, entry, ws=None):
     if entry == "workspace":
         need = int(L.arb_query_sorted_work_bytes(o._g, prec, n))
         ws = torch.empty(need, dtype=torch.uint8, device="cuda")
-        rc = L.arb_query_eval_sorted(o._g, prec, 0, qq.data_ptr(), n, 3, 1, out, ws.data_ptr(), need,
+        rc = L.arb_query_eval_sorted(o._g, prec, use_table, qq.data_ptr(), n, d, 1, out, ws.data_ptr(), need,
                                      status.data_ptr(), stream)
     else:
-        rc = L.arb_query_eval_sorted_noalloc(o._g, prec, 0, qq.data_ptr(), n, 3, 1, out,
+        rc = L.arb_query_eval_sorted_noalloc(o._g, prec, use_table, qq.data_ptr(), n, d, 1, out,
                                              status.data_ptr(), stream)
     assert rc == _lib.ARB_OK, (entry, rc)
     assert L.arb_status_fetch(status.data_ptr(), stream) == _lib.ARB_OK
@@ -58,19 +60,41 @@ def _run(torch, _lib, L, o, q, entry, ws=None):
             "q": qq.cpu().numpy()}
 
 
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_noalloc_matches_workspace_entry_point_twice(prec):
+def _field(case):
+    from arbinterp_gb300 import quadcubic, synth, tricubic
+    kind, prec, table = case
+    if kind == "both":
+        o = tricubic(synth.dipole_field3(n=(40, 36, 44), seed=12).numpy(), "quiet", mode="both", precision=prec)
+    elif kind == "scalar":
+        o = tricubic(synth.gaussian_field3(n=(38, 41, 35), seed=14).numpy(), "quiet", precision=prec)
+    else:
+        o = quadcubic(synth.moving_gaussian_field4(n=(14, 13, 15, 11), seed=15).numpy(), "quiet", precision=prec)
+    if table:
+        o.allCoeffs()
+    return o
+
+
+# 3D 'both' (the 8-lane bin kernel in mixed precision), a 3D scalar field,
+# a 4D scalar field and the coefficient-table strategy: each carves the
+# shared array differently
+CASES = [("both", "fp64", 0), ("both", "mixed", 0), ("both", "mixed", 1), ("scalar", "mixed", 0),
+         ("scalar", "fp64", 1), ("quad", "mixed", 0), ("quad", "fp64", 1)]
+
+
+@pytest.mark.parametrize("case", CASES, ids=["-".join(map(str, c)) for c in CASES])
+def test_noalloc_matches_workspace_entry_point_twice(case):
     torch, _lib, L = _setup()
-    from arbinterp_gb300 import synth, tricubic
-    f = synth.dipole_field3(n=(40, 36, 44), seed=12).numpy()
-    o = tricubic(f, "quiet", mode="both", precision=prec)
-    lo = [o.xIntMin, o.yIntMin, o.zIntMin]
-    hi = [o.xIntMax, o.yIntMax, o.zIntMax]
-    h = [o.hx, o.hy, o.hz]
+    from arbinterp_gb300 import synth
+    o = _field(case)
+    d = o._dim
+    names = "xyzt"[:d]
+    lo = [getattr(o, a + "IntMin") for a in names]
+    hi = [getattr(o, a + "IntMax") for a in names]
+    h = [getattr(o, "h" + a) for a in names]
     for call, n_in in enumerate((60000, 25000)):     # two calls in a row, different sizes
         q = synth.uniform_queries(lo, hi, n_in, n_in // 100, h, seed=70 + call, device="cuda")
-        want = _run(torch, _lib, L, o, q, "workspace")
-        got = _run(torch, _lib, L, o, q, "noalloc")
+        want = _run(torch, _lib, L, o, q, "workspace", case[2])
+        got = _run(torch, _lib, L, o, q, "noalloc", case[2])
         assert np.array_equal(got["inds"], want["inds"])
         assert np.array_equal(got["oob"], want["oob"]) and len(got["oob"]) > 0
         assert np.array_equal(got["q"], want["q"], equal_nan=True)
@@ -88,10 +112,17 @@ def test_noalloc_rejects_oversized_calls():
     n = 1
     while int(L.arb_query_sorted_work_bytes(o._g, _lib.PREC_FP64, n)) <= limit:
         n *= 2
-    q = torch.zeros((1, 3), dtype=torch.float64, device="cuda")
-    out = _lib.ArbQueryOut(None, None, None, None, None, None)
+    # valid arguments throughout: the size alone is refused, on the host,
+    # before any device work (none of these buffers is touched)
+    f64 = dict(dtype=torch.float64, device="cuda")
+    q = torch.zeros((1, 3), **f64)
+    comps, norms, grads = torch.zeros((1, 3), **f64), torch.zeros((1, 1), **f64), torch.zeros((1, 3), **f64)
+    out = _lib.ArbQueryOut(comps.data_ptr(), norms.data_ptr(), grads.data_ptr(), None, None, None)
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
-    # rejected on the host before any device work (q is never read)
     rc = L.arb_query_eval_sorted_noalloc(o._g, _lib.PREC_FP64, 0, q.data_ptr(), n, 3, 0, out,
                                          status.data_ptr(), torch.cuda.current_stream().cuda_stream)
     assert rc == _lib.ARB_ERR_CAPACITY
+    # and a call with a bad argument is refused as invalid whatever its size
+    rc = L.arb_query_eval_sorted_noalloc(o._g, _lib.PREC_FP64, 0, q.data_ptr(), n, 2, 0, out,
+                                         status.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.ARB_ERR_INVALID
