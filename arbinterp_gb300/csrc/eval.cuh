@@ -218,6 +218,10 @@ struct Grid32Block3 {  // the mixed grid in global memory
   __device__ __forceinline__ float2 hl(int64_t p) const { return __ldg(reinterpret_cast<const float2 *>(g32) + p); }
   __device__ __forceinline__ float4 hi4(int64_t p) const { return __ldg(reinterpret_cast<const float4 *>(g32) + p); }
   __device__ __forceinline__ float lo(int64_t p) const { return __ldg(g32 + npts * 4 + p); }
+  __device__ __forceinline__ void lo_row(int64_t p, float l[4]) const {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) l[i] = __ldg(g32 + npts * 4 + p + i);
+  }
   template <int F>
   __device__ __forceinline__ void load(int64_t p, int f, float &h, float &l) const {
     g32_load<F>(g32, npts, p, f, h, l);
@@ -329,6 +333,147 @@ __device__ __forceinline__ void eval_otf3_mixed_block(const BLK &blk, const KPar
   grad[2] = f2d_exact(gz * kp.inv_hf[2]);
 }
 
+// Packed float32 pairs (.f32x2): one instruction computes both components
+// with the rounding of the scalar operation.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+
+// 'both' fields (three components, values only, and |B| with its gradient),
+// float32.  |B| is hi + lo per point.  The lo words (|lo| <= ulp(hi) / 2)
+// are contracted as they are: their rounding errors are ~2^-24 of a quantity
+// already ~2^-24 of |B|.  The hi words carry the variation, so each gradient
+// component is formed from hi differences along its own axis (exact by
+// Sterbenz's lemma where neighbouring values are within a factor of 2, and
+// otherwise rounded relative to the difference itself):
+//   d/dx from x-local differences hi[k][j][i] - hi[k][j][1],
+//   d/dy from y-local differences hi[k][j][i] - hi[k][1][i],
+//   d/dz from z-local differences hi[k][j][i] - hi[1][j][i],
+// and the value from the x-local differences plus each row's own difference
+// to the cell corner (1, 1, 1).  Components accumulate their float32 values
+// directly.  Planes and rows are visited in the order 1, 0, 2, 3 so the
+// references come first; pairs of products share one .f32x2 instruction.
+// BLK as for eval_otf3_mixed_block (at, hi4, lo), plus lo_row(index, l):
+// the lo words of the four points of an x-row from its first point.
+template <class BLK>
+__device__ __forceinline__ void eval_otf3_both_block(const BLK &blk, const KParams &kp, const float frac[3],
+                                                     double val[4], double grad[3]) {
+  float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
+  cr_weights<float>(frac[0], wx);
+  cr_weights<float>(frac[1], wy);
+  cr_weights<float>(frac[2], wz);
+  cr_dweights<float>(frac[0], dx);
+  cr_dweights<float>(frac[1], dy);
+  cr_dweights<float>(frac[2], dz);
+  const auto pc = blk.at(1, 1, 1);
+  const float hc = blk.hi4(pc).w;
+  float zr[4][4], yr[4];                     // hi of plane 1 (z references), of row 1 (y references)
+  float2 Cxy = make_float2(0.f, 0.f);        // components
+  float Cz = 0.f;
+  float V = 0.f, GX = 0.f, GY = 0.f, GZ = 0.f;   // hi part: value (relative to the corner), gradients
+  float LV = 0.f, LX = 0.f, LY = 0.f, LZ = 0.f;  // lo part
+  constexpr int ORD[4] = {1, 0, 2, 3};
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk) {
+    const int k = ORD[kk];
+    float2 cxy = make_float2(0.f, 0.f);
+    float cz = 0.f, vp = 0.f, xp = 0.f, yp = 0.f, zp = 0.f, lp = 0.f, lxp = 0.f, lyp = 0.f;
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = ORD[jj];
+      const auto p = blk.at(0, j, k);
+      float4 a[4];
+      float l[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = blk.hi4(p + i);
+      blk.lo_row(p, l);
+      float h[4] = {a[0].w, a[1].w, a[2].w, a[3].w};
+      if (k == 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) zr[j][i] = h[i];
+      }
+      if (j == 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) yr[i] = h[i];
+      }
+      // components, and the lo words for the value (wx) and d/dx (dx)
+      float2 rxy = make_float2(0.f, 0.f), rzl = make_float2(0.f, 0.f);
+      float rlx = 0.f;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        rxy = ffma2(make_float2(wx[i], wx[i]), make_float2(a[i].x, a[i].y), rxy);
+        rzl = ffma2(make_float2(wx[i], wx[i]), make_float2(a[i].z, l[i]), rzl);
+        rlx = fmaf(dx[i], l[i], rlx);
+      }
+      // x-local differences: the value (plus the row's offset to the corner) and d/dx
+      const float2 e02 = fsub2(make_float2(h[0], h[2]), make_float2(h[1], h[1]));
+      const float e3 = h[3] - h[1];
+      float2 vx = make_float2(h[1] - hc, 0.f);
+      vx = ffma2(make_float2(wx[0], dx[0]), make_float2(e02.x, e02.x), vx);
+      vx = ffma2(make_float2(wx[2], dx[2]), make_float2(e02.y, e02.y), vx);
+      vx = ffma2(make_float2(wx[3], dx[3]), make_float2(e3, e3), vx);
+      // y-local and z-local differences, contracted along x
+      float ry = 0.f, rz = 0.f;
+      if (j != 1 && k != 1) {
+        float2 yz = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          yz = ffma2(make_float2(wx[i], wx[i]), fsub2(make_float2(h[i], h[i]), make_float2(yr[i], zr[j][i])), yz);
+        ry = yz.x;
+        rz = yz.y;
+      } else if (j != 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) ry = fmaf(wx[i], h[i] - yr[i], ry);
+      } else if (k != 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) rz = fmaf(wx[i], h[i] - zr[j][i], rz);
+      }
+      // along y
+      cxy = ffma2(make_float2(wy[j], wy[j]), rxy, cxy);
+      cz = fmaf(wy[j], rzl.x, cz);
+      vp = fmaf(wy[j], vx.x, vp);
+      xp = fmaf(wy[j], vx.y, xp);
+      yp = fmaf(dy[j], ry, yp);
+      zp = fmaf(wy[j], rz, zp);
+      lp = fmaf(wy[j], rzl.y, lp);
+      lxp = fmaf(wy[j], rlx, lxp);
+      lyp = fmaf(dy[j], rzl.y, lyp);
+    }
+    // along z
+    Cxy = ffma2(make_float2(wz[k], wz[k]), cxy, Cxy);
+    Cz = fmaf(wz[k], cz, Cz);
+    V = fmaf(wz[k], vp, V);
+    GX = fmaf(wz[k], xp, GX);
+    GY = fmaf(wz[k], yp, GY);
+    GZ = fmaf(dz[k], zp, GZ);
+    LV = fmaf(wz[k], lp, LV);
+    LX = fmaf(wz[k], lxp, LX);
+    LY = fmaf(wz[k], lyp, LY);
+    LZ = fmaf(dz[k], lp, LZ);
+  }
+  val[0] = f2d_exact(Cxy.x);
+  val[1] = f2d_exact(Cxy.y);
+  val[2] = f2d_exact(Cz);
+  val[3] = f2d_exact(hc + (V + LV));
+  grad[0] = f2d_exact((GX + LX) * kp.inv_hf[0]);
+  grad[1] = f2d_exact((GY + LY) * kp.inv_hf[1]);
+  grad[2] = f2d_exact((GZ + LZ) * kp.inv_hf[2]);
+}
+
 template <int F>
 __device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KParams &kp, const int64_t c[3],
                                                      const float frac[3], double val[F], double grad[3]) {
@@ -339,7 +484,10 @@ __device__ __forceinline__ void eval_otf3_mixed_grad(const arb_grid &g, const KP
   blk.sy = nx;
   blk.sz = nx * ny;
   blk.base = (c[2] * ny + c[1]) * nx + c[0];
-  eval_otf3_mixed_block<F>(blk, kp, frac, val, grad);
+  if constexpr (F == 4)
+    eval_otf3_both_block(blk, kp, frac, val, grad);
+  else
+    eval_otf3_mixed_block<F>(blk, kp, frac, val, grad);
 }
 
 // Vector fields (values only) in float32: corner deltas of the three

@@ -52,17 +52,28 @@ struct __align__(16) QRec<double> {
 static_assert(sizeof(QRec<float>) == 32 && sizeof(QRec<double>) == 48, "record sizes");
 
 struct SortedWork {
-  uint32_t *hist;  // nbins + 1: counts, exclusive offsets after the scan, bin ends after placement
-  void *rec;       // nq records (QRec<float> or QRec<double>), bin order
+  uint32_t *hist;  // nsub + 1: counts, exclusive offsets after the scan, sub-bin ends after placement
+  uint32_t *part;  // per-block totals of the scan
+  void *rec;       // nq records (QRec<float> or QRec<double>), sub-bin order
 };
 
 struct BinGeom {
   int64_t nb[4];     // bins per axis
-  int64_t nbins;     // product (the special bin is index nbins)
+  int64_t nbins;     // product
   int shift;         // log2 cells per bin edge
+  int cls;           // log2 bank classes per bin (3: 3D mixed 8^3-cell bins; 0 otherwise)
+  int64_t nsub;      // nbins << cls sub-bins (bin-major); the special sub-bin is index nsub
 };
 
-static inline BinGeom bin_geom(const arb_grid *g) {
+// Bank class of a cell inside its 8^3-cell bin: the 16-byte bank group
+// (mod 8) of the cell's corner point in an unpadded 11 x 11 x 11 tile
+// (x + 11 y + 121 z, with 11 = 3 and 121 = 1 mod 8).  The bin origin is a
+// multiple of 8 on every axis, so the global cell coordinates give it.
+__host__ __device__ __forceinline__ int bank_class(int64_t cx, int64_t cy, int64_t cz) {
+  return (int)((cx + 3 * cy + cz) & 7);
+}
+
+static inline BinGeom bin_geom(const arb_grid *g, int precision) {
   BinGeom b;
   b.shift = (g->bin_shift > 0 && g->bin_shift <= 8) ? g->bin_shift : (g->dim == 3 ? 3 : 2);
   b.nbins = 1;
@@ -75,13 +86,22 @@ static inline BinGeom bin_geom(const arb_grid *g) {
     }
     b.nbins *= b.nb[a];
   }
+  b.cls = (g->dim == 3 && precision == ARB_PREC_MIXED && b.shift == 3) ? 3 : 0;
+  b.nsub = b.nbins << b.cls;
   return b;
 }
 
 static inline size_t align_up(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Exclusive scan of the sub-bin histogram: SCAN_THREADS x SCAN_PER counters
+// per block, two launches (block totals, then the scan with carry-in).
+constexpr int SCAN_THREADS = 1024, SCAN_PER = 8;
+constexpr int64_t SCAN_CHUNK = (int64_t)SCAN_THREADS * SCAN_PER;
+
+static inline int64_t scan_blocks(int64_t n) { return (n + SCAN_CHUNK - 1) / SCAN_CHUNK; }
+
 static size_t carve(SortedWork *w, void *base, const arb_grid *g, int precision, int64_t nq) {
-  const BinGeom bg = bin_geom(g);
+  const BinGeom bg = bin_geom(g, precision);
   const size_t tsz = precision == ARB_PREC_MIXED ? 4 : 8;
   size_t off = 0;
   char *p = (char *)base;
@@ -91,7 +111,8 @@ static size_t carve(SortedWork *w, void *base, const arb_grid *g, int precision,
     return r;
   };
   SortedWork t;
-  t.hist = (uint32_t *)take(sizeof(uint32_t) * (bg.nbins + 1));
+  t.hist = (uint32_t *)take(sizeof(uint32_t) * (bg.nsub + 1));
+  t.part = (uint32_t *)take(sizeof(uint32_t) * scan_blocks(bg.nsub + 1));
   t.rec = take((tsz == 4 ? sizeof(QRec<float>) : sizeof(QRec<double>)) * nq);
   if (w) *w = t;
   return off;
@@ -111,7 +132,7 @@ __device__ __forceinline__ CoordStep bin_step(const arb_grid &g, const KParams &
     s = coord_step<DIM, true>(qv, g, kp.inv_h, frac);
   else
     s = coord_step_fast<DIM>(qv, kp.ax, g, frac);
-  bin = bg.nbins;
+  bin = bg.nsub;
   bad_index = false;
   if (s.oob || s.nan) {
     cw = CELL_SPECIAL;
@@ -127,6 +148,9 @@ __device__ __forceinline__ CoordStep bin_step(const arb_grid &g, const KParams &
     bin = c[DIM - 1] >> bg.shift;
 #pragma unroll
     for (int a = DIM - 2; a >= 0; --a) bin = bin * bg.nb[a] + (c[a] >> bg.shift);
+    if constexpr (DIM == 3) {
+      if (bg.cls) bin = (bin << 3) | bank_class(c[0], c[1], c[2]);
+    }
   }
   return s;
 }
@@ -181,26 +205,78 @@ __global__ void __launch_bounds__(256) bin_place_kernel(arb_grid g, KParams kp, 
   }
 }
 
-// Exclusive scan of n counters in one block (n up to a few million).
-__global__ void __launch_bounds__(1024) scan_kernel(uint32_t *hist, int64_t n) {
-  __shared__ uint32_t part[1024];
-  const int64_t per = (n + blockDim.x - 1) / blockDim.x;
-  const int64_t b = threadIdx.x * per, e = min(b + per, n);
+// Block totals of the histogram chunks (SCAN_CHUNK counters per block).
+__global__ void __launch_bounds__(SCAN_THREADS) scan_part_kernel(const uint32_t *hist, int64_t n, uint32_t *part) {
+  __shared__ uint32_t wsum[SCAN_THREADS / 32];
+  const int64_t b = blockIdx.x * SCAN_CHUNK + (int64_t)threadIdx.x * SCAN_PER;
   uint32_t sum = 0;
-  for (int64_t k = b; k < e; ++k) sum += hist[k];
-  part[threadIdx.x] = sum;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER; ++k)
+    if (b + k < n) sum += hist[b + k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = sum;
   __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    const uint32_t v = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0u;
-    __syncthreads();
-    part[threadIdx.x] += v;
-    __syncthreads();
+  if (threadIdx.x < 32) {
+    uint32_t v = wsum[threadIdx.x];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
   }
-  uint32_t run = part[threadIdx.x] - sum;
-  for (int64_t k = b; k < e; ++k) {
-    const uint32_t c = hist[k];
-    hist[k] = run;
-    run += c;
+}
+
+// Exclusive scan of each chunk, offset by the totals of the chunks before it.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(uint32_t *hist, int64_t n, const uint32_t *part) {
+  __shared__ uint32_t wsum[SCAN_THREADS / 32];
+  __shared__ uint32_t carry_s;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // carry-in: the totals of the chunks before this one
+  uint32_t c = 0;
+  for (int64_t k = threadIdx.x; k < blockIdx.x; k += SCAN_THREADS) c += part[k];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0) wsum[warp] = c;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t v = wsum[lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) carry_s = v;
+  }
+  __syncthreads();
+  const uint32_t carry = carry_s;
+  __syncthreads();  // wsum is reused below
+  const int64_t b = blockIdx.x * SCAN_CHUNK + (int64_t)threadIdx.x * SCAN_PER;
+  uint32_t v[SCAN_PER], sum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER; ++k) {
+    v[k] = b + k < n ? hist[b + k] : 0u;
+    sum += v[k];
+  }
+  // inclusive warp scan of the thread totals, then of the warp totals
+  uint32_t incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t x = wsum[lane], xi = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += y;
+    }
+    wsum[lane] = xi - x;  // exclusive prefix of the warp totals
+  }
+  __syncthreads();
+  uint32_t run = carry + wsum[warp] + (incl - sum);
+#pragma unroll
+  for (int k = 0; k < SCAN_PER; ++k) {
+    if (b + k < n) hist[b + k] = run;
+    run += v[k];
   }
 }
 
@@ -236,129 +312,41 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
   write_vals<DIM, F>(o, i, val, grad);
 }
 
-// 3D, four fields ('both' mode), mixed precision: 4 lanes per query, lane
-// s owning grid point s of every x-row.  A row is 4 points x float4
-// (hi_x, hi_y, hi_z, hi_n) = 64 bytes plus 4 x float lo_n, so the 4 lanes of
-// a query read it with one 16-byte and one 4-byte load each.  Each lane
-// contracts its 16 rows over y and z (components from their float32 values
-// as deltas to the cell corner; |B| from (hi, lo) deltas so its gradient keeps
-// full precision), then the 4 lanes reduce over x with two butterfly
-// shuffles.  Each block walks COOP_CHUNK consecutive sorted queries (about
-// one spatial bin) so the bin's grid footprint stays in that SM's L1.
-constexpr int COOP_CHUNK = 256;
-
-__global__ void __launch_bounds__(256) eval_sorted_coop4_kernel(arb_grid g, KParams kp, int64_t nq,
-                                                                arb_query_out o, SortedWork w) {
-  const int lane = threadIdx.x & 31;
-  const int p = lane & 3;
-  const int64_t t0 = (int64_t)blockIdx.x * COOP_CHUNK;
-  const int64_t t1 = min(t0 + COOP_CHUNK, nq);
-  const int64_t nx = g.n[0], ny = g.n[1];
-  const int64_t npts = grid_points(g);
-  const float4 *g4 = reinterpret_cast<const float4 *>(g.grid32);
-  const float *glo = g.grid32 + npts * 4;
-  const unsigned mask = 0xfu << (lane & 28);
-  for (int64_t t = t0 + (threadIdx.x >> 2); t < t1; t += blockDim.x >> 2) {  // groups stay converged
-    const QRec<float> r = reinterpret_cast<const QRec<float> *>(w.rec)[t];
-    const unsigned long long cw = r.cell;
-    const int64_t i = r.row;
-    if (cw & CELL_SPECIAL) {
-      if (p == 0) write_const<3, 4>(o, i, (cw & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
-      continue;
-    }
-    int64_t c[3];
-    unpack_cell<3>(cw, c);
-    const float fx = r.f[0], fy = r.f[1], fz = r.f[2];
-    float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
-    cr_weights<float>(fx, wx);
-    cr_dweights<float>(fx, dx);
-    cr_weights<float>(fy, wy);
-    cr_dweights<float>(fy, dy);
-    cr_weights<float>(fz, wz);
-    cr_dweights<float>(fz, dz);
-    const int64_t pref = ((c[2] + 1) * ny + (c[1] + 1)) * nx + (c[0] + 1);
-    const float4 ref = __ldg(g4 + pref);
-    const float rlo = __ldg(glo + pref);
-    float Sx = 0.f, Sy_ = 0.f, Sz_ = 0.f, Sn = 0.f, Gy = 0.f, Gz = 0.f;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int64_t pt = ((c[2] + k) * ny + (c[1] + j)) * nx + c[0] + p;
-        const float4 v = __ldg(g4 + pt);
-        const float lo = __ldg(glo + pt);
-        const float dn = (v.w - ref.w) + (lo - rlo);
-        const float wyz = wy[j] * wz[k];
-        Sx += wyz * (v.x - ref.x);
-        Sy_ += wyz * (v.y - ref.y);
-        Sz_ += wyz * (v.z - ref.z);
-        Sn += wyz * dn;
-        Gy += (dy[j] * wz[k]) * dn;
-        Gz += (wy[j] * dz[k]) * dn;
-      }
-    }
-    float Vx = wx[p] * Sx, Vy = wx[p] * Sy_, Vz = wx[p] * Sz_, Vn = wx[p] * Sn;
-    float Gx = dx[p] * Sn;
-    Gy *= wx[p];
-    Gz *= wx[p];
-#pragma unroll
-    for (int off = 1; off <= 2; off <<= 1) {
-      Vx += __shfl_xor_sync(mask, Vx, off);
-      Vy += __shfl_xor_sync(mask, Vy, off);
-      Vz += __shfl_xor_sync(mask, Vz, off);
-      Vn += __shfl_xor_sync(mask, Vn, off);
-      Gx += __shfl_xor_sync(mask, Gx, off);
-      Gy += __shfl_xor_sync(mask, Gy, off);
-      Gz += __shfl_xor_sync(mask, Gz, off);
-    }
-    const double nv = f2d_exact(ref.w + (rlo + Vn));
-    if (interleaved_rows<3, 4>(o)) {
-      if (p == 0)
-        st_v4(o.comps + i * 8, f2d_exact(ref.x + Vx), f2d_exact(ref.y + Vy), f2d_exact(ref.z + Vz), nv);
-      else if (p == 2)
-        st_v4(o.comps + i * 8 + 4, f2d_exact(Gx * kp.inv_hf[0]), f2d_exact(Gy * kp.inv_hf[1]),
-              f2d_exact(Gz * kp.inv_hf[2]), 0.0);
-    } else if (p == 0) {
-      if (o.comps) {
-        o.comps[i * o.comps_stride + 0] = f2d_exact(ref.x + Vx);
-        o.comps[i * o.comps_stride + 1] = f2d_exact(ref.y + Vy);
-        o.comps[i * o.comps_stride + 2] = f2d_exact(ref.z + Vz);
-      }
-    } else if (p == 1) {
-      if (o.norms) o.norms[i * o.norms_stride] = nv;
-    } else if (p == 2) {
-      if (o.grads) {
-        o.grads[i * o.grads_stride + 0] = f2d_exact(Gx * kp.inv_hf[0]);
-        o.grads[i * o.grads_stride + 1] = f2d_exact(Gy * kp.inv_hf[1]);
-        o.grads[i * o.grads_stride + 2] = f2d_exact(Gz * kp.inv_hf[2]);
-      }
-    }
-  }
-}
-
 // ---- bin-staged evaluation (3D, mixed, 8^3-cell bins) -------------------------
+// rQuery1/2/3 (ARBInterp.py:344-521) on the fly for the three field layouts
+// of mixed precision: F = 1 (scalar and norm fields: one (hi, lo) field),
+// F = 3 (vector fields: three components, values only) and F = 4 ('both':
+// three components plus |B| as (hi, lo)).
+//
 // One CTA per bin (round-robin over bins): the bin's footprint of 11^3 grid
 // points (8 cells + 3 per axis) is copied into shared memory with cp.async,
-// double-buffered so the next bin's copy overlaps this bin's queries, and
-// every query of the bin gathers its 4x4x4 block from shared memory.  Reading
-// the block from L1 instead costs ~3 L1 wavefronts per (query, x-row) because
-// the 8 queries of a warp touch 16 scattered 64-byte and 16-byte segments;
-// from shared memory it is about one.
+// double-buffered so the next bin's copy overlaps this bin's queries, and one
+// thread per query evaluates eval_otf3_mixed_block / eval_otf3_vec_block on
+// the staged block -- the code the global-memory kernels run, so binned and
+// unbinned queries return the same bits, and every gradient component is
+// differenced along its own axis first.
+//
+// Bank order.  The tile is unpadded, x fastest: point (x, y, z) at
+// x + 11 y + 121 z, so point (i, j, k) of the block of local cell
+// (cx, cy, cz) lies in 16-byte bank group (bank_class(cx, cy, cz) +
+// i + 3 j + k) mod 8.  The placement pass orders each bin's queries into
+// eight sub-bins by bank class, and each group of 8 consecutive threads takes
+// 8 queries of 8 distinct classes (round robin over the classes), so every
+// 8-thread phase of a 16-byte shared load touches 8 distinct bank groups: one
+// wavefront, where 8 random queries would need about three.  Where fewer
+// than 8 classes are left in a bin, its last queries conflict as random
+// queries would.
 constexpr int BIN_EDGE = 8;
 constexpr int TILE_EDGE = BIN_EDGE + 3;
 constexpr int TILE_PTS = TILE_EDGE * TILE_EDGE * TILE_EDGE;
+constexpr int BINC_THREADS = 128;
 
 template <int F>
 struct BinTile;
-// hi planes are 124 points apart (121 used): 124 * 16 B = 1984 B is 64 B
-// modulo the 128-byte bank cycle, so a query's x-rows in planes k and k+1
-// (read by one 8-thread phase of a 128-bit load) fall on complementary banks.
-constexpr int HI_PLANE = 124;
-constexpr int HI_PTS = TILE_EDGE * HI_PLANE;
 template <>
-struct BinTile<4> {          // (hi_x, hi_y, hi_z, hi_n) and lo_n per point
-  float4 hi[HI_PTS];         // [z][HI_PLANE] with rows of TILE_EDGE points
-  float lo[TILE_PTS];        // [z][y][x], unpadded
+struct BinTile<4> {          // (hi_x, hi_y, hi_z, hi_n) per point; lo_n of each point and of its x successor
+  float4 hi[TILE_PTS];
+  float2 lo2[TILE_PTS];      // lo2[e] = (lo_n[e], lo_n[e + 1]): an x-row's four lo words in two 8-byte loads
 };
 template <>
 struct BinTile<1> {          // (hi, lo) per point
@@ -409,210 +397,46 @@ __device__ __forceinline__ void load_bin_tile(const arb_grid &g, const BinGeom &
     const int64_t x = o[0] + lx, y = o[1] + ly, z = o[2] + lz;
     if (x >= nx || y >= ny || z >= nz) continue;
     const int64_t p = (z * ny + y) * nx + x;
-    if (F == 4) {
-      cp_async16(&reinterpret_cast<BinTile<4> &>(t).hi[lz * HI_PLANE + ly * TILE_EDGE + lx],
-                 reinterpret_cast<const float4 *>(g.grid32) + p);
-      cp_async4(&reinterpret_cast<BinTile<4> &>(t).lo[e], g.grid32 + npts * 4 + p);
-    } else if (F == 3) {
-      cp_async16(&reinterpret_cast<BinTile<3> &>(t).v[e], reinterpret_cast<const float4 *>(g.grid32) + p);
+    if constexpr (F == 4) {
+      cp_async16(&t.hi[e], reinterpret_cast<const float4 *>(g.grid32) + p);
+      cp_async4(&t.lo2[e].x, g.grid32 + npts * 4 + p);
+      if (lx + 1 < TILE_EDGE && x + 1 < nx) cp_async4(&t.lo2[e].y, g.grid32 + npts * 4 + p + 1);
+    } else if constexpr (F == 3) {
+      cp_async16(&t.v[e], reinterpret_cast<const float4 *>(g.grid32) + p);
     } else {
-      cp_async8(&reinterpret_cast<BinTile<1> &>(t).v[e], reinterpret_cast<const float2 *>(g.grid32) + p);
+      cp_async8(&t.v[e], reinterpret_cast<const float2 *>(g.grid32) + p);
     }
   }
 }
 
-// Packed float32 FMA on (x, y) pairs: d = a * b + c per component.
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
-  float2 d;
-  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
-      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
-      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-      : "=f"(d.x), "=f"(d.y)
-      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-  return d;
-}
-
 template <int F>
-__global__ void __launch_bounds__(256, 4) eval_bin_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
-                                                       arb_query_out o, SortedWork w) {
-  extern __shared__ __align__(16) unsigned char bin_smem[];
-  BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(bin_smem);
-  const int lane = threadIdx.x & 31;
-  const int g8 = lane & 7;        // lane within the query's group; also the output column it writes
-  const int p = lane & 3;         // x offset in the 4x4x4 block
-  const int h = g8 >> 2;          // z parity: this lane reads planes h and h + 2
-  const unsigned mask = 0xffu << (lane & 24);
-  const int64_t nbins = bg.nbins;
-  int stage = 0;
-  int64_t b = blockIdx.x;
-  // after placement hist[b] is the end of bin b; bins with no query need no copy
-  auto bin_begin = [&](int64_t bb) { return bb > 0 ? (int64_t)w.hist[bb - 1] : (int64_t)0; };
-  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb] - bin_begin(bb) : 0; };
-  if (count(b) > 0) load_bin_tile<F>(g, bg, b, tiles[0]);
-  cp_async_commit();
-  for (; b < nbins; b += gridDim.x) {
-    const int64_t bn = b + gridDim.x;
-    if (count(bn) > 0) load_bin_tile<F>(g, bg, bn, tiles[stage ^ 1]);
-    cp_async_commit();
-    const int64_t t0 = bin_begin(b), t1 = w.hist[b];
-    cp_async_wait1();
-    __syncthreads();
-    if (t1 > t0) {
-      const BinTile<F> &T = tiles[stage];
-      int64_t og[3];
-      bin_origin(b, bg, og);
-      if (F == 4) {
-        // 8 lanes per query: lane (p, h) owns x offset p of the rows in
-        // planes h and h + 2, so each 8-thread phase of a 128-bit shared load
-        // reads one query's two x-rows on complementary banks.  The next
-        // record is loaded while this one is evaluated.
-        const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
-        const int64_t tstep = blockDim.x >> 3;
-        int64_t t = t0 + (threadIdx.x >> 3);
-        QRec<float> rnext;
-        if (t < t1) rnext = recs[t];
-        for (; t < t1; t += tstep) {
-          const QRec<float> r = rnext;
-          if (t + tstep < t1) rnext = recs[t + tstep];
-          const int64_t i = r.row;
-          int64_t c[3];
-          unpack_cell<3>(r.cell, c);
-          const int cx = (int)(c[0] - og[0]), cy = (int)(c[1] - og[1]), cz = (int)(c[2] - og[2]);
-          const int lph = cz * HI_PLANE + cy * TILE_EDGE + cx;     // block corner in hi
-          const int lpl = (cz * TILE_EDGE + cy) * TILE_EDGE + cx;  // block corner in lo
-          const float fx = r.f[0], fy = r.f[1], fz = r.f[2];
-          float wx[4], dx[4], wy[4], dy[4], wz[4], dz[4];
-          cr_weights<float>(fx, wx);
-          cr_dweights<float>(fx, dx);
-          cr_weights<float>(fy, wy);
-          cr_dweights<float>(fy, dy);
-          cr_weights<float>(fz, wz);
-          cr_dweights<float>(fz, dz);
-          const float nref = reinterpret_cast<const BinTile<4> &>(T).hi[lph + HI_PLANE + TILE_EDGE + 1].w;
-          const float rlo = reinterpret_cast<const BinTile<4> &>(T).lo[lpl + TILE_EDGE * TILE_EDGE + TILE_EDGE + 1];
-          // this lane's weights, selected in registers
-          const float wzk[2] = {h ? wz[1] : wz[0], h ? wz[3] : wz[2]};
-          const float dzk[2] = {h ? dz[1] : dz[0], h ? dz[3] : dz[2]};
-          const float wxp = (p & 2) ? ((p & 1) ? wx[3] : wx[2]) : ((p & 1) ? wx[1] : wx[0]);
-          const float dxp = (p & 2) ? ((p & 1) ? dx[3] : dx[2]) : ((p & 1) ? dx[1] : dx[0]);
-          // Components (values only) accumulate raw float32 values; |B|
-          // accumulates deltas to the corner so its derivatives keep full
-          // relative precision.  y first, then z: d/dz reuses the layer sums.
-          float2 Sxy = make_float2(0.f, 0.f), Szn = make_float2(0.f, 0.f);
-          float Gy = 0.f, Gz = 0.f;
-#pragma unroll
-          for (int kk = 0; kk < 2; ++kk) {
-            const int k = 2 * kk + h;
-            float2 axy = make_float2(0.f, 0.f), azn = make_float2(0.f, 0.f);
-            float gy = 0.f;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              const float4 v = reinterpret_cast<const BinTile<4> &>(T).hi[lph + k * HI_PLANE + j * TILE_EDGE + p];
-              const float lo = reinterpret_cast<const BinTile<4> &>(T).lo[lpl + (k * TILE_EDGE + j) * TILE_EDGE + p];
-              const float dn = (v.w - nref) + (lo - rlo);
-              const float2 wj = make_float2(wy[j], wy[j]);
-              axy = ffma2(wj, make_float2(v.x, v.y), axy);
-              azn = ffma2(wj, make_float2(v.z, dn), azn);
-              gy += dy[j] * dn;
-            }
-            const float2 wk = make_float2(wzk[kk], wzk[kk]);
-            Sxy = ffma2(wk, axy, Sxy);
-            Szn = ffma2(wk, azn, Szn);
-            Gy += wzk[kk] * gy;
-            Gz += dzk[kk] * azn.y;
-          }
-          // Reduce-scatter over the 8 lanes of the group (butterfly on lane
-          // bits 2, 1, 0): lane g8 ends with the sum of output column g8 of
-          // (Vx, Vy, Vz, Vn, Gx, Gy, Gz, 0).
-          float u[4];
-          {
-            const float v8[8] = {wxp * Sxy.x, wxp * Sxy.y, wxp * Szn.x, wxp * Szn.y,
-                                 dxp * Szn.y, wxp * Gy, wxp * Gz, 0.f};
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-              const float send = h ? v8[m] : v8[m + 4];
-              u[m] = (h ? v8[m + 4] : v8[m]) + __shfl_xor_sync(mask, send, 4);
-            }
-          }
-          const bool b1 = (p & 2) != 0, b0 = (p & 1) != 0;
-          float u2[2];
-#pragma unroll
-          for (int m = 0; m < 2; ++m) {
-            const float send = b1 ? u[m] : u[m + 2];
-            u2[m] = (b1 ? u[m + 2] : u[m]) + __shfl_xor_sync(mask, send, 2);
-          }
-          const float val = (b0 ? u2[1] : u2[0]) + __shfl_xor_sync(mask, b0 ? u2[0] : u2[1], 1);
-          // column g8 as the caller's float64
-          const float ih = g8 == 4 ? kp.inv_hf[0] : (g8 == 5 ? kp.inv_hf[1] : kp.inv_hf[2]);
-          const float x = g8 == 3 ? nref + (rlo + val) : (g8 >= 4 ? val * ih : val);
-          const double out = g8 == 7 ? 0.0 : f2d_exact(x);
-          if (interleaved_rows<3, 4>(o)) {
-            o.comps[i * 8 + g8] = out;      // a group writes its 64-byte row
-          } else if (g8 < 3) {
-            if (o.comps) o.comps[i * o.comps_stride + g8] = out;
-          } else if (g8 == 3) {
-            if (o.norms) o.norms[i * o.norms_stride] = out;
-          } else if (g8 < 7) {
-            if (o.grads) o.grads[i * o.grads_stride + (g8 - 4)] = out;
-          }
-        }
-      }
-    }
-    __syncthreads();  // this stage is refilled two bins later
-    stage ^= 1;
-  }
-  // records that need no evaluation (out of volume, NaN, sentinel column)
-  for (int64_t t = bin_begin(nbins) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const QRec<float> r = reinterpret_cast<const QRec<float> *>(w.rec)[t];
-    write_const<3, F>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
-  }
-}
-
-static int sm_count_sorted() { return device_sms(); }
-
-// Launches the bin-staged kernel when it applies (3D, mixed, 'both' fields,
-// 8^3-cell bins); returns false otherwise.
-static bool launch_eval_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
-                            const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
-  if (g->dim != 3 || g->nfield != 4 || bg.shift != 3) return false;
-  const size_t smem = 2 * sizeof(BinTile<4>);
-  static bool attr[MAX_DEVICES] = {};
-  const int dev = current_device();
-  if (dev < 0) return false;
-  if (!attr[dev]) {
-    if (cudaFuncSetAttribute(eval_bin_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      return false;
-    attr[dev] = true;
-  }
-  int64_t grid = (int64_t)sm_count_sorted() * 4;  // 4 resident per SM (64 registers)
-  if (grid > bg.nbins) grid = bg.nbins;
-  if (grid < 1) grid = 1;
-  eval_bin_kernel<4><<<(unsigned)grid, 256, smem, s>>>(*g, kp, bg, nq, *out, w);
-  return true;
-}
-
-// ---- bin-staged evaluation (3D, mixed, scalar / norm or vector fields) -------
-// rQuery2 (ARBInterp.py:399-455, scalar and norm fields: one (hi, lo) field)
-// and rQuery1 (ARBInterp.py:344-397, vector fields: three components, values
-// only) on the fly: the bin's 11^3 points staged in shared memory as in
-// eval_bin, one query per thread evaluating eval_otf3_mixed_block /
-// eval_otf3_vec_block on the staged block (the code the global-memory kernel
-// runs, so the same bits).
-constexpr int BINF_THREADS = 128;
-
-template <int F>
-struct TileBlock3 {  // a 4x4x4 block inside a staged tile
-  // F = 1: (hi, lo) pairs, read by hl and load; F = 3: float4 components,
-  // read by hi4 (the accessors of the other layout are never instantiated)
-  const typename std::conditional<F == 1, float2, float4>::type *v;
+struct TileBlock3;  // a 4x4x4 block inside a staged tile
+template <>
+struct TileBlock3<4> {
+  const float4 *h4;
+  const float2 *l2;
   int base;  // tile index of the block corner
   __device__ __forceinline__ int at(int i, int j, int k) const {
     return base + (k * TILE_EDGE + j) * TILE_EDGE + i;
   }
+  __device__ __forceinline__ float4 hi4(int p) const { return h4[p]; }
+  __device__ __forceinline__ float lo(int p) const { return l2[p].x; }
+  __device__ __forceinline__ void lo_row(int p, float l[4]) const {
+    const float2 a = l2[p], b = l2[p + 2];
+    l[0] = a.x;
+    l[1] = a.y;
+    l[2] = b.x;
+    l[3] = b.y;
+  }
+};
+template <>
+struct TileBlock3<1> {
+  const float2 *v;
+  int base;
+  __device__ __forceinline__ int at(int i, int j, int k) const {
+    return base + (k * TILE_EDGE + j) * TILE_EDGE + i;
+  }
   __device__ __forceinline__ float2 hl(int p) const { return v[p]; }
-  __device__ __forceinline__ float4 hi4(int p) const { return v[p]; }
   template <int FF>
   __device__ __forceinline__ void load(int p, int, float &hi, float &lo) const {
     const float2 x = v[p];
@@ -620,70 +444,158 @@ struct TileBlock3 {  // a 4x4x4 block inside a staged tile
     lo = x.y;
   }
 };
+template <>
+struct TileBlock3<3> {
+  const float4 *v;
+  int base;
+  __device__ __forceinline__ int at(int i, int j, int k) const {
+    return base + (k * TILE_EDGE + j) * TILE_EDGE + i;
+  }
+  __device__ __forceinline__ float4 hi4(int p) const { return v[p]; }
+};
+
+// Round-robin order of one bin's queries over its 8 bank classes.  Level r
+// holds the r-th query of every class that has more than r; levels come one
+// after another, classes in increasing order within a level.  With the class
+// counts sorted, m_0 <= ... <= m_7, segment s covers levels [m_(s-1), m_s)
+// and holds 8 - s classes per level.
+struct BinSched {
+  uint32_t start[8];    // first record of each class
+  uint32_t slot[9];     // first slot of each segment; slot[8] = queries in the bin
+  uint32_t lvl[8];      // first level of each segment
+  uint8_t cls[8][8];    // classes of segment s, increasing
+  uint32_t sorted[8];   // class counts in increasing order (set-up scratch)
+};
+
+// Warp 0 fills the schedule of bin b from the sub-bin ends in hist.
+__device__ __forceinline__ void bin_sched(const uint32_t *hist, int64_t b, BinSched &sc) {
+  const int l = threadIdx.x;  // called by warp 0 only
+  const int64_t sb = (b << 3) + (l & 7);
+  uint32_t st = 0, cnt = 0;
+  if (l < 8) {
+    st = sb > 0 ? hist[sb - 1] : 0u;
+    cnt = hist[sb] - st;
+  }
+  int rank = 0;
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const uint32_t cm = __shfl_sync(0xffffffffu, cnt, m);
+    rank += (cm < cnt || (cm == cnt && m < l)) ? 1 : 0;
+  }
+  if (l < 8) {
+    sc.start[l] = st;
+    sc.sorted[rank] = cnt;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int sg = 0; sg < 8; ++sg) {
+    const unsigned act = __ballot_sync(0xffffffffu, l < 8 && rank >= sg);
+    if (l < 8 && rank >= sg) sc.cls[sg][__popc(act & ((1u << l) - 1u))] = (uint8_t)l;
+  }
+  if (l == 0) {
+    uint32_t prev = 0, slot = 0;
+#pragma unroll
+    for (int sg = 0; sg < 8; ++sg) {
+      const uint32_t m = sc.sorted[sg];
+      sc.slot[sg] = slot;
+      sc.lvl[sg] = prev;
+      slot += (m - prev) * (uint32_t)(8 - sg);
+      prev = m;
+    }
+    sc.slot[8] = slot;
+  }
+}
+
+// Record index (absolute) of slot t of the bin.
+__device__ __forceinline__ int64_t sched_record(const BinSched &sc, uint32_t t) {
+  int sg = 0;
+#pragma unroll
+  for (int q = 1; q < 8; ++q) sg += t >= sc.slot[q] ? 1 : 0;
+  const uint32_t off = t - sc.slot[sg];
+  const uint32_t k = 8u - (uint32_t)sg;
+  const uint32_t lv = off / k;
+  const int c = sc.cls[sg][off - lv * k];
+  return (int64_t)sc.start[c] + sc.lvl[sg] + lv;
+}
 
 template <int F>
-__global__ void __launch_bounds__(BINF_THREADS) eval_binf_kernel(arb_grid g, KParams kp, BinGeom bg, int64_t nq,
-                                                                 arb_query_out o, SortedWork w) {
-  extern __shared__ __align__(16) unsigned char binf_smem[];
-  BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(binf_smem);
+__global__ void __launch_bounds__(BINC_THREADS, 3) eval_binc_kernel(arb_grid g, KParams kp, BinGeom bg,
+                                                                   int64_t nq, arb_query_out o, SortedWork w) {
+  extern __shared__ __align__(16) unsigned char binc_smem[];
+  BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(binc_smem);
+  __shared__ BinSched sc;
   const int64_t nbins = bg.nbins;
   const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
+  // after placement hist[sb] is the end of sub-bin sb; bin b is sub-bins 8b .. 8b + 7
+  auto sub_begin = [&](int64_t sb) { return sb > 0 ? (int64_t)w.hist[sb - 1] : (int64_t)0; };
+  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[(bb << 3) + 7] - sub_begin(bb << 3) : 0; };
   int stage = 0;
   int64_t b = blockIdx.x;
-  // after placement hist[b] is the end of bin b; bins with no query need no copy
-  auto bin_begin = [&](int64_t bb) { return bb > 0 ? (int64_t)w.hist[bb - 1] : (int64_t)0; };
-  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb] - bin_begin(bb) : 0; };
   if (count(b) > 0) load_bin_tile<F>(g, bg, b, tiles[0]);
   cp_async_commit();
   for (; b < nbins; b += gridDim.x) {
     const int64_t bn = b + gridDim.x;
     if (count(bn) > 0) load_bin_tile<F>(g, bg, bn, tiles[stage ^ 1]);
     cp_async_commit();
-    const int64_t t0 = bin_begin(b), t1 = w.hist[b];
+    const int64_t nb = count(b);
+    if (nb > 0 && threadIdx.x < 32) bin_sched(w.hist, b, sc);
     cp_async_wait1();
     __syncthreads();
-    if (t1 > t0) {
+    if (nb > 0) {
       int64_t og[3];
       bin_origin(b, bg, og);
-      for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-        const QRec<float> r = recs[t];
+      for (int64_t t = threadIdx.x; t < nb; t += blockDim.x) {
+        const QRec<float> r = recs[sched_record(sc, (uint32_t)t)];
         int64_t c[3];
         unpack_cell<3>(r.cell, c);
-        TileBlock3<F> blk;
-        blk.v = tiles[stage].v;
-        blk.base = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));
+        const int base = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));
         const float fr[3] = {r.f[0], r.f[1], r.f[2]};
         double val[F], grad[3] = {0.0, 0.0, 0.0};
-        if constexpr (F == 1)
-          eval_otf3_mixed_block<1>(blk, kp, fr, val, grad);
-        else
+        TileBlock3<F> blk;
+        if constexpr (F == 4) {
+          blk.h4 = tiles[stage].hi;
+          blk.l2 = tiles[stage].lo2;
+        } else {
+          blk.v = tiles[stage].v;
+        }
+        blk.base = base;
+        if constexpr (F == 3)
           eval_otf3_vec_block(blk, fr, val);
+        else if constexpr (F == 4)
+          eval_otf3_both_block(blk, kp, fr, val, grad);
+        else
+          eval_otf3_mixed_block<F>(blk, kp, fr, val, grad);
         write_vals<3, F>(o, r.row, val, grad);
       }
     }
-    __syncthreads();  // this stage is refilled two bins later
+    __syncthreads();  // this stage is refilled two bins later; the schedule is rebuilt
     stage ^= 1;
   }
   // records that need no evaluation (out of volume, NaN, sentinel column)
-  for (int64_t t = bin_begin(nbins) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
+  for (int64_t t = sub_begin(bg.nsub) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
        t += (int64_t)gridDim.x * blockDim.x) {
     const QRec<float> r = recs[t];
     write_const<3, F>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
   }
 }
 
-// Launches the 3D one-field / vector bin-staged kernel when it applies (3D,
-// mixed, F = 1 or 3, 8^3-cell bins); returns false otherwise.
+static int sm_count_sorted() { return device_sms(); }
+
+// Launches the bank-ordered bin kernel when it applies (3D, mixed, 8^3-cell
+// bins with bank classes); returns false otherwise.
 template <int F>
-static bool launch_eval_binf(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
-                             const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
+static bool launch_eval_binc_f(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
+                               const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
   const size_t smem = 2 * sizeof(BinTile<F>);
   static int per_sm[MAX_DEVICES] = {};
   const int dev = current_device();
   if (dev < 0) return false;
   if (!per_sm[dev]) {
+    if (cudaFuncSetAttribute(eval_binc_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return false;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, eval_binf_kernel<F>, BINF_THREADS, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, eval_binc_kernel<F>, BINC_THREADS, smem) !=
             cudaSuccess ||
         n < 1)
       return false;
@@ -692,15 +604,16 @@ static bool launch_eval_binf(const arb_grid *g, const KParams &kp, const BinGeom
   int64_t grid = (int64_t)sm_count_sorted() * per_sm[dev];
   if (grid > bg.nbins) grid = bg.nbins;
   if (grid < 1) grid = 1;
-  eval_binf_kernel<F><<<(unsigned)grid, BINF_THREADS, smem, s>>>(*g, kp, bg, nq, *out, w);
+  eval_binc_kernel<F><<<(unsigned)grid, BINC_THREADS, smem, s>>>(*g, kp, bg, nq, *out, w);
   return true;
 }
 
-static bool launch_eval_bin1(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
+static bool launch_eval_binc(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
                              const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
-  if (g->dim != 3 || bg.shift != 3) return false;
-  if (g->nfield == 1) return launch_eval_binf<1>(g, kp, bg, nq, out, w, s);
-  if (g->nfield == 3) return launch_eval_binf<3>(g, kp, bg, nq, out, w, s);
+  if (g->dim != 3 || bg.shift != 3 || bg.cls != 3) return false;
+  if (g->nfield == 1) return launch_eval_binc_f<1>(g, kp, bg, nq, out, w, s);
+  if (g->nfield == 3) return launch_eval_binc_f<3>(g, kp, bg, nq, out, w, s);
+  if (g->nfield == 4) return launch_eval_binc_f<4>(g, kp, bg, nq, out, w, s);
   return false;
 }
 
@@ -845,7 +758,9 @@ static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, 
   const int TB = 256;
   const unsigned B = (unsigned)((nq + TB - 1) / TB);
   bin_count_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, wb, *out, status, w);
-  scan_kernel<<<1, 1024, 0, s>>>(w.hist, bg.nbins + 1);
+  const int64_t nh = bg.nsub + 1, nb = scan_blocks(nh);
+  scan_part_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(w.hist, nh, w.part);
+  scan_apply_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(w.hist, nh, w.part);
   bin_place_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, w);
 }
 
@@ -957,9 +872,9 @@ __global__ void __launch_bounds__(256) eval_tab_coop_kernel(arb_grid g, KParams 
 template <int DIM, bool MIXED>
 static void launch_eval(const arb_grid *g, const KParams &kp, int64_t nq, const arb_query_out *out,
                         const SortedWork &w, bool table, cudaStream_t s) {
-  if (DIM == 3 && MIXED && !table && launch_eval_bin(g, kp, bin_geom(g), nq, out, w, s)) return;
-  if (DIM == 3 && MIXED && !table && launch_eval_bin1(g, kp, bin_geom(g), nq, out, w, s)) return;
-  if (DIM == 4 && MIXED && !table && launch_eval_bin4(g, kp, bin_geom(g), nq, out, w, s)) return;
+  const BinGeom bg = bin_geom(g, MIXED ? ARB_PREC_MIXED : ARB_PREC_FP64);
+  if (DIM == 3 && MIXED && !table && launch_eval_binc(g, kp, bg, nq, out, w, s)) return;
+  if (DIM == 4 && MIXED && !table && launch_eval_bin4(g, kp, bg, nq, out, w, s)) return;
   const int TE = DIM == 3 ? 256 : 128;
   const unsigned BE = (unsigned)((nq + TE - 1) / TE);
 #define ES(FF, TAB) eval_sorted_kernel<DIM, FF, MIXED, TAB><<<BE, TE, 0, s>>>(*g, kp, nq, *out, w)
@@ -968,9 +883,6 @@ static void launch_eval(const arb_grid *g, const KParams &kp, int64_t nq, const 
 #define ET(FF) eval_tab_coop_kernel<DIM, FF, MIXED><<<BT, 256, 0, s>>>(*g, kp, nq, *out, w)
     switch (g->nfield) { case 1: ET(1); break; case 3: ET(3); break; default: ET(4); break; }
 #undef ET
-  } else if (DIM == 3 && MIXED && g->nfield == 4) {
-    const unsigned BC = (unsigned)((nq + COOP_CHUNK - 1) / COOP_CHUNK);
-    eval_sorted_coop4_kernel<<<BC, 256, 0, s>>>(*g, kp, nq, *out, w);
   } else {
     switch (g->nfield) { case 1: ES(1, false); break; case 3: ES(3, false); break; default: ES(4, false); break; }
   }
@@ -1063,11 +975,11 @@ extern "C" int arb_query_eval_sorted(const arb_grid *g, int32_t precision, int32
   }
   SortedWork w;
   if (carve(&w, work, g, precision, nq) > work_bytes) return ARB_ERR_INVALID;
-  const BinGeom bg = bin_geom(g);
+  const BinGeom bg = bin_geom(g, precision);
   cudaStream_t s = (cudaStream_t)stream;
   const arb_query_out out_norm = normalize_out(*out, g->dim);
   out = &out_norm;
-  if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nbins + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
+  if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nsub + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
   const KParams kp = make_kparams(g);
   if (g->dim == 3) {
     if (mixed) {
@@ -1105,11 +1017,11 @@ extern "C" int arb_query_bin(const arb_grid *g, int32_t precision, double *q, in
     if (g->n[a] - 3 >= ((int64_t)1 << bits)) return ARB_ERR_UNSUPPORTED;
   SortedWork w;
   if (carve(&w, work, g, precision, nq) > work_bytes) return ARB_ERR_INVALID;
-  const BinGeom bg = bin_geom(g);
+  const BinGeom bg = bin_geom(g, precision);
   cudaStream_t s = (cudaStream_t)stream;
   const arb_query_out out_norm = normalize_out(*out, g->dim);
   out = &out_norm;
-  if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nbins + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
+  if (cudaMemsetAsync(w.hist, 0, sizeof(uint32_t) * (bg.nsub + 1), s) != cudaSuccess) return ARB_ERR_CUDA;
   const KParams kp = make_kparams(g);
   const bool mixed = precision == ARB_PREC_MIXED;
   if (g->dim == 3) {

@@ -18,9 +18,11 @@ Multi-GPU: replicas (every rank builds the full field and evaluates its own
 1.01e7 queries; no collective): scaling "weak", value = all ranks' queries /
 max-over-ranks time.
 
---impl reference times the CPU oracle port of the reference's algorithm
-(lazy per-cell A @ f solve + monomial evaluation, NumPy/BLAS on all host
-threads) on fresh 1e5-row samples of the same workload.
+--impl reference times the reference's own code (its module byte-compiled
+into oracle/_ref by oracle/ref_build.py; the oracle port where that is
+absent) on all host cores: worker processes split the 1.01e7-query job by
+cell range, each constructing from the whole field, and every step runs one
+cold part of the job (its own cells' lazy solves included) on every worker.
 """
 from __future__ import annotations
 
@@ -52,6 +54,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-configs", action="store_true", help="skip the c0/c2/c3/c4 keys of the default line")
+    p.add_argument("--grid", type=int, default=GRID[0], help=argparse.SUPPRESS)   # CPU tests of the reference arm
     p.add_argument("--kernel-only", action="store_true", help="time only the query kernel (profiling)")
     p.add_argument("--workload", default=None, choices=["c0", "c2", "c3", "c4", "traj", "csv"],
                    help="measure one of the other seeded configurations and print its own JSON line: "
@@ -176,15 +180,42 @@ def _normwise(a, b):
 
 
 def run_workload(args):
-    """Seeded stand-ins for the other configurations; one JSON line each.
-    Mixed precision is compared with the float64 GPU path (itself pinned to
-    the reference by the parity tests)."""
+    """One JSON line for one of the other seeded configurations."""
+    print(json.dumps(workload_line(args.workload, args.steps, args.warmup)), flush=True)
+
+
+def _vs_oracle(out, want, inds=None, want_inds=None):
+    """Normwise errors of (norms, grads[, comps]) device outputs against the
+    oracle's dict, plus bit-exact NaN masks and cell indices."""
+    import numpy as np
+    res = {}
+    for name, got in out.items():
+        g = got.cpu().numpy().reshape(len(got), -1)
+        w = np.asarray(want[name]).reshape(len(g), -1)
+        m = np.isfinite(w).all(1)
+        res[name] = [float(x) for x in np.abs(g[m] - w[m]).max(0) / np.maximum(np.abs(w[m]).max(0), 1e-300)]
+        res[name + "_nan_mask_equal"] = bool(np.array_equal(np.isnan(g), np.isnan(w)))
+    if inds is not None:
+        res["indices_bitexact"] = bool(np.array_equal(inds.cpu().numpy(), want_inds))
+    return res
+
+
+def workload_line(name, steps, warmup):
+    """Seeded stand-ins for the other configurations.  Mixed precision is
+    compared with the float64 GPU path, and both with the CPU oracle on the
+    whole query set (c0) or a bounded sample of it (c2: 1e5 rows; c3: 16 of
+    the fields; c4: 1e5 rows, forward values and the adjoint)."""
     import numpy as np
     import torch
     from arbinterp_gb300 import tricubic, quadcubic, synth, _lib
     _lib.lib()
     dev = torch.device("cuda")
     gpu_index = torch.cuda.current_device()
+
+    class _A:
+        pass
+    args = _A()
+    args.workload, args.steps, args.warmup = name, steps, warmup
     line = {"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
             "scaling": "weak", "vs_baseline": None, "higher_is_better": True, "workload": args.workload}
     if args.workload in ("c0", "c2"):
@@ -217,10 +248,22 @@ def run_workload(args):
             got = r.pop("_out")
             r["max_rel_err_vs_fp64"] = {"norms": _normwise(got[0], ref[0]), "grads": _normwise(got[1], ref[1])}
         head = res[("mixed", "otf" if args.workload == "c2" else "auto")]
+        # against the CPU oracle (c0: every query; c2: the first 1e5 rows)
+        from oracle.arb_oracle import OracleQuadcubic, OracleTricubic
+        ns = nq if args.workload == "c0" else 100_000
+        qs_ = q[:ns]
+        orc = (OracleTricubic if args.workload == "c0" else OracleQuadcubic)(field.cpu().numpy())
+        want = orc.query(qs_.cpu().numpy().copy())
+        vs_or = {}
+        for (p_, s_) in res:
+            ob = cls(field, "quiet", precision=p_, strategy=s_)
+            nrm, grd = ob.Query(qs_.clone())
+            vs_or[f"{p_}/{s_}"] = _vs_oracle({"norms": nrm, "grads": grd}, want, ob._last_inds, want["inds"])
         line.update({"metric": f"{args.workload}: queries/s, construct + query", "value": head["value"],
                      "unit": "queries/s", "ms_per_step": head["ms_per_step"], "dtype": "f32",
                      "config": {"workload": desc, "precision": "mixed"},
-                     "paths": {f"{p}/{s}": v for (p, s), v in res.items()}})
+                     "paths": {f"{p}/{s}": v for (p, s), v in res.items()},
+                     "vs_oracle": {"rows": ns, **vs_or}})
     elif args.workload == "c3":
         from arbinterp_gb300.batched import BatchedTricubic
         fields, qs, counts = [], [], []
@@ -252,8 +295,21 @@ def run_workload(args):
             sl = slice(int(off[k]), int(off[k + 1]))
             e = [max(_normwise(a[sl], r[sl])) for a, r in zip(out["mixed"]["_o"], out["fp64"]["_o"])]
             per_field.append(max(e))
+        # against the CPU oracle: every 32nd field, at most 2e4 of its rows
+        from oracle.arb_oracle import OracleTricubic
+        vs_or = {"fields": 0, "rows": 0, "fp64_max": 0.0, "mixed_max": 0.0, "nan_masks_equal": True}
+        for k in range(0, len(fields), 32):
+            sl = slice(int(off[k]), int(min(off[k + 1], off[k] + 20_000)))
+            want = OracleTricubic(fields[k].cpu().numpy()).query(q[sl].cpu().numpy().copy())
+            for prec in ("fp64", "mixed"):
+                e = _vs_oracle({"norms": out[prec]["_o"][0][sl], "grads": out[prec]["_o"][1][sl]}, want)
+                vs_or[prec + "_max"] = max(vs_or[prec + "_max"], max(e["norms"] + e["grads"]))
+                vs_or["nan_masks_equal"] &= e["norms_nan_mask_equal"] and e["grads_nan_mask_equal"]
+            vs_or["fields"] += 1
+            vs_or["rows"] += sl.stop - sl.start
         for v in out.values():
             v.pop("_o")
+        line["vs_oracle"] = vs_or
         line.update({"metric": "c3: batched queries/s (one persistent launch, CUDA graph replay)",
                      "value": out["mixed"]["value"], "unit": "queries/s",
                      "ms_per_step": out["mixed"]["ms_per_step"], "dtype": "f32",
@@ -360,6 +416,24 @@ def run_workload(args):
         m = torch.isfinite(gq_d).all(1)
         for v in res.values():
             v.pop("_g")
+        # against the CPU oracle on the first 1e5 rows: forward values, and the
+        # adjoint (value gradient of that subset's loss) against the oracle's
+        from oracle.arb_oracle import OracleTricubic
+        ns = 100_000
+        qs_, ks_ = q[:ns], keep[:ns]
+        orc = OracleTricubic(rows.cpu().numpy())
+        want = orc.query(qs_.cpu().numpy().copy())
+        v = v64.clone().requires_grad_(True)
+        val, _ = f64(v, qs_)
+        dsub = torch.where(ks_, val - target[:ns], torch.zeros_like(val))
+        (dsub * dsub).sum().backward()
+        dval = (2 * dsub).detach().cpu().numpy()
+        g_or = orc.adjoint(qs_.cpu().numpy(), dval)
+        g_gpu = v.grad.detach().cpu().numpy()
+        line["vs_oracle"] = {
+            "rows": ns,
+            "fp64_values": _vs_oracle({"norms": val.detach().view(-1, 1)}, want)["norms"][0],
+            "adjoint_fp64_max_rel_err": float(np.abs(g_gpu - g_or).max() / np.abs(g_or).max())}
         line.update({"metric": "c4: forward + backward queries/s (loss = sum of squared residuals)",
                      "value": res["mixed"]["value"], "unit": "queries/s",
                      "ms_per_step": res["mixed"]["ms_per_step"], "dtype": "f32",
@@ -374,7 +448,7 @@ def run_workload(args):
                      "mixed_vs_fp64_grad": {
                          "values": float((gv_m - gv_d).abs().max() / gv_d.abs().max()),
                          "queries": float((gq_m[m] - gq_d[m]).abs().max() / gq_d[m].abs().max())}})
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ---------------------------------------------------------------- clocks
@@ -528,15 +602,20 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------- workload
-def make_workload(device, rank=0):
+def make_workload(device, rank=0, n=GRID[0]):
+    """The 256^3 dipole field and its 1.01e7 queries.  n: the grid edge (other
+    values only in the CPU tests of the reference arm, with the query count
+    scaled by the cell count, so the queries per cell stay the job's)."""
     import torch
     from arbinterp_gb300 import synth
-    field = synth.dipole_field3(n=GRID, seed=1, device=device)
-    h = 2.0 / (GRID[0] - 1)
-    ax = -1.0 + h * torch.arange(GRID[0], dtype=torch.float64)
+    field = synth.dipole_field3(n=(n, n, n), seed=1, device=device)
+    h = 2.0 / (n - 1)
+    ax = -1.0 + h * torch.arange(n, dtype=torch.float64)
     lo = [float(ax[1])] * 3
-    hi = [float(ax[GRID[0] - 2])] * 3
-    q = synth.uniform_queries(lo, hi, N_IN, N_OUT, [h] * 3, seed=10 + rank, device=device)
+    hi = [float(ax[n - 2])] * 3
+    scale = ((n - 3) / (GRID[0] - 3)) ** 3
+    q = synth.uniform_queries(lo, hi, int(N_IN * scale), int(N_OUT * scale), [h] * 3, seed=10 + rank,
+                              device=device)
     return field, q, lo, hi, [h] * 3
 
 
@@ -559,97 +638,206 @@ def cuda_time(fn, steps, warmup, barrier=None):
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_baseline(field_np, q_np, lo, hi, h, budget_s=25.0, sample=100_000):
-    """Time the oracle port on the host: construct once, then fresh cold
-    samples (lazy solve of each sample's cells + evaluation).  The whole-job
-    time is estimated as construct + N * eval/query + D * solve/cell with D
-    the expected number of distinct cells 1.01e7 uniform queries touch."""
+# The reference's own code (oracle/_ref: its module byte-compiled by
+# oracle/ref_build.py; the oracle port where that file is absent) runs the
+# job on the host cores as N worker processes that split the query set, the
+# way SURVEY's CPU plan describes: every worker constructs its own
+# interpolant from the whole 256^3 field (the reference's getFieldParams,
+# unchanged), then evaluates, with `Query`, the queries of its share of the
+# cells.  Shares are contiguous ranges of the flat cell index (z-slabs), so a
+# worker's lazily solved coefficient columns are its own and its memory stays
+# near 1/N of the reference's 33 GB of coefficient arrays.  Each share is cut
+# into P parts, again by cell range, so every part is cold (its cells are
+# solved by its own queries) and has the query density of the whole job; a
+# step runs one part on every worker at once.  Out-of-volume rows are dealt
+# out round robin.
+
+def _ref_cells(q, lo, hi, h, npos, nc):
+    """Flat cell index of each row as the reference computes it (rQuery3,
+    ARBInterp.py:463-485: rows outside [IntMin, IntMax] are NaN, then float64
+    (q - IntMin) / h, floor, NaN -> nc)."""
     import numpy as np
-    from oracle.arb_oracle import OracleTricubic
+    idx = np.zeros(len(q))
+    bad = np.zeros(len(q), bool)
+    stride = 1.0
+    for a in range(3):
+        bad |= (q[:, a] < lo[a]) | (q[:, a] > hi[a])
+        idx += np.floor((q[:, a] - lo[a]) / h[a]) * stride
+        stride *= npos[a]
+    idx[bad | np.isnan(idx)] = nc
+    return np.minimum(idx, nc).astype(np.int64)
+
+
+REF_CHUNK = 100_000
+
+
+def _ref_worker(conn, field_path, parts, kind):
+    """One worker of the CPU baseline (spawned; see the block comment)."""
+    import contextlib
+    import io
+    import numpy as np
+    field = np.load(field_path, mmap_mode="r")
     t0 = time.perf_counter()
-    o = OracleTricubic(field_np, mode="both")
-    t_con = time.perf_counter() - t0
-    rng = np.random.default_rng(0)
-    ev, sv, nq, ncell = 0.0, 0.0, 0, 0
-    t_start = time.perf_counter()
-    while time.perf_counter() - t_start < budget_s or nq == 0:
-        idx = rng.integers(0, len(q_np), sample)
-        qs = q_np[idx].copy()
-        bad = np.zeros(len(qs), bool)
-        for a in range(3):
-            bad |= (qs[:, a] < lo[a]) | (qs[:, a] > hi[a])
-        qq = qs[~bad]
-        fl = [np.floor((qq[:, a] - o.lo[a]) / o.h[a]) for a in range(3)]
-        cells = np.unique((fl[0] + fl[1] * o.ncell[0] + fl[2] * o.ncell[0] * o.ncell[1]).astype(np.int64))
-        cells = cells[(cells < o.nc) & ~o.solved[cells]]
-        t1 = time.perf_counter()
-        o._solve(cells)
-        t2 = time.perf_counter()
-        o.query(qs)
-        t3 = time.perf_counter()
-        sv += t2 - t1
-        ev += t3 - t2
-        nq += len(qs)
-        ncell += len(cells)
-    n_total = N_IN + N_OUT
-    D = o.nc * (1.0 - math.exp(-N_IN / o.nc))
-    t_est = t_con + n_total * ev / nq + D * sv / max(ncell, 1)
-    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    if kind == "reference":
+        from oracle import ref_build
+        R = ref_build.load()
+        with contextlib.redirect_stdout(io.StringIO()):
+            o = R.tricubic(field, "quiet", mode="both")
+        run = o.Query
+    else:
+        from oracle.arb_oracle import OracleTricubic
+        o = OracleTricubic(np.asarray(field), mode="both")
+        run = o.query
+    conn.send(time.perf_counter() - t0)
+    while True:
+        k = conn.recv()
+        if k is None:
+            break
+        t0 = time.perf_counter()
+        qk = parts[k]
+        for c0 in range(0, len(qk), REF_CHUNK):     # Query in 1e5-row chunks (result-identical)
+            run(qk[c0:c0 + REF_CHUNK].copy())
+        conn.send(time.perf_counter() - t0)
+    conn.close()
+
+
+def _mem_available_gb():
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) / 1e6
+    except OSError:
+        pass
+    return 64.0
+
+
+def reference_cpu(field_np, q_np, nparts, run_parts, warm_parts=0, n=GRID[0]):
+    """Run the CPU baseline: construct on every worker, then `warm_parts`
+    untimed and `run_parts` timed steps (one part per worker per step).
+    Returns a dict of the measurements."""
+    import multiprocessing as mp
+    import tempfile
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    from oracle import ref_build
+    kind = "reference" if ref_build.available() else "port"
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    # each worker holds the sorted field copy (805 MB), its share of the
+    # coefficient arrays and the evaluation temporaries: about 6 GB at most
+    nw = max(1, min(cores, 16, int(_mem_available_gb() // 6)))
+    ax = np.array(field_np[:n, 2])            # meshgrid('ij') rows: z fastest; the same axis on x and y
+    lo, hi, npos = [ax[1]] * 3, [ax[n - 2]] * 3, [n - 3] * 3
+    nc = (n - 3) ** 3
+    cell = _ref_cells(q_np, lo, hi, [abs(ax[0] - ax[1])] * 3, npos, nc)
+    share = np.minimum(cell * nw // nc, nw - 1)
+    part = np.minimum((cell * nw * nparts // nc) % nparts, nparts - 1)
+    oob = np.flatnonzero(cell >= nc)
+    share[oob] = oob % nw
+    part[oob] = (oob // nw) % nparts
+    parts = [[q_np[(share == w) & (part == k)] for k in range(nparts)] for w in range(nw)]
+    tmp = tempfile.mkdtemp(prefix="arb_ref_")
+    fpath = os.path.join(tmp, "field.npy")
+    np.save(fpath, field_np)
+    env_keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in env_keys}
+    for k in env_keys:
+        os.environ[k] = "1"
+    ctx = mp.get_context("spawn")
+    conns, procs = [], []
+    try:
+        for w in range(nw):
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_ref_worker, args=(b, fpath, parts[w], kind), daemon=True)
+            p.start()
+            conns.append(a)
+            procs.append(p)
+        t0 = time.perf_counter()
+        con = [c.recv() for c in conns]
+        t_con = time.perf_counter() - t0
+        steps = []
+        for k in range(warm_parts + run_parts):
+            t0 = time.perf_counter()
+            for c in conns:
+                c.send(k)
+            for c in conns:
+                c.recv()
+            steps.append(time.perf_counter() - t0)
+        for c in conns:
+            c.send(None)
+        for p in procs:
+            p.join(60)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+        for p in procs:
+            if p.is_alive():
+                p.kill()
+        try:
+            os.remove(fpath)
+            os.rmdir(tmp)
+        except OSError:
+            pass
+    nq_part = [sum(len(parts[w][k]) for w in range(nw)) for k in range(nparts)]
+    timed = range(warm_parts, warm_parts + run_parts)
+    return {"kind": kind, "workers": nw, "construct_s": t_con, "construct_worker_s": max(con),
+            "step_s": steps, "nq_part": nq_part,
+            "timed_queries": sum(nq_part[k] for k in timed), "timed_s": sum(steps[k] for k in timed),
+            "nparts": nparts}
+
+
+def cpu_baseline(field_np, q_np, nparts=25, run_parts=3):
+    """cpu_baseline of the default line: the reference on all host cores,
+    construct plus `run_parts` of the `nparts` parts of the job (a bounded
+    sample with the job's query density; every part cold)."""
+    r = reference_cpu(field_np, q_np, nparts, run_parts)
+    v = r["timed_queries"] / r["timed_s"]
+    who = ("the reference's own module (oracle/_ref, byte-compiled, unmodified)" if r["kind"] == "reference"
+           else "the oracle port (oracle/_ref absent)")
     return {
-        "value": n_total / t_est, "unit": "queries/s", "cores": threads, "kind": "port",
-        "sample": (f"oracle port (NumPy/BLAS, {threads} host threads): construct 256^3 once "
-                   f"({t_con:.1f} s) + {nq} cold sample queries solving {ncell} cells; "
-                   f"whole-job time estimated for 1.01e7 queries and {D:.3g} distinct cells"),
-        "construct_s": t_con, "solve_us_per_cell": 1e6 * sv / max(ncell, 1),
-        "eval_us_per_query": 1e6 * ev / nq,
+        "value": v, "unit": "queries/s", "cores": r["workers"], "kind": r["kind"],
+        "sample": (f"{who} in {r['workers']} processes splitting the 1.01e7-query job by cell range; each "
+                   f"constructs from the whole 256^3 field ({r['construct_worker_s']:.1f} s, not in the value), then "
+                   f"{run_parts} of the job's {nparts} parts ({r['timed_queries']} queries, cold: lazy "
+                   f"coefficient solves of their own cells) are timed"),
+        "construct_s": r["construct_worker_s"], "step_s": r["step_s"],
     }
 
 
 def run_reference(args):
-    """Reference arm: the CPU oracle port (the reference is pure Python and
-    does not travel to the GPU host); each step = one fresh 1e5-row sample
-    with the lazy coefficient solve of its cells."""
-    import numpy as np
-    import torch
+    """Reference arm: the reference's own code on all host cores (see the
+    CPU-baseline block comment).  The job's queries are cut into warmup +
+    steps parts per worker; step k evaluates part k on every worker (cold),
+    the last `steps` are timed."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from oracle.arb_oracle import OracleTricubic
-    field, q, lo, hi, h = make_workload("cpu")
+    field, q, lo, hi, h = make_workload("cpu", n=args.grid)
     field_np, q_np = field.numpy(), q.numpy()
-    t0 = time.perf_counter()
-    o = OracleTricubic(field_np, mode="both")
-    t_con = time.perf_counter() - t0
-    rng = np.random.default_rng(1)
-    S = 100_000
-
-    def step():
-        qs = q_np[rng.integers(0, len(q_np), S)].copy()
-        o.query(qs)
-
-    for _ in range(args.warmup):
-        step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step()
-    dt = time.perf_counter() - t0
-    threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    val = S * args.steps / dt
+    nparts = args.warmup + args.steps
+    r = reference_cpu(field_np, q_np, nparts, args.steps, warm_parts=args.warmup, n=args.grid)
+    val = r["timed_queries"] / r["timed_s"]
+    whole = r["construct_worker_s"] + sum(r["step_s"])
+    who = ("the reference's own module (oracle/_ref, byte-compiled, unmodified)" if r["kind"] == "reference"
+           else "the oracle port (oracle/_ref absent)")
     line = {
         "metric": METRIC, "value": val, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1000 * r["timed_s"] / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": "tricubic 256^3 dipole vector field, mode both; 1e5-row samples of the "
-                               "1.01e7-query set (1% outside the volume)",
-                   "construct_s": t_con},
-        "cpu_baseline": {"value": val, "unit": "queries/s", "cores": threads, "kind": "port",
-                         "sample": f"each step: {S} fresh rows, lazy A@f solve of their new cells + "
-                                   f"monomial evaluation (oracle port, NumPy/BLAS {threads} threads); "
-                                   f"construction ({t_con:.1f} s) outside the timed steps"},
+        "config": {"workload": f"tricubic {args.grid}^3 dipole vector field, mode both, {len(q_np)} queries "
+                               f"(1% outside the volume), cut into {nparts} parts of equal query density; one part "
+                               "per step",
+                   "construct_s": r["construct_worker_s"],
+                   "whole_job_s": whole, "whole_job_queries_per_s": len(q_np) / whole},
+        "cpu_baseline": {"value": val, "unit": "queries/s", "cores": r["workers"], "kind": r["kind"],
+                         "sample": f"{who} in {r['workers']} processes splitting the query set by cell range; "
+                                   f"each step = one cold part per process; construction "
+                                   f"({r['construct_worker_s']:.1f} s) before the steps"},
         "e2e": {"value": val, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
-    del torch
 
 
 # ---------------------------------------------------------------- our arm
@@ -728,7 +916,7 @@ def main():
     grid_bytes = o._npts * (20 if prec == "mixed" else 32)    # grid read once (compulsory)
     algo = nq * (rec + 7 * 8) + (nq * 4 * 64 * (4 if prec == "mixed" else 8) if use_tab else grid_bytes)
     kname = ("eval_sorted_kernel<3,4,table>" if use_tab else
-             ("eval_bin_kernel<4>" if prec == "mixed" else "eval_sorted_kernel<3,4,fp64>"))
+             ("eval_binc_kernel<4>" if prec == "mixed" else "eval_sorted_kernel<3,4,fp64>"))
     # DRAM traffic per launch, scaled from the small-case ncu capture of the
     # same kernel (profiles/eval_bin_kernel__tricubic160_both_mixed.md:
     # EVAL_SMALL_TRAFFIC bytes for 2.02e6 queries on a 160^3 grid whose mixed
@@ -758,6 +946,19 @@ def main():
         extra = {"fp64_path": {"value": v64, "unit": "queries/s", "ms_per_step": 1000 * t64 / max(2, args.steps // 3)},
                  "speedup_vs_fp64": value / v64,
                  "max_rel_err_vs_fp64": errs, "indices_bitexact": same_inds}
+        # both paths against the CPU oracle on the first 1e5 rows of the 256^3 job
+        # (bin-grouped: above the sort threshold)
+        if rank == 0:
+            from oracle.arb_oracle import OracleTricubic
+            ns = 100_000
+            want = OracleTricubic(field.cpu().numpy(), mode="both").query(q[:ns].cpu().numpy().copy())
+            for pname in ("fp64", "mixed"):
+                ob = tricubic(field, "quiet", mode="both", precision=pname, strategy="otf")
+                c_, n_, g_ = ob.Query(q[:ns].clone())
+                extra[pname + "_vs_oracle"] = _vs_oracle({"comps": c_, "norms": n_, "grads": g_}, want,
+                                                         ob._last_inds, want["inds"])
+                extra[pname + "_vs_oracle"]["rows"] = ns
+                del ob
 
     # warm query-only throughput (interpolant already constructed)
     tq = cuda_time(lambda: o.Query(q), 5, 2) / 5
@@ -833,16 +1034,25 @@ def main():
                "h2d_bytes_per_step": int(fnp.nbytes + qnp.nbytes), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": 1000 * te / ksteps}
 
+    # the other seeded configurations, measured in the same run (one GPU)
+    if rank == 0 and world == 1 and not args.no_configs:
+        skip = ("n_gpus", "steps", "warmup", "data", "scaling", "vs_baseline", "higher_is_better", "workload")
+        extra["configs"] = {}
+        for wname in ("c0", "c2", "c3", "c4"):
+            ln = workload_line(wname, args.steps, args.warmup)
+            extra["configs"][wname] = {k: v for k, v in ln.items() if k not in skip}
+            torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(field.cpu().numpy(), q.cpu().numpy(), lo, hi, h)
+        cpu = cpu_baseline(field.cpu().numpy(), q.cpu().numpy())
 
     if rank == 0:
         # this library's kernels per step: ingest (meshgrid-order rows: probe, gather, summary;
         # otherwise those three plus axes init/collect/sort, index, gather, summary) and the
-        # query (binned: count, scan, place, evaluate; plain: one)
+        # query (binned: count, two scan passes, place, evaluate; plain: one)
         launches_per_step = ((3 if o.ingest_path == "ordered" else 9) +
-                             (4 if o.last_plan.get("binned") else 1))
+                             (5 if o.last_plan.get("binned") else 1))
         line = {
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps, "higher_is_better": True,

@@ -68,7 +68,7 @@ def test_noalloc_capacity_stated_in_header():
     from arbinterp_gb300 import _lib
     src = open(os.path.join(ROOT, "include", "arbinterp.h")).read()
     cap = eval(re.search(r"#define ARB_NOALLOC_SCRATCH_BYTES \((\d+)u << (\d+)\)", src).expand(r"\1 << \2"))
-    m = re.search(r"at most ([\d,]+) query[\s*]+rows per call in float64 and[\s*]+([\d,]+) in mixed", src)
+    m = re.search(r"at most ([\d,]+)[\s*]+query[\s*]+rows per call in float64 and[\s*]+([\d,]+) in mixed", src)
     assert m, "row limits not found in the header"
     stated = [int(m.group(1).replace(",", "")), int(m.group(2).replace(",", ""))]
     L = _lib.lib()

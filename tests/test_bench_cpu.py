@@ -1,7 +1,8 @@
 """CPU checks of bench.py's contract with the driver: the reference arm (the
-oracle port timed on host cores) prints one JSON line with the keys the
-driver reads, on the same metric as the GPU arm, and a rank other than 0 of a
-multi-process launch exits 0 without work."""
+reference's own module, or the oracle port where that is not built, timed on
+host cores) prints one JSON line with the keys the driver reads, on the same
+metric as the GPU arm, and a rank other than 0 of a multi-process launch
+exits 0 without work."""
 import json
 import os
 import subprocess
@@ -12,7 +13,9 @@ ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 
 def _reference_arm(env_extra, timeout):
     env = dict(os.environ, **env_extra)
-    return subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
+    # a 64^3 grid with the job's queries per cell keeps this CPU test short
+    return subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0",
+                           "--grid", "64"],
                           cwd=ROOT, env=env, capture_output=True, text=True, timeout=timeout)
 
 

@@ -544,14 +544,14 @@ def test_quadcubic_bin_tiles_equal_global_gathers():
     assert torch.isnan(outs[0][1]).any() and not torch.isnan(outs[0][1]).all()
 
 
-@pytest.mark.parametrize("mode", [None, "norm", "vector"])
+@pytest.mark.parametrize("mode", [None, "norm", "vector", "both"])
 def test_tricubic_scalar_bin_tiles_equal_global_gathers(mode):
-    """3D mixed on the fly, one field (a scalar field, or |B| in norm mode)
-    or the three components (vector mode): the bin-staged kernel (8^3-cell
-    bins, blocks read from shared memory) returns the same bits as the kernel
-    gathering from global memory (4^3-cell bins), on a grid whose cell counts
-    are not multiples of 8, with queries outside the volume and in the last
-    cells."""
+    """3D mixed on the fly, one field (a scalar field, or |B| in norm mode),
+    the three components (vector mode) or both: the bin-staged kernel (8^3-cell
+    bins in bank-class order, blocks read from shared memory) returns the same
+    bits as the kernel gathering from global memory (4^3-cell bins), on a grid
+    whose cell counts are not multiples of 8, with queries outside the volume
+    and in the last cells."""
     import torch
     tricubic, _ = _mods()
     from arbinterp_gb300 import synth
