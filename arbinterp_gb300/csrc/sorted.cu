@@ -544,8 +544,12 @@ __global__ void __launch_bounds__(BINC_THREADS, 3) eval_binc_kernel(arb_grid g, 
     if (nb > 0) {
       int64_t og[3];
       bin_origin(b, bg, og);
+      // the next record is loaded while this one is evaluated
+      QRec<float> rnext;
+      if ((int64_t)threadIdx.x < nb) rnext = recs[sched_record(sc, threadIdx.x)];
       for (int64_t t = threadIdx.x; t < nb; t += blockDim.x) {
-        const QRec<float> r = recs[sched_record(sc, (uint32_t)t)];
+        const QRec<float> r = rnext;
+        if (t + blockDim.x < nb) rnext = recs[sched_record(sc, (uint32_t)(t + blockDim.x))];
         int64_t c[3];
         unpack_cell<3>(r.cell, c);
         const int base = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));

@@ -86,7 +86,7 @@ CSV_PARSE_TRAFFIC_PER_BYTE = (366.16e6 + 77.83e6) / 324.01e6
 
 
 def run_profile(args):
-    """Workloads for ncu captures (profiles/ cites these command lines)."""
+    """Fixed workloads for ncu captures (no timing, no JSON)."""
     import torch
     from arbinterp_gb300 import tricubic, synth
     dev = torch.device("cuda")
@@ -711,16 +711,18 @@ def _mem_available_gb():
     return 64.0
 
 
-def reference_cpu(field_np, q_np, nparts, run_parts, warm_parts=0, n=GRID[0]):
+def reference_cpu(field_np, q_np, nparts, run_parts, warm_parts=0, n=GRID[0], kind=None):
     """Run the CPU baseline: construct on every worker, then `warm_parts`
     untimed and `run_parts` timed steps (one part per worker per step).
-    Returns a dict of the measurements."""
+    Returns a dict of the measurements.  kind: 'reference' (oracle/_ref) or
+    'port' (the oracle); by default the reference where it is built."""
     import multiprocessing as mp
     import tempfile
     import numpy as np
     sys.path.insert(0, ROOT)
     from oracle import ref_build
-    kind = "reference" if ref_build.available() else "port"
+    if kind is None:
+        kind = "reference" if ref_build.available() else "port"
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
     # each worker holds the sorted field copy (805 MB), its share of the
     # coefficient arrays and the evaluation temporaries: about 6 GB at most
@@ -918,9 +920,9 @@ def main():
     kname = ("eval_sorted_kernel<3,4,table>" if use_tab else
              ("eval_binc_kernel<4>" if prec == "mixed" else "eval_sorted_kernel<3,4,fp64>"))
     # DRAM traffic per launch, scaled from the small-case ncu capture of the
-    # same kernel (profiles/eval_bin_kernel__tricubic160_both_mixed.md:
-    # EVAL_SMALL_TRAFFIC bytes for 2.02e6 queries on a 160^3 grid whose mixed
-    # grid is 81.92 MB), per query plus one read of the grid
+    # same kernel (`bench.py --profile small`: EVAL_SMALL_TRAFFIC bytes for
+    # 2.02e6 queries on a 160^3 grid whose mixed grid is 81.92 MB), per query
+    # plus one read of the grid
     traffic = ((nq * (EVAL_SMALL_TRAFFIC - 81.92e6) / 2.02e6 + grid_bytes)
                if (prec == "mixed" and not use_tab) else None)
     peak, peak_src = measured_peaks()
