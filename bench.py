@@ -619,6 +619,42 @@ def make_workload(device, rank=0, n=GRID[0]):
     return field, q, lo, hi, [h] * 3
 
 
+def copy_peaks(dev, nbytes=1 << 29, reps=3):
+    """Pinned host <-> device copy rates on this machine (GB/s): H2D and D2H alone,
+    and each direction while both run (two streams), best of `reps`."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    h2 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    h.fill_(1)
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def timed(fn):
+        best = None
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return nbytes / best / 1e9
+
+    def both():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    out = {"h2d_gbs": timed(lambda: d.copy_(h, non_blocking=True)),
+           "d2h_gbs": timed(lambda: h2.copy_(d2, non_blocking=True)),
+           "bidir_gbs_each": timed(both),
+           "how": f"pinned torch copies of {nbytes >> 20} MiB, best of {reps}; bidir: both directions at once"}
+    del h, h2, d, d2
+    return out
+
+
 def cuda_time(fn, steps, warmup, barrier=None):
     import torch
     for _ in range(warmup):
@@ -1032,9 +1068,20 @@ def main():
         ksteps = max(3, args.steps // 2)
         # the outputs are column views of one row buffer (packed: only the returned columns), copied whole
         d2h = last["rows_bytes"]
+        h2d = int(fnp.nbytes + qnp.nbytes)
+        cp = copy_peaks(dev)
+        # copy roofline: the link moves H2D and D2H bytes at the measured
+        # pinned rates; "link" ignores what depends on what, "staged" keeps the
+        # job's order (the whole field before any result, then the queries in
+        # and the results out at the concurrent per-direction rate)
+        link_floor = max(h2d / cp["h2d_gbs"], d2h / cp["d2h_gbs"],
+                         (h2d + d2h) / (2 * cp["bidir_gbs_each"])) / 1e6
+        staged_floor = (fnp.nbytes / cp["h2d_gbs"] + max(qnp.nbytes, d2h) / cp["bidir_gbs_each"]) / 1e6
+        ms_e2e = 1000 * te / ksteps
         e2e = {"value": world * nq * ksteps / te, "unit": "queries/s",
-               "h2d_bytes_per_step": int(fnp.nbytes + qnp.nbytes), "d2h_bytes_per_step": int(d2h),
-               "ms_per_step": 1000 * te / ksteps}
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(d2h), "ms_per_step": ms_e2e,
+               "copy_peak": cp, "copy_floor_ms": {"link": link_floor, "staged": staged_floor},
+               "copy_frac": {"link": link_floor / ms_e2e, "staged": staged_floor / ms_e2e}}
 
     # the other seeded configurations, measured in the same run (one GPU)
     if rank == 0 and world == 1 and not args.no_configs:
