@@ -318,6 +318,266 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
   if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
 }
 
+// ---- full solves: the block gather fed by TMA -------------------------------
+// allCoeffs over every cell.  A tile holds C = 128 / F consecutive cells of one
+// x-row of cells (C x F rows of the table; the last tile of each row holds the
+// row's remaining cells).  Its grid footprint -- C + 3 points along x, 4
+// along y and z -- arrives in shared memory as 3D TMA boxes (zeros beyond the
+// grid), issued by one thread as soon as the previous tile's A operand is
+// built, so the load overlaps that tile's MMAs, epilogue and stores; the
+// gather then reads the footprint from shared memory (one float per (row,
+// point): a warp reads consecutive words) instead of global memory.
+// Footprint boxes (the TMA rule: x * element size a multiple of 16 bytes):
+//   F = 4: hi, 4 x 35 floats x 4 x 4 (x = 4 x0); lo of |B|, 40 x 4 x 4 floats
+//          from x = x0 rounded down to a multiple of 4 (needs nx % 4 == 0);
+//   F = 3: hi, 4 x 45 floats x 4 x 4;
+//   F = 1: (hi, lo) pairs as 8-byte elements, 132 x 4 x 4, x0 even (needs nx
+//          even: the row stride must be a multiple of 16 bytes).
+// Grids that miss these rules, and partial solves, take coef3_tc_kernel.
+namespace {
+template <int F>
+struct TmaShape;
+template <>
+struct TmaShape<4> {
+  static constexpr int C = 32, HX = 35, LX = 40, HBYTES = 4 * HX * 16 * 4, LBYTES = LX * 16 * 4;
+};
+template <>
+struct TmaShape<3> {
+  static constexpr int C = 42, HX = 45, HBYTES = 4 * HX * 16 * 4, LBYTES = 0;
+};
+template <>
+struct TmaShape<1> {
+  static constexpr int C = 128, HX = 132, HBYTES = HX * 16 * 8, LBYTES = 0;
+};
+constexpr int FP_BYTES = 17408;  // >= every shape's HBYTES + LBYTES, a multiple of 1 KB
+
+struct TcTmaSmem {
+  unsigned char a[A_BYTES];              // A tile, no-swizzle K-major (offset 0)
+  unsigned char b[B_BYTES];              // B = 8 A (offset 48 KB)
+  unsigned char stage[2][BOX_BYTES];     // output rows, 128-byte swizzled (offset 56 KB)
+  unsigned char fp[FP_BYTES];            // the tile's grid footprint (offset 88 KB)
+  float amax[2][TM];
+  uint64_t mbar;                         // MMA completion
+  uint64_t mbar_fp;                      // footprint arrival
+  uint32_t tmem_base;
+};
+static_assert(TmaShape<4>::HBYTES + TmaShape<4>::LBYTES <= FP_BYTES && TmaShape<3>::HBYTES <= FP_BYTES &&
+                  TmaShape<1>::HBYTES <= FP_BYTES,
+              "footprint buffer");
+static_assert(offsetof(TcTmaSmem, stage) % 1024 == 0 && offsetof(TcTmaSmem, fp) % 1024 == 0, "alignment");
+}  // namespace
+
+template <int F>
+__global__ void __launch_bounds__(NT, 2) coef3_tma_kernel(const __grid_constant__ CUtensorMap tmap_full,
+                                                          const __grid_constant__ CUtensorMap tmap_part,
+                                                          const __grid_constant__ CUtensorMap tmap_hi,
+                                                          const __grid_constant__ CUtensorMap tmap_lo, arb_grid g,
+                                                          int32_t *status) {
+  using S = TmaShape<F>;
+  extern __shared__ unsigned char smem_raw[];
+  TcTmaSmem &sm = *reinterpret_cast<TcTmaSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (TM - 1), half = tid >> 7;
+  const int64_t ncx = g.n[0] - 3, ncy = g.n[1] - 3, ncz = g.n[2] - 3;
+  const int64_t tpr = (ncx + S::C - 1) / S::C;          // tiles per x-row of cells
+  const int rem = (int)(ncx - (tpr - 1) * S::C);         // cells in a row's last tile
+  const int64_t ntiles = tpr * ncy * ncz;
+  const int cl = row / F, f = row % F;                   // this row's cell in the tile, and field
+
+  for (int e = tid; e < 64 * 64; e += NT) {
+    const int n = e >> 6, k = e & 63;
+    const float v = 8.f * kA1[n & 3][k & 3] * kA1[(n >> 2) & 3][(k >> 2) & 3] * kA1[n >> 4][k >> 4];
+    *reinterpret_cast<__half *>(sm.b + kmaj(n, k, B_SBO)) = __float2half_rn(v);
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(&sm.tmem_base, TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  // footprint boxes of one tile, on mbar_fp (issued by one thread)
+  auto issue_fp = [&](int64_t tile) {
+    const int64_t xr = tile / tpr;
+    const int x0 = (int)((tile - xr * tpr) * S::C);
+    const int y = (int)(xr % ncy), z = (int)(xr / ncy);
+    tc::mbar_arrive_expect_tx(&sm.mbar_fp, (uint32_t)(S::HBYTES + S::LBYTES));
+    if constexpr (F == 1) {
+      tc::tma_load_3d(sm.fp, &tmap_hi, x0 & ~1, y, z, &sm.mbar_fp);
+    } else {
+      tc::tma_load_3d(sm.fp, &tmap_hi, 4 * x0, y, z, &sm.mbar_fp);
+      if constexpr (F == 4) tc::tma_load_3d(sm.fp + S::HBYTES, &tmap_lo, x0 & ~3, y, z, &sm.mbar_fp);
+    }
+  };
+  if (tid == 0) {
+    tc::mbar_init(&sm.mbar, 1);
+    tc::mbar_init(&sm.mbar_fp, 1);
+    tc::fence_mbar_init();
+  }
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  if (tid == 0 && blockIdx.x < ntiles) issue_fp(blockIdx.x);
+  bool fp_pending = blockIdx.x < ntiles;
+  const uint32_t tmem = sm.tmem_base;
+  const uint32_t idesc = tc::idesc_f16(0u, 128u, 64u);
+  const uint32_t a_base = tc::smem_u32(sm.a), b_base = tc::smem_u32(sm.b);
+  const uint32_t t_row = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * 32);
+  unsigned char *st_row = sm.stage[half] + row * 128;
+  uint32_t parity = 0, pfp = 0;
+  bool timed_out = false, fp_timed_out = false;
+  const uint32_t mma_wait_limit = g_mma_wait_limit;
+
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t xr = tile / tpr;
+    const int64_t kx = tile - xr * tpr;
+    const int x0 = (int)(kx * S::C);
+    const int cnt = kx == tpr - 1 ? rem : S::C;
+    const int64_t row0 = (xr * ncx + x0) * F;             // first table row of the tile
+    // ---- the footprint has landed ------------------------------------------
+    const bool fok = tc::mbar_wait_bounded(&sm.mbar_fp, pfp, WAIT_LIMIT);
+    pfp ^= 1u;
+    if (!fok) set_status(status, ARB_ERR_TIMEOUT);
+    if (__syncthreads_or(!fok)) {
+      fp_timed_out = true;
+      break;
+    }
+    fp_pending = false;
+    // ---- gather block layers oz = 2h, 2h+1 as deltas to the corner ---------
+    float rhi = 0.f, rlo = 0.f, d[32], amax = 0.f;
+    if (cl < cnt) {
+      const float *fh = reinterpret_cast<const float *>(sm.fp);
+      auto pt = [&](int ox, int oy, int oz, float &h, float &l) {
+        const int P = (oz * 4 + oy) * S::HX + cl + ox;
+        if constexpr (F == 1) {
+          const float2 v = reinterpret_cast<const float2 *>(sm.fp)[P + (x0 & 1)];
+          h = v.x;
+          l = v.y;
+        } else {
+          h = fh[4 * P + f];
+          l = 0.f;
+          if constexpr (F == 4) {
+            if (f == 3)
+              l = reinterpret_cast<const float *>(sm.fp + S::HBYTES)[(oz * 4 + oy) * S::LX + cl + ox + (x0 & 3)];
+          }
+        }
+      };
+      pt(1, 1, 1, rhi, rlo);
+#pragma unroll
+      for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+        for (int oy = 0; oy < 4; ++oy)
+#pragma unroll
+          for (int ox = 0; ox < 4; ox += 2) {
+            float h0, l0, h1, l1;
+            pt(ox, oy, 2 * half + oz, h0, l0);
+            pt(ox + 1, oy, 2 * half + oz, h1, l1);
+            const float2 dd = fadd2(fsub2(make_float2(h0, h1), make_float2(rhi, rhi)),
+                                    fsub2(make_float2(l0, l1), make_float2(rlo, rlo)));
+            d[oz * 16 + oy * 4 + ox] = dd.x;
+            d[oz * 16 + oy * 4 + ox + 1] = dd.y;
+            amax = fmaxf(amax, fmaxf(fabsf(dd.x), fabsf(dd.y)));
+          }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) d[j] = 0.f;
+    }
+    sm.amax[half][row] = amax;
+    __syncthreads();
+    const int E = scale_exp(fmaxf(amax, sm.amax[half ^ 1][row]));
+    const float c10 = __uint_as_float((uint32_t)(137 - E) << 23);    // 2^(10 - E)
+    // ---- three-part FP16 split into the A tile ------------------------------
+#pragma unroll
+    for (int ch = 0; ch < 4; ++ch) {
+      uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        float2 h0, h1, h2;
+        split3_pair(fmul2(make_float2(d[ch * 8 + v * 2], d[ch * 8 + v * 2 + 1]), make_float2(c10, c10)), kRound1,
+                    4194304.0f, h0, h1, h2);
+        w0[v] = pack_h2(h0.x, h0.y);
+        w1[v] = pack_h2(h1.x, h1.y);
+        w2[v] = pack_h2(h2.x, h2.y);
+      }
+      const int k = half * 32 + ch * 8;
+      *reinterpret_cast<uint4 *>(sm.a + kmaj(row, k, A_SBO)) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+      *reinterpret_cast<uint4 *>(sm.a + kmaj(row, KP + k, A_SBO)) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+      *reinterpret_cast<uint4 *>(sm.a + kmaj(row, 2 * KP + k, A_SBO)) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+    }
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    if (tid == 0) tc::bulk_wait_read0();  // the previous tile's stores have read the staging buffer
+    __syncthreads();
+    // every thread has read the footprint: the next tile's boxes may land
+    const int64_t next = tile + gridDim.x;
+    if (next < ntiles) {
+      if (tid == 0) issue_fp(next);
+      fp_pending = true;
+    }
+    // ---- 12 MMAs of 128 x 64 x 16: part p accumulates into columns 64p -----
+    if (tid == 0) {
+      tc::tc_fence_after();
+#pragma unroll
+      for (int p = 0; p < PARTS; ++p)
+#pragma unroll
+        for (int kc = 0; kc < 4; ++kc) {
+          const int s = p * 4 + kc;
+          const uint64_t ad = tc::smem_desc(a_base + (uint32_t)(2 * s) * 128u, 128u, (uint32_t)A_SBO);
+          const uint64_t bd = tc::smem_desc(b_base + (uint32_t)(2 * kc) * 128u, 128u, (uint32_t)B_SBO);
+          tc::mma_f16(tmem + (uint32_t)(64 * p), ad, bd, idesc, kc > 0 ? 1u : 0u);
+        }
+      tc::mma_commit(&sm.mbar);
+    }
+    const bool ok = tc::mbar_wait_bounded(&sm.mbar, parity, mma_wait_limit);
+    parity ^= 1u;
+    if (!ok) set_status(status, ARB_ERR_TIMEOUT);
+    tc::tc_fence_after();
+    if (__syncthreads_or(!ok)) {
+      timed_out = true;
+      break;
+    }
+    // ---- epilogue: combine the part sums, stage swizzled, TMA-store --------
+    float a[32], t[32];
+    tc::tmem_ld16(t_row + 128u, t);
+    tc::tmem_ld16(t_row + 144u, t + 16);
+    tc::tmem_ld16(t_row + 64u, a);
+    tc::tmem_ld16(t_row + 80u, a + 16);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 32; ++j) t[j] = __fmaf_rn(t[j], 0x1p-22f, a[j]);
+    tc::tmem_ld16(t_row, a);
+    tc::tmem_ld16(t_row + 16u, a + 16);
+    tc::tmem_wait_ld();
+    const float so = __uint_as_float((uint32_t)(E - 13 + 127) << 23);   // 2^(E - 13)
+#pragma unroll
+    for (int j = 0; j < 32; ++j) a[j] = __fmul_rn(__fadd_rn(a[j], t[j]), so);
+    if (half == 0) a[0] = rhi + (rlo + a[0]);
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      *reinterpret_cast<float4 *>(st_row + 16 * (q ^ (row & 7))) =
+          make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      const CUtensorMap *tm = cnt == S::C ? &tmap_full : &tmap_part;
+      tc::tma_store_2d(tm, sm.stage[0], 0, (int32_t)row0);
+      tc::tma_store_2d(tm, sm.stage[1], 32, (int32_t)row0);
+      tc::bulk_commit();
+    }
+  }
+  if (tid == 0) tc::bulk_wait0();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  // after a timed-out wait: one more bounded wait for the MMAs in flight
+  // before the accumulator columns are released, and for a footprint load
+  // still in flight before the CTA's shared memory is given back
+  if (timed_out) (void)tc::mbar_wait_bounded(&sm.mbar, parity ^ 1u, WAIT_LIMIT);
+  if ((timed_out || fp_timed_out) && fp_pending)
+    (void)tc::mbar_wait_bounded(&sm.mbar_fp, fp_timed_out ? pfp ^ 1u : pfp, WAIT_LIMIT);
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+}
+
 static int num_sms() {
   return device_sms();
 }
@@ -350,11 +610,104 @@ extern "C" int arb_test_set_mma_wait_limit(int64_t limit) {
 // Host launcher used by arb_coef_solve for 3D mixed precision.  The table is
 // written as a 2D tensor [rows][64] float32 (rows = ncells x nfield) through
 // 128-row x 32-float boxes in the 128-byte swizzled layout.
+// Full solves through coef3_tma_kernel; returns ARB_ERR_UNSUPPORTED (nothing
+// launched) where the grid misses the TMA rules, so the caller falls back.
+template <int F>
+static int coef3_solve_tma(const arb_grid *g, float *table, int32_t *status, cudaStream_t s, EncodeTiled encode) {
+  using S = TmaShape<F>;
+  const int64_t nx = g->n[0], ny = g->n[1], nz = g->n[2];
+  if ((F == 4 && nx % 4 != 0) || (F == 1 && nx % 2 != 0)) return ARB_ERR_UNSUPPORTED;
+  const int64_t rows = g->nc * F;
+  if (rows >= ((int64_t)1 << 31) || nx > ((int64_t)1 << 30) || ny > ((int64_t)1 << 30) || nz > ((int64_t)1 << 30))
+    return ARB_ERR_UNSUPPORTED;
+  const int64_t ncx = nx - 3;
+  const int64_t tpr = (ncx + S::C - 1) / S::C;
+  const int rem = (int)(ncx - (tpr - 1) * S::C);
+  const size_t smem = sizeof(TcTmaSmem) + 1024;
+  static std::once_flag once[MAX_DEVICES];
+  static int per_sm_dev[MAX_DEVICES];
+  static cudaError_t attr_err[MAX_DEVICES];
+  const int dev = current_device();
+  if (dev < 0) return ARB_ERR_CUDA;
+  std::call_once(once[dev], [&] {
+    attr_err[dev] = cudaFuncSetAttribute(coef3_tma_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (attr_err[dev] == cudaSuccess)
+      attr_err[dev] = cudaFuncSetAttribute(coef3_tma_kernel<F>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    // CTAs per SM from the shared memory (1 KB reserved per CTA); TMEM
+    // (2 x 256 columns) allows two
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    const int n = (int)(smem_sm / (int64_t)(smem + 1024));
+    per_sm_dev[dev] = n < 1 ? 1 : (n > 2 ? 2 : n);
+  });
+  if (attr_err[dev] != cudaSuccess) return ARB_ERR_CUDA;
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUtensorMap tm_full, tm_part, tm_hi, tm_lo;
+  {  // table rows: full tiles and the last tile of each row
+    const cuuint64_t dims[2] = {64, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {64 * sizeof(float)};
+    const cuuint32_t box_f[2] = {32, (cuuint32_t)(S::C * F)}, box_p[2] = {32, (cuuint32_t)(rem * F)};
+    if (encode(&tm_full, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, table, dims, strides, box_f, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+        encode(&tm_part, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, table, dims, strides, box_p, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return ARB_ERR_CUDA;
+  }
+  {  // grid footprints
+    float *g32 = const_cast<float *>(g->grid32);
+    if (F == 1) {
+      const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+      const cuuint64_t strides[2] = {(cuuint64_t)(8 * nx), (cuuint64_t)(8 * nx * ny)};
+      const cuuint32_t box[3] = {(cuuint32_t)S::HX, 4, 4};
+      if (encode(&tm_hi, CU_TENSOR_MAP_DATA_TYPE_INT64, 3, g32, dims, strides, box, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return ARB_ERR_CUDA;
+    } else {
+      const cuuint64_t dims[3] = {(cuuint64_t)(4 * nx), (cuuint64_t)ny, (cuuint64_t)nz};
+      const cuuint64_t strides[2] = {(cuuint64_t)(16 * nx), (cuuint64_t)(16 * nx * ny)};
+      const cuuint32_t box[3] = {(cuuint32_t)(4 * S::HX), 4, 4};
+      if (encode(&tm_hi, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, g32, dims, strides, box, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return ARB_ERR_CUDA;
+    }
+    tm_lo = tm_hi;
+    if (F == 4) {
+      const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+      const cuuint64_t strides[2] = {(cuuint64_t)(4 * nx), (cuuint64_t)(4 * nx * ny)};
+      const cuuint32_t box[3] = {(cuuint32_t)TmaShape<4>::LX, 4, 4};
+      if (encode(&tm_lo, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, g32 + 4 * nx * ny * nz, dims, strides, box, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return ARB_ERR_CUDA;
+    }
+  }
+  const int64_t tiles = tpr * (ny - 3) * (nz - 3);
+  int64_t grid = (int64_t)num_sms() * per_sm_dev[dev];
+  if (grid > tiles) grid = tiles;
+  if (grid < 1) return ARB_OK;
+  coef3_tma_kernel<F><<<(unsigned)grid, NT, smem, s>>>(tm_full, tm_part, tm_hi, tm_lo, *g, status);
+  return launch_status();
+}
+
 int coef3_solve_tc(const arb_grid *g, int64_t cell0, int64_t ncells, float *table, int32_t *status,
                    cudaStream_t s) {
   if (!g->grid32 || ((uintptr_t)table & 15u)) return ARB_ERR_INVALID;
   const EncodeTiled encode = encode_fn();
   if (!encode) return ARB_ERR_CUDA;
+  if (cell0 == 0 && ncells == g->nc) {
+    int rc = ARB_ERR_UNSUPPORTED;
+    switch (g->nfield) {
+      case 1: rc = coef3_solve_tma<1>(g, table, status, s, encode); break;
+      case 3: rc = coef3_solve_tma<3>(g, table, status, s, encode); break;
+      case 4: rc = coef3_solve_tma<4>(g, table, status, s, encode); break;
+      default: break;
+    }
+    if (rc != ARB_ERR_UNSUPPORTED) return rc;
+  }
   const size_t smem = sizeof(TcSmem) + 1024;
   static_assert(3 * (sizeof(TcSmem) + 1024 + 1024) > 228 * 1024, "a third CTA per SM would oversubscribe TMEM");
   static_assert(offsetof(TcSmem, stage) % 1024 == 0, "swizzled boxes need 1 KB alignment");

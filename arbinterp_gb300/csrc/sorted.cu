@@ -519,7 +519,7 @@ __device__ __forceinline__ int64_t sched_record(const BinSched &sc, uint32_t t) 
 }
 
 template <int F>
-__global__ void __launch_bounds__(BINC_THREADS, 3) eval_binc_kernel(arb_grid g, KParams kp, BinGeom bg,
+__global__ void __launch_bounds__(BINC_THREADS, F == 4 ? 3 : (F == 3 ? 5 : 4)) eval_binc_kernel(arb_grid g, KParams kp, BinGeom bg,
                                                                    int64_t nq, arb_query_out o, SortedWork w) {
   extern __shared__ __align__(16) unsigned char binc_smem[];
   BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(binc_smem);

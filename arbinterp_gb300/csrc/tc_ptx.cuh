@@ -148,6 +148,17 @@ __device__ __forceinline__ void tma_store_2d(const void *tmap, const void *ssrc,
                "r"(x), "r"(y), "r"(smem_u32(ssrc))
                : "memory");
 }
+// 3D tiled tensor load global -> shared through a tensor map, completing on
+// an mbarrier (which must expect the box's bytes).  Box elements outside the
+// tensor are filled with zeros.
+__device__ __forceinline__ void tma_load_3d(void *sdst, const void *tmap, int32_t x, int32_t y, int32_t z,
+                                            uint64_t *mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(sdst)),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(mbar))
+      : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read0() {
   asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");

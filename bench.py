@@ -77,7 +77,7 @@ def parse():
     return p.parse_args()
 
 
-EVAL_SMALL_TRAFFIC = 252.54e6  # dram read + write of eval_bin_kernel<4> on the 160^3 case (ncu capture)
+EVAL_SMALL_TRAFFIC = 246.96e6  # dram read + write of eval_binc_kernel<4> on the 160^3 case (ncu capture)
 # dram read + write of eval_tab_coop_kernel<4, mixed> per query: 1.902 GB for 2.02e6 queries on the
 # 160^3 table (3.94M cells; ncu capture)
 TAB_SMALL_TRAFFIC_PER_QUERY = (1.777388e9 + 0.124713e9) / 2.02e6
