@@ -8,15 +8,16 @@
 //
 //   count    : cell index + fractional offset (exactly the reference's
 //              iu = (q - IntMin)/h, floor, flat index), the out-of-volume
-//              bookkeeping of rQuery (NaN rows, queryInds) and the bin
+//              bookkeeping of rQuery (NaN rows, queryInds) and the sub-bin
 //              histogram (fire-and-forget atomics)
-//   scan     : exclusive prefix sum of the bin histogram
-//   place    : the same coordinate step again, a slot in the query's bin
-//              (atomic on the running offset) and one 32-byte record
-//              (packed cell, row, fraction) written there; afterwards
-//              hist[b] is the end of bin b
-//   evaluate : on-the-fly or table evaluation in bin order, outputs written
-//              to the query's original row
+//   scan     : exclusive prefix sum of the histogram into a second array
+//              (the counts stay)
+//   place    : the same coordinate step again, a rank inside the query's
+//              sub-bin (an atomic that counts the histogram back down to
+//              zero) and one 32-byte record (packed cell, row, fraction)
+//              written at its final position
+//   evaluate : on-the-fly or table evaluation in record order, outputs
+//              written to the query's original row
 // Recomputing the coordinate step (float32 pipe in mixed precision) is
 // cheaper than storing it: the unsorted intermediates and a separate scatter
 // pass cost three partial-sector writes per query, the record one full one.
@@ -52,16 +53,20 @@ struct __align__(16) QRec<double> {
 static_assert(sizeof(QRec<float>) == 32 && sizeof(QRec<double>) == 48, "record sizes");
 
 struct SortedWork {
-  uint32_t *hist;  // nsub + 1: counts, exclusive offsets after the scan, sub-bin ends after placement
-  uint32_t *part;  // per-block totals of the scan
-  void *rec;       // nq records (QRec<float> or QRec<double>), sub-bin order
+  uint32_t *hist;   // nsub + 1 sub-bin counts; placement counts them back down to zero
+  uint32_t *offs;   // nsub + 1 exclusive offsets: sub-bin sb holds records [offs[sb], offs[sb + 1]),
+                    // the special sub-bin nsub [offs[nsub], nq)
+  uint32_t *part;   // per-block totals of the scan
+  void *rec;        // nq records (QRec<float> or QRec<double>) in bin order; with bank classes each
+                    // bin's records are in its bank schedule (see bank_slot)
 };
 
 struct BinGeom {
   int64_t nb[4];     // bins per axis
   int64_t nbins;     // product
   int shift;         // log2 cells per bin edge
-  int cls;           // log2 bank classes per bin (3: 3D mixed 8^3-cell bins; 0 otherwise)
+  int cls;           // log2 bank classes per bin (3: 3D mixed 8^3-cell bins; 4: 4D mixed scalar
+                     // 4^4-cell bins; 0 otherwise)
   int64_t nsub;      // nbins << cls sub-bins (bin-major); the special sub-bin is index nsub
 };
 
@@ -71,6 +76,15 @@ struct BinGeom {
 // multiple of 8 on every axis, so the global cell coordinates give it.
 __host__ __device__ __forceinline__ int bank_class(int64_t cx, int64_t cy, int64_t cz) {
   return (int)((cx + 3 * cy + cz) & 7);
+}
+
+// 4D: the 8-byte bank slot (mod 16) of the cell's corner point in an unpadded
+// 7^4 tile of (hi, lo) pairs (x + 7 y + 49 z + 343 t, with 49 = 1 and
+// 343 = 7 mod 16).  Bin origins are multiples of 4, so the class from the
+// global cell coordinates is the local one plus a constant per bin: the
+// classes of one bin still map to 16 distinct slots.
+__host__ __device__ __forceinline__ int bank_class4(int64_t cx, int64_t cy, int64_t cz, int64_t ct) {
+  return (int)((cx + 7 * cy + cz + 7 * ct) & 15);
 }
 
 static inline BinGeom bin_geom(const arb_grid *g, int precision) {
@@ -86,7 +100,11 @@ static inline BinGeom bin_geom(const arb_grid *g, int precision) {
     }
     b.nbins *= b.nb[a];
   }
-  b.cls = (g->dim == 3 && precision == ARB_PREC_MIXED && b.shift == 3) ? 3 : 0;
+  b.cls = 0;
+  if (precision == ARB_PREC_MIXED) {
+    if (g->dim == 3 && b.shift == 3) b.cls = 3;
+    if (g->dim == 4 && b.shift == 2 && g->nfield == 1) b.cls = 4;
+  }
   b.nsub = b.nbins << b.cls;
   return b;
 }
@@ -112,6 +130,7 @@ static size_t carve(SortedWork *w, void *base, const arb_grid *g, int precision,
   };
   SortedWork t;
   t.hist = (uint32_t *)take(sizeof(uint32_t) * (bg.nsub + 1));
+  t.offs = (uint32_t *)take(sizeof(uint32_t) * (bg.nsub + 1));
   t.part = (uint32_t *)take(sizeof(uint32_t) * scan_blocks(bg.nsub + 1));
   t.rec = take((tsz == 4 ? sizeof(QRec<float>) : sizeof(QRec<double>)) * nq);
   if (w) *w = t;
@@ -150,6 +169,8 @@ __device__ __forceinline__ CoordStep bin_step(const arb_grid &g, const KParams &
     for (int a = DIM - 2; a >= 0; --a) bin = bin * bg.nb[a] + (c[a] >> bg.shift);
     if constexpr (DIM == 3) {
       if (bg.cls) bin = (bin << 3) | bank_class(c[0], c[1], c[2]);
+    } else {
+      if (bg.cls) bin = (bin << 4) | bank_class4(c[0], c[1], c[2], c[3]);
     }
   }
   return s;
@@ -177,6 +198,23 @@ __global__ void __launch_bounds__(256) bin_count_kernel(arb_grid g, KParams kp, 
     for (int64_t c = 0; c < qs; ++c) qr[c] = qnan();
 }
 
+// Position of the query of rank r in class c of a bin whose NC class
+// sub-bins start at o[0..NC-1] (o[NC]: the bin's end), in the bin's bank
+// schedule: round robin over the classes, level l holding the l-th query of
+// every class with more than l, classes in increasing order within a level.
+// So every NC consecutive records of a level with all classes present have
+// NC distinct bank classes, wherever the NC start.
+template <int NC>
+__device__ __forceinline__ uint32_t bank_slot(const uint32_t o[NC + 1], int c, uint32_t r) {
+  uint32_t pos = o[0];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    const uint32_t n = o[k + 1] - o[k];
+    pos += min(n, r) + ((k < c && n > r) ? 1u : 0u);
+  }
+  return pos;
+}
+
 template <int DIM, bool EXACT, typename T>
 __global__ void __launch_bounds__(256) bin_place_kernel(arb_grid g, KParams kp, BinGeom bg, const double *q,
                                                         int64_t nq, int64_t qs, SortedWork w) {
@@ -187,21 +225,40 @@ __global__ void __launch_bounds__(256) bin_place_kernel(arb_grid g, KParams kp, 
   int64_t bin;
   bool bad;
   (void)bin_step<DIM, EXACT, T>(g, kp, bg, q + i * qs, frac, cw, bin, bad);
-  const uint32_t pos = atomicAdd(&w.hist[bin], 1u);
-  QRec<T> r;
-  r.cell = cw;
-  r.row = (uint32_t)i;
+  // rank inside the sub-bin (any order: the count runs back down to zero)
+  const uint32_t r = atomicSub(&w.hist[bin], 1u) - 1u;
+  uint32_t pos;
+  if (bg.cls && bin < bg.nsub) {
+    constexpr int NC = DIM == 3 ? 8 : 16;  // the class sub-bins of one bin, 32- or 64-byte aligned
+    const int64_t b0 = bin & ~(int64_t)(NC - 1);
+    uint32_t o[NC + 1];
 #pragma unroll
-  for (int a = 0; a < 4; ++a) r.f[a] = a < DIM ? frac[a] : T(0);
-  r.pad = 0;
+    for (int k = 0; k < NC; k += 4) {
+      const uint4 a = *reinterpret_cast<const uint4 *>(w.offs + b0 + k);
+      o[k] = a.x;
+      o[k + 1] = a.y;
+      o[k + 2] = a.z;
+      o[k + 3] = a.w;
+    }
+    o[NC] = w.offs[b0 + NC];
+    pos = bank_slot<NC>(o, (int)(bin & (NC - 1)), r);
+  } else {
+    pos = w.offs[bin] + r;
+  }
+  QRec<T> rec;
+  rec.cell = cw;
+  rec.row = (uint32_t)i;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) rec.f[a] = a < DIM ? frac[a] : T(0);
+  rec.pad = 0;
   if constexpr (sizeof(T) == 4) {
     // one 32-byte store: a whole sector, no partial-sector merge in L2
-    const uint32_t *u = reinterpret_cast<const uint32_t *>(&r);
+    const uint32_t *u = reinterpret_cast<const uint32_t *>(&rec);
     asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(reinterpret_cast<QRec<T> *>(w.rec) + pos),
                  "r"(u[0]), "r"(u[1]), "r"(u[2]), "r"(u[3]), "r"(u[4]), "r"(u[5]), "r"(u[6]), "r"(u[7])
                  : "memory");
   } else {
-    reinterpret_cast<QRec<T> *>(w.rec)[pos] = r;
+    reinterpret_cast<QRec<T> *>(w.rec)[pos] = rec;
   }
 }
 
@@ -225,8 +282,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_part_kernel(const uint32_t 
   }
 }
 
-// Exclusive scan of each chunk, offset by the totals of the chunks before it.
-__global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(uint32_t *hist, int64_t n, const uint32_t *part) {
+// Exclusive scan of each chunk into offs, offset by the totals of the chunks
+// before it (the counts in hist stay for the placement pass).
+__global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(const uint32_t *hist, int64_t n,
+                                                                  const uint32_t *part, uint32_t *offs) {
   __shared__ uint32_t wsum[SCAN_THREADS / 32];
   __shared__ uint32_t carry_s;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -275,7 +334,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(uint32_t *hist
   uint32_t run = carry + wsum[warp] + (incl - sum);
 #pragma unroll
   for (int k = 0; k < SCAN_PER; ++k) {
-    if (b + k < n) hist[b + k] = run;
+    if (b + k < n) offs[b + k] = run;
     run += v[k];
   }
 }
@@ -375,20 +434,10 @@ __device__ __forceinline__ void cp_async4(void *sdst, const void *gsrc) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-// grid-point origin of bin b (x fastest)
-__device__ __forceinline__ void bin_origin(int64_t b, const BinGeom &bg, int64_t o[3]) {
-  o[0] = (b % bg.nb[0]) * BIN_EDGE;
-  const int64_t r = b / bg.nb[0];
-  o[1] = (r % bg.nb[1]) * BIN_EDGE;
-  o[2] = (r / bg.nb[1]) * BIN_EDGE;
-}
-
-// Copy bin b's footprint into `t` (points outside the grid are skipped: no
-// cell of the bin reads them).
+// Copy the footprint of the bin whose tile origin is o into `t` (points
+// outside the grid are skipped: no cell of the bin reads them).
 template <int F>
-__device__ __forceinline__ void load_bin_tile(const arb_grid &g, const BinGeom &bg, int64_t b, BinTile<F> &t) {
-  int64_t o[3];
-  bin_origin(b, bg, o);
+__device__ __forceinline__ void load_bin_tile(const arb_grid &g, const int o[3], BinTile<F> &t) {
   const int64_t nx = g.n[0], ny = g.n[1], nz = g.n[2];
   const int64_t npts = nx * ny * nz;
   for (int e = threadIdx.x; e < TILE_PTS; e += blockDim.x) {
@@ -454,105 +503,57 @@ struct TileBlock3<3> {
   __device__ __forceinline__ float4 hi4(int p) const { return v[p]; }
 };
 
-// Round-robin order of one bin's queries over its 8 bank classes.  Level r
-// holds the r-th query of every class that has more than r; levels come one
-// after another, classes in increasing order within a level.  With the class
-// counts sorted, m_0 <= ... <= m_7, segment s covers levels [m_(s-1), m_s)
-// and holds 8 - s classes per level.
-struct BinSched {
-  uint32_t start[8];    // first record of each class
-  uint32_t slot[9];     // first slot of each segment; slot[8] = queries in the bin
-  uint32_t lvl[8];      // first level of each segment
-  uint8_t cls[8][8];    // classes of segment s, increasing
-  uint32_t sorted[8];   // class counts in increasing order (set-up scratch)
-};
-
-// Warp 0 fills the schedule of bin b from the sub-bin ends in hist.
-__device__ __forceinline__ void bin_sched(const uint32_t *hist, int64_t b, BinSched &sc) {
-  const int l = threadIdx.x;  // called by warp 0 only
-  const int64_t sb = (b << 3) + (l & 7);
-  uint32_t st = 0, cnt = 0;
-  if (l < 8) {
-    st = sb > 0 ? hist[sb - 1] : 0u;
-    cnt = hist[sb] - st;
-  }
-  int rank = 0;
-#pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    const uint32_t cm = __shfl_sync(0xffffffffu, cnt, m);
-    rank += (cm < cnt || (cm == cnt && m < l)) ? 1 : 0;
-  }
-  if (l < 8) {
-    sc.start[l] = st;
-    sc.sorted[rank] = cnt;
-  }
-  __syncwarp();
-#pragma unroll
-  for (int sg = 0; sg < 8; ++sg) {
-    const unsigned act = __ballot_sync(0xffffffffu, l < 8 && rank >= sg);
-    if (l < 8 && rank >= sg) sc.cls[sg][__popc(act & ((1u << l) - 1u))] = (uint8_t)l;
-  }
-  if (l == 0) {
-    uint32_t prev = 0, slot = 0;
-#pragma unroll
-    for (int sg = 0; sg < 8; ++sg) {
-      const uint32_t m = sc.sorted[sg];
-      sc.slot[sg] = slot;
-      sc.lvl[sg] = prev;
-      slot += (m - prev) * (uint32_t)(8 - sg);
-      prev = m;
-    }
-    sc.slot[8] = slot;
-  }
-}
-
-// Record index (absolute) of slot t of the bin.
-__device__ __forceinline__ int64_t sched_record(const BinSched &sc, uint32_t t) {
-  int sg = 0;
-#pragma unroll
-  for (int q = 1; q < 8; ++q) sg += t >= sc.slot[q] ? 1 : 0;
-  const uint32_t off = t - sc.slot[sg];
-  const uint32_t k = 8u - (uint32_t)sg;
-  const uint32_t lv = off / k;
-  const int c = sc.cls[sg][off - lv * k];
-  return (int64_t)sc.start[c] + sc.lvl[sg] + lv;
-}
-
+// One CTA per bin (round-robin over bins, so the CTAs work on neighbouring
+// bins at the same time and their tiles' shared halo points are read from
+// HBM about once): the bin's tile is copied into shared memory with
+// cp.async, double-buffered so the next bin's copy overlaps this bin's
+// queries, and thread t of the CTA evaluates records t, t + BINC_THREADS, ...
+// of the bin, which placement wrote in the bin's bank schedule.
 template <int F>
 __global__ void __launch_bounds__(BINC_THREADS, F == 4 ? 3 : (F == 3 ? 5 : 4)) eval_binc_kernel(arb_grid g, KParams kp, BinGeom bg,
                                                                    int64_t nq, arb_query_out o, SortedWork w) {
   extern __shared__ __align__(16) unsigned char binc_smem[];
   BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(binc_smem);
-  __shared__ BinSched sc;
   const int64_t nbins = bg.nbins;
   const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
-  // after placement hist[sb] is the end of sub-bin sb; bin b is sub-bins 8b .. 8b + 7
-  auto sub_begin = [&](int64_t sb) { return sb > 0 ? (int64_t)w.hist[sb - 1] : (int64_t)0; };
-  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[(bb << 3) + 7] - sub_begin(bb << 3) : 0; };
+  // bin b holds records [offs[8b], offs[8b + 8]) (its 8 class sub-bins)
+  auto begin = [&](int64_t bb) { return w.offs[bb << 3]; };
+  auto count = [&](int64_t bb) { return bb < nbins ? w.offs[(bb + 1) << 3] - begin(bb) : 0u; };
+  auto origin = [&](int64_t bb, int og[3]) {
+    og[0] = (int)((bb % bg.nb[0]) * BIN_EDGE);
+    const int64_t r = bb / bg.nb[0];
+    og[1] = (int)((r % bg.nb[1]) * BIN_EDGE);
+    og[2] = (int)((r / bg.nb[1]) * BIN_EDGE);
+  };
   int stage = 0;
   int64_t b = blockIdx.x;
-  if (count(b) > 0) load_bin_tile<F>(g, bg, b, tiles[0]);
+  int og[3];
+  if (count(b) > 0) {
+    origin(b, og);
+    load_bin_tile<F>(g, og, tiles[0]);
+  }
   cp_async_commit();
   for (; b < nbins; b += gridDim.x) {
     const int64_t bn = b + gridDim.x;
-    if (count(bn) > 0) load_bin_tile<F>(g, bg, bn, tiles[stage ^ 1]);
+    if (count(bn) > 0) {
+      origin(bn, og);
+      load_bin_tile<F>(g, og, tiles[stage ^ 1]);
+    }
     cp_async_commit();
-    const int64_t nb = count(b);
-    if (nb > 0 && threadIdx.x < 32) bin_sched(w.hist, b, sc);
+    const uint32_t t0 = begin(b), t1 = t0 + count(b);
     cp_async_wait1();
     __syncthreads();
-    if (nb > 0) {
-      int64_t og[3];
-      bin_origin(b, bg, og);
+    if (t1 > t0) {
+      origin(b, og);
       // the next record is loaded while this one is evaluated
       QRec<float> rnext;
-      if ((int64_t)threadIdx.x < nb) rnext = recs[sched_record(sc, threadIdx.x)];
-      for (int64_t t = threadIdx.x; t < nb; t += blockDim.x) {
+      if (t0 + threadIdx.x < t1) rnext = recs[t0 + threadIdx.x];
+      for (uint32_t t = t0 + threadIdx.x; t < t1; t += BINC_THREADS) {
         const QRec<float> r = rnext;
-        if (t + blockDim.x < nb) rnext = recs[sched_record(sc, (uint32_t)(t + blockDim.x))];
+        if (t + BINC_THREADS < t1) rnext = recs[t + BINC_THREADS];
         int64_t c[3];
         unpack_cell<3>(r.cell, c);
-        const int base = (int)(((c[2] - og[2]) * TILE_EDGE + (c[1] - og[1])) * TILE_EDGE + (c[0] - og[0]));
+        const int bi = (((int)c[2] - og[2]) * TILE_EDGE + ((int)c[1] - og[1])) * TILE_EDGE + ((int)c[0] - og[0]);
         const float fr[3] = {r.f[0], r.f[1], r.f[2]};
         double val[F], grad[3] = {0.0, 0.0, 0.0};
         TileBlock3<F> blk;
@@ -562,7 +563,7 @@ __global__ void __launch_bounds__(BINC_THREADS, F == 4 ? 3 : (F == 3 ? 5 : 4)) e
         } else {
           blk.v = tiles[stage].v;
         }
-        blk.base = base;
+        blk.base = bi;
         if constexpr (F == 3)
           eval_otf3_vec_block(blk, fr, val);
         else if constexpr (F == 4)
@@ -572,11 +573,11 @@ __global__ void __launch_bounds__(BINC_THREADS, F == 4 ? 3 : (F == 3 ? 5 : 4)) e
         write_vals<3, F>(o, r.row, val, grad);
       }
     }
-    __syncthreads();  // this stage is refilled two bins later; the schedule is rebuilt
+    __syncthreads();  // this stage is refilled two bins later
     stage ^= 1;
   }
   // records that need no evaluation (out of volume, NaN, sentinel column)
-  for (int64_t t = sub_begin(bg.nsub) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
+  for (int64_t t = (int64_t)w.offs[bg.nsub] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
        t += (int64_t)gridDim.x * blockDim.x) {
     const QRec<float> r = recs[t];
     write_const<3, F>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
@@ -627,8 +628,13 @@ static bool launch_eval_binc(const arb_grid *g, const KParams &kp, const BinGeom
 // footprint of (hi, lo) pairs copied into shared memory with cp.async and
 // double-buffered, one thread per query evaluating eval_otf4_mixed_block on
 // the staged block.  From global memory each thread's 8-byte loads touch a
-// different 128-byte line per instruction and the kernel was L1-bound; shared
-// memory serves a warp's 32 scattered 8-byte loads in a few wavefronts.
+// different 128-byte line per instruction and the kernel was L1-bound.
+// Bank order: an 8-byte shared load is served half-warp by half-warp, 16
+// slots of 8 bytes per wavefront, and point (i, j, k, l) of the block of a
+// cell of class c (bank_class4) lies in slot (c + i + 7 j + k + 7 l + const)
+// mod 16; placement writes each bin's queries round robin over its 16
+// classes, so in every level with all 16 classes a half-warp's 16 loads hit
+// 16 distinct slots: one wavefront, where 16 random queries need about three.
 constexpr int BIN4_EDGE = 4;
 constexpr int TILE4_EDGE = BIN4_EDGE + 3;
 constexpr int TILE4_PTS = TILE4_EDGE * TILE4_EDGE * TILE4_EDGE * TILE4_EDGE;
@@ -687,16 +693,18 @@ __global__ void __launch_bounds__(BIN4_THREADS) eval_bin4_kernel(arb_grid g, KPa
   const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
   int stage = 0;
   int64_t b = blockIdx.x;
-  // after placement hist[b] is the end of bin b; bins with no query need no copy
-  auto bin_begin = [&](int64_t bb) { return bb > 0 ? (int64_t)w.hist[bb - 1] : (int64_t)0; };
-  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.hist[bb] - bin_begin(bb) : 0; };
+  // bin b holds records [offs[b << cls], offs[(b + 1) << cls]) (its class
+  // sub-bins, in the bin's bank schedule); bins with no query need no copy
+  const int cls = bg.cls;
+  auto bin_begin = [&](int64_t bb) { return (int64_t)w.offs[bb << cls]; };
+  auto count = [&](int64_t bb) { return bb < nbins ? (int64_t)w.offs[(bb + 1) << cls] - bin_begin(bb) : 0; };
   if (count(b) > 0) load_bin_tile4(g, bg, b, tiles[0]);
   cp_async_commit();
   for (; b < nbins; b += gridDim.x) {
     const int64_t bn = b + gridDim.x;
     if (count(bn) > 0) load_bin_tile4(g, bg, bn, tiles[stage ^ 1]);
     cp_async_commit();
-    const int64_t t0 = bin_begin(b), t1 = w.hist[b];
+    const int64_t t0 = bin_begin(b), t1 = w.offs[(b + 1) << cls];
     cp_async_wait1();
     __syncthreads();
     if (t1 > t0) {
@@ -721,7 +729,7 @@ __global__ void __launch_bounds__(BIN4_THREADS) eval_bin4_kernel(arb_grid g, KPa
     stage ^= 1;
   }
   // records that need no evaluation (out of volume, NaN, sentinel column)
-  for (int64_t t = bin_begin(nbins) + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
+  for (int64_t t = (int64_t)w.offs[bg.nsub] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq;
        t += (int64_t)gridDim.x * blockDim.x) {
     const QRec<float> r = recs[t];
     write_const<4, 1>(o, r.row, (r.cell & 1ULL) && !g.sentinel_nan ? 0.0 : qnan());
@@ -764,7 +772,7 @@ static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, 
   bin_count_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, wb, *out, status, w);
   const int64_t nh = bg.nsub + 1, nb = scan_blocks(nh);
   scan_part_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(w.hist, nh, w.part);
-  scan_apply_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(w.hist, nh, w.part);
+  scan_apply_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(w.hist, nh, w.part, w.offs);
   bin_place_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, w);
 }
 
