@@ -83,6 +83,16 @@ __host__ __device__ __forceinline__ uint32_t kmaj(int row, int k, int sbo) {
   return (uint32_t)((row >> 3) * sbo + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
+// The 1 KB-aligned start of a kernel's dynamic shared memory, reached by an
+// offset from the shared array itself: a pointer rounded through an integer
+// loses the shared address space and every access through it becomes a
+// generic load or store.
+template <typename T>
+__device__ __forceinline__ T &smem_aligned_1k(unsigned char *raw) {
+  const uint32_t a = tc::smem_u32(raw);
+  return *reinterpret_cast<T *>(raw + (((a + 1023u) & ~1023u) - a));
+}
+
 __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
   const __half2 h = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<const uint32_t *>(&h);
@@ -156,7 +166,7 @@ template <int F>
 __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__ CUtensorMap tmap, arb_grid g,
                                                          int64_t cell0, int64_t ncells, int32_t *status) {
   extern __shared__ unsigned char smem_raw[];
-  TcSmem &sm = *reinterpret_cast<TcSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  TcSmem &sm = smem_aligned_1k<TcSmem>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5;
   const int row = tid & (TM - 1), half = tid >> 7;
   const int64_t rows = ncells * F;
@@ -318,15 +328,12 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
   if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
 }
 
-// ---- full solves: the block gather fed by TMA -------------------------------
+// ---- full solves: warp-specialised, the block gather fed by TMA -------------
 // allCoeffs over every cell.  A tile holds C = 128 / F consecutive cells of one
 // x-row of cells (C x F rows of the table; the last tile of each row holds the
 // row's remaining cells).  Its grid footprint -- C + 3 points along x, 4
 // along y and z -- arrives in shared memory as 3D TMA boxes (zeros beyond the
-// grid), issued by one thread as soon as the previous tile's A operand is
-// built, so the load overlaps that tile's MMAs, epilogue and stores; the
-// gather then reads the footprint from shared memory (one float per (row,
-// point): a warp reads consecutive words) instead of global memory.
+// grid) and the gather reads the footprint from shared memory.
 // Footprint boxes (the TMA rule: x * element size a multiple of 16 bytes):
 //   F = 4: hi, 4 x 35 floats x 4 x 4 (x = 4 x0); lo of |B|, 40 x 4 x 4 floats
 //          from x = x0 rounded down to a multiple of 4 (needs nx % 4 == 0);
@@ -334,6 +341,26 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
 //   F = 1: (hi, lo) pairs as 8-byte elements, 132 x 4 x 4, x0 even (needs nx
 //          even: the row stride must be a multiple of 16 bytes).
 // Grids that miss these rules, and partial solves, take coef3_tc_kernel.
+//
+// One CTA per SM, three roles working on consecutive tiles at once, each
+// hand-off an mbarrier and every resource two-deep:
+//   producers (8 warps): the gather of a footprint into row deltas, the
+//       per-row scale, the three-part FP16 split into an A tile; thread t
+//       owns half t >> 7 (block layers 2h, 2h+1) of row t & 127;
+//   loader (one thread): the footprint boxes two tiles ahead and the 12
+//       MMAs of each tile into one of two TMEM accumulator stages
+//       (3 x 64 columns each, at columns 0 and 256);
+//   epilogue (4 warps): warp 8 + w reads TMEM lanes 32w..32w+31 (a whole
+//       row per thread), combines the three part sums, stages the rows
+//       128-byte swizzled and one thread writes them with two TMA stores.
+// So the split of one tile overlaps the MMAs of the previous one and the
+// epilogue and stores of the one before, where coef3_tc runs that chain in
+// order inside each CTA.  Every wait is bounded: a wait that runs out ORs
+// ARB_ERR_TIMEOUT into the status word and raises a shared abort flag that
+// ends every role's waits; the producer and epilogue warps leave their loops
+// together (a barrier that ORs their failures), and before the accumulator
+// columns are released and the CTA exits, the loader waits with the full
+// limit for its last MMAs and for any footprint load still in flight.
 namespace {
 template <int F>
 struct TmaShape;
@@ -351,231 +378,289 @@ struct TmaShape<1> {
 };
 constexpr int FP_BYTES = 17408;  // >= every shape's HBYTES + LBYTES, a multiple of 1 KB
 
-struct TcTmaSmem {
-  unsigned char a[A_BYTES];              // A tile, no-swizzle K-major (offset 0)
-  unsigned char b[B_BYTES];              // B = 8 A (offset 48 KB)
-  unsigned char stage[2][BOX_BYTES];     // output rows, 128-byte swizzled (offset 56 KB)
-  unsigned char fp[FP_BYTES];            // the tile's grid footprint (offset 88 KB)
-  float amax[2][TM];
-  uint64_t mbar;                         // MMA completion
-  uint64_t mbar_fp;                      // footprint arrival
+constexpr int WS_PROD = 256;                        // producer threads (warps 0-7)
+constexpr int WS_EPI = 128;                         // epilogue threads (warps 8-11)
+constexpr int WS_THREADS = WS_PROD + WS_EPI + 32;   // + warp 12: loader and MMA issue
+constexpr int WS_TMEM_COLS = 512;                   // two accumulator stages of 3 x 64 columns
+constexpr uint32_t BAR_PROD = 1, BAR_EPI = 2;       // named barriers of the producer and epilogue warps
+
+struct WsSmem {
+  unsigned char a[2][A_BYTES];             // A tiles, no-swizzle K-major (offset 0)
+  unsigned char stage[2][2][BOX_BYTES];    // output rows of a tile: two 128-byte swizzled boxes (1 KB aligned)
+  unsigned char b[B_BYTES];                // B = 8 A
+  unsigned char fp[2][FP_BYTES];           // footprints
+  float amax[2][2][TM];                    // [tile parity][half][row]
+  float mrhi[4][TM], mrlo[4][TM];          // each row's corner value (hi, lo), by tile mod 4
+  int mexp[4][TM];                         // each row's scale exponent
+  uint64_t fp_full[2], fp_empty[2], a_full[2], a_empty[2], acc_full[2], acc_empty[2];
   uint32_t tmem_base;
+  int abort;
 };
 static_assert(TmaShape<4>::HBYTES + TmaShape<4>::LBYTES <= FP_BYTES && TmaShape<3>::HBYTES <= FP_BYTES &&
                   TmaShape<1>::HBYTES <= FP_BYTES,
               "footprint buffer");
-static_assert(offsetof(TcTmaSmem, stage) % 1024 == 0 && offsetof(TcTmaSmem, fp) % 1024 == 0, "alignment");
+static_assert(offsetof(WsSmem, stage) % 1024 == 0 && offsetof(WsSmem, fp) % 1024 == 0 &&
+                  offsetof(WsSmem, b) % 1024 == 0,
+              "alignment");
+
+// Bounded wait that also gives up once another role has raised the abort
+// flag; a wait that runs out raises it.
+__device__ __forceinline__ bool ws_wait(WsSmem &sm, uint64_t *bar, uint32_t parity, uint32_t limit,
+                                        int32_t *status) {
+  for (uint32_t it = 0; it < limit; ++it) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    if (*(volatile int *)&sm.abort) return false;
+  }
+  set_status(status, ARB_ERR_TIMEOUT);
+  *(volatile int *)&sm.abort = 1;
+  return false;
+}
 }  // namespace
 
 template <int F>
-__global__ void __launch_bounds__(NT, 2) coef3_tma_kernel(const __grid_constant__ CUtensorMap tmap_full,
-                                                          const __grid_constant__ CUtensorMap tmap_part,
-                                                          const __grid_constant__ CUtensorMap tmap_hi,
-                                                          const __grid_constant__ CUtensorMap tmap_lo, arb_grid g,
-                                                          int32_t *status) {
+__global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_constant__ CUtensorMap tmap_full,
+                                                                  const __grid_constant__ CUtensorMap tmap_part,
+                                                                  const __grid_constant__ CUtensorMap tmap_hi,
+                                                                  const __grid_constant__ CUtensorMap tmap_lo,
+                                                                  arb_grid g, int32_t *status) {
   using S = TmaShape<F>;
   extern __shared__ unsigned char smem_raw[];
-  TcTmaSmem &sm = *reinterpret_cast<TcTmaSmem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int row = tid & (TM - 1), half = tid >> 7;
+  WsSmem &sm = smem_aligned_1k<WsSmem>(smem_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t ncx = g.n[0] - 3, ncy = g.n[1] - 3, ncz = g.n[2] - 3;
   const int64_t tpr = (ncx + S::C - 1) / S::C;          // tiles per x-row of cells
   const int rem = (int)(ncx - (tpr - 1) * S::C);         // cells in a row's last tile
   const int64_t ntiles = tpr * ncy * ncz;
-  const int cl = row / F, f = row % F;                   // this row's cell in the tile, and field
+  const int nloc = blockIdx.x < ntiles ? (int)((ntiles - 1 - blockIdx.x) / gridDim.x + 1) : 0;
 
-  for (int e = tid; e < 64 * 64; e += NT) {
+  for (int e = tid; e < 64 * 64; e += WS_THREADS) {
     const int n = e >> 6, k = e & 63;
     const float v = 8.f * kA1[n & 3][k & 3] * kA1[(n >> 2) & 3][(k >> 2) & 3] * kA1[n >> 4][k >> 4];
     *reinterpret_cast<__half *>(sm.b + kmaj(n, k, B_SBO)) = __float2half_rn(v);
   }
   if (warp == 0) {
-    tc::tmem_alloc(&sm.tmem_base, TMEM_COLS);
+    tc::tmem_alloc(&sm.tmem_base, WS_TMEM_COLS);
     tc::tmem_relinquish();
   }
-  // footprint boxes of one tile, on mbar_fp (issued by one thread)
-  auto issue_fp = [&](int64_t tile) {
-    const int64_t xr = tile / tpr;
-    const int x0 = (int)((tile - xr * tpr) * S::C);
-    const int y = (int)(xr % ncy), z = (int)(xr / ncy);
-    tc::mbar_arrive_expect_tx(&sm.mbar_fp, (uint32_t)(S::HBYTES + S::LBYTES));
-    if constexpr (F == 1) {
-      tc::tma_load_3d(sm.fp, &tmap_hi, x0 & ~1, y, z, &sm.mbar_fp);
-    } else {
-      tc::tma_load_3d(sm.fp, &tmap_hi, 4 * x0, y, z, &sm.mbar_fp);
-      if constexpr (F == 4) tc::tma_load_3d(sm.fp + S::HBYTES, &tmap_lo, x0 & ~3, y, z, &sm.mbar_fp);
-    }
-  };
   if (tid == 0) {
-    tc::mbar_init(&sm.mbar, 1);
-    tc::mbar_init(&sm.mbar_fp, 1);
+    for (int s = 0; s < 2; ++s) {
+      tc::mbar_init(&sm.fp_full[s], 1);
+      tc::mbar_init(&sm.fp_empty[s], WS_PROD / 32);
+      tc::mbar_init(&sm.a_full[s], WS_PROD / 32);
+      tc::mbar_init(&sm.a_empty[s], 1);
+      tc::mbar_init(&sm.acc_full[s], 1);
+      tc::mbar_init(&sm.acc_empty[s], WS_EPI / 32);
+    }
+    sm.abort = 0;
     tc::fence_mbar_init();
   }
   tc::fence_proxy_async_smem();
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
-  if (tid == 0 && blockIdx.x < ntiles) issue_fp(blockIdx.x);
-  bool fp_pending = blockIdx.x < ntiles;
   const uint32_t tmem = sm.tmem_base;
-  const uint32_t idesc = tc::idesc_f16(0u, 128u, 64u);
-  const uint32_t a_base = tc::smem_u32(sm.a), b_base = tc::smem_u32(sm.b);
-  const uint32_t t_row = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(half * 32);
-  unsigned char *st_row = sm.stage[half] + row * 128;
-  uint32_t parity = 0, pfp = 0;
-  bool timed_out = false, fp_timed_out = false;
-  const uint32_t mma_wait_limit = g_mma_wait_limit;
+  auto tile_of = [&](int k) { return (int64_t)blockIdx.x + (int64_t)k * gridDim.x; };
 
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t xr = tile / tpr;
-    const int64_t kx = tile - xr * tpr;
-    const int x0 = (int)(kx * S::C);
-    const int cnt = kx == tpr - 1 ? rem : S::C;
-    const int64_t row0 = (xr * ncx + x0) * F;             // first table row of the tile
-    // ---- the footprint has landed ------------------------------------------
-    const bool fok = tc::mbar_wait_bounded(&sm.mbar_fp, pfp, WAIT_LIMIT);
-    pfp ^= 1u;
-    if (!fok) set_status(status, ARB_ERR_TIMEOUT);
-    if (__syncthreads_or(!fok)) {
-      fp_timed_out = true;
-      break;
-    }
-    fp_pending = false;
-    // ---- gather block layers oz = 2h, 2h+1 as deltas to the corner ---------
-    float rhi = 0.f, rlo = 0.f, d[32], amax = 0.f;
-    if (cl < cnt) {
-      const float *fh = reinterpret_cast<const float *>(sm.fp);
-      auto pt = [&](int ox, int oy, int oz, float &h, float &l) {
-        const int P = (oz * 4 + oy) * S::HX + cl + ox;
-        if constexpr (F == 1) {
-          const float2 v = reinterpret_cast<const float2 *>(sm.fp)[P + (x0 & 1)];
-          h = v.x;
-          l = v.y;
-        } else {
-          h = fh[4 * P + f];
-          l = 0.f;
-          if constexpr (F == 4) {
-            if (f == 3)
-              l = reinterpret_cast<const float *>(sm.fp + S::HBYTES)[(oz * 4 + oy) * S::LX + cl + ox + (x0 & 3)];
-          }
-        }
-      };
-      pt(1, 1, 1, rhi, rlo);
-#pragma unroll
-      for (int oz = 0; oz < 2; ++oz)
-#pragma unroll
-        for (int oy = 0; oy < 4; ++oy)
-#pragma unroll
-          for (int ox = 0; ox < 4; ox += 2) {
-            float h0, l0, h1, l1;
-            pt(ox, oy, 2 * half + oz, h0, l0);
-            pt(ox + 1, oy, 2 * half + oz, h1, l1);
-            const float2 dd = fadd2(fsub2(make_float2(h0, h1), make_float2(rhi, rhi)),
-                                    fsub2(make_float2(l0, l1), make_float2(rlo, rlo)));
-            d[oz * 16 + oy * 4 + ox] = dd.x;
-            d[oz * 16 + oy * 4 + ox + 1] = dd.y;
-            amax = fmaxf(amax, fmaxf(fabsf(dd.x), fabsf(dd.y)));
-          }
-    } else {
+  if (warp < WS_PROD / 32) {
+    // ---- producers: gather, scale, split -----------------------------------
+    const int row = tid & (TM - 1), half = tid >> 7;
+    const int cl = row / F, f = row % F;                 // this row's cell in the tile, and field
+    bool fail = false;
+    for (int k = 0; k < nloc; ++k) {
+      const int s = k & 1;
+      const uint32_t ph = (uint32_t)(k >> 1) & 1u;
+      const int64_t tile = tile_of(k);
+      const int64_t xr = tile / tpr;
+      const int x0 = (int)((tile - xr * tpr) * S::C);
+      const int cnt = tile - xr * tpr == tpr - 1 ? rem : S::C;
+      bool ok = !fail && ws_wait(sm, &sm.fp_full[s], ph, WAIT_LIMIT, status);
+      float rhi = 0.f, rlo = 0.f, d[32], amax = 0.f;
 #pragma unroll
       for (int j = 0; j < 32; ++j) d[j] = 0.f;
-    }
-    sm.amax[half][row] = amax;
-    __syncthreads();
-    const int E = scale_exp(fmaxf(amax, sm.amax[half ^ 1][row]));
-    const float c10 = __uint_as_float((uint32_t)(137 - E) << 23);    // 2^(10 - E)
-    // ---- three-part FP16 split into the A tile ------------------------------
+      if (ok && cl < cnt) {
+        const unsigned char *fpb = sm.fp[s];
+        const float *fh = reinterpret_cast<const float *>(fpb);
+        auto pt = [&](int ox, int oy, int oz, float &h, float &l) {
+          const int P = (oz * 4 + oy) * S::HX + cl + ox;
+          if constexpr (F == 1) {
+            const float2 v = reinterpret_cast<const float2 *>(fpb)[P + (x0 & 1)];
+            h = v.x;
+            l = v.y;
+          } else {
+            h = fh[4 * P + f];
+            l = 0.f;
+            if constexpr (F == 4) {
+              if (f == 3)
+                l = reinterpret_cast<const float *>(fpb + S::HBYTES)[(oz * 4 + oy) * S::LX + cl + ox + (x0 & 3)];
+            }
+          }
+        };
+        pt(1, 1, 1, rhi, rlo);
 #pragma unroll
-    for (int ch = 0; ch < 4; ++ch) {
-      uint32_t w0[4], w1[4], w2[4];
+        for (int oz = 0; oz < 2; ++oz)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        float2 h0, h1, h2;
-        split3_pair(fmul2(make_float2(d[ch * 8 + v * 2], d[ch * 8 + v * 2 + 1]), make_float2(c10, c10)), kRound1,
-                    4194304.0f, h0, h1, h2);
-        w0[v] = pack_h2(h0.x, h0.y);
-        w1[v] = pack_h2(h1.x, h1.y);
-        w2[v] = pack_h2(h2.x, h2.y);
+          for (int oy = 0; oy < 4; ++oy)
+#pragma unroll
+            for (int ox = 0; ox < 4; ox += 2) {
+              float h0, l0, h1, l1;
+              pt(ox, oy, 2 * half + oz, h0, l0);
+              pt(ox + 1, oy, 2 * half + oz, h1, l1);
+              const float2 dd = fadd2(fsub2(make_float2(h0, h1), make_float2(rhi, rhi)),
+                                      fsub2(make_float2(l0, l1), make_float2(rlo, rlo)));
+              d[oz * 16 + oy * 4 + ox] = dd.x;
+              d[oz * 16 + oy * 4 + ox + 1] = dd.y;
+              amax = fmaxf(amax, fmaxf(fabsf(dd.x), fabsf(dd.y)));
+            }
       }
-      const int k = half * 32 + ch * 8;
-      *reinterpret_cast<uint4 *>(sm.a + kmaj(row, k, A_SBO)) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
-      *reinterpret_cast<uint4 *>(sm.a + kmaj(row, KP + k, A_SBO)) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
-      *reinterpret_cast<uint4 *>(sm.a + kmaj(row, 2 * KP + k, A_SBO)) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+      __syncwarp();
+      if (ok && lane == 0) tc::mbar_arrive(&sm.fp_empty[s]);  // this warp has read the footprint
+      sm.amax[s][half][row] = amax;
+      if (tc::named_bar_or(BAR_PROD, WS_PROD, !ok)) break;   // every producer leaves together
+      const int E = scale_exp(fmaxf(amax, sm.amax[s][half ^ 1][row]));
+      const float c10 = __uint_as_float((uint32_t)(137 - E) << 23);    // 2^(10 - E)
+      ok = k < 2 || ws_wait(sm, &sm.a_empty[s], ph ^ 1u, WAIT_LIMIT, status);  // the MMAs of tile k - 2 are done
+      if (ok) {
+        unsigned char *at = sm.a[s];
+#pragma unroll
+        for (int ch = 0; ch < 4; ++ch) {
+          uint32_t w0[4], w1[4], w2[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            float2 h0, h1, h2;
+            split3_pair(fmul2(make_float2(d[ch * 8 + v * 2], d[ch * 8 + v * 2 + 1]), make_float2(c10, c10)),
+                        kRound1, 4194304.0f, h0, h1, h2);
+            w0[v] = pack_h2(h0.x, h0.y);
+            w1[v] = pack_h2(h1.x, h1.y);
+            w2[v] = pack_h2(h2.x, h2.y);
+          }
+          const int kk = half * 32 + ch * 8;
+          *reinterpret_cast<uint4 *>(at + kmaj(row, kk, A_SBO)) = make_uint4(w0[0], w0[1], w0[2], w0[3]);
+          *reinterpret_cast<uint4 *>(at + kmaj(row, KP + kk, A_SBO)) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+          *reinterpret_cast<uint4 *>(at + kmaj(row, 2 * KP + kk, A_SBO)) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+        }
+        if (half == 0) {
+          sm.mrhi[k & 3][row] = rhi;
+          sm.mrlo[k & 3][row] = rlo;
+          sm.mexp[k & 3][row] = E;
+        }
+        tc::fence_proxy_async_smem();  // the A tile is visible to the tensor core
+      }
+      __syncwarp();
+      if (ok && lane == 0) tc::mbar_arrive(&sm.a_full[s]);
+      fail = !ok;
     }
-    tc::fence_proxy_async_smem();
-    tc::tc_fence_before();
-    if (tid == 0) tc::bulk_wait_read0();  // the previous tile's stores have read the staging buffer
-    __syncthreads();
-    // every thread has read the footprint: the next tile's boxes may land
-    const int64_t next = tile + gridDim.x;
-    if (next < ntiles) {
-      if (tid == 0) issue_fp(next);
-      fp_pending = true;
-    }
-    // ---- 12 MMAs of 128 x 64 x 16: part p accumulates into columns 64p -----
-    if (tid == 0) {
+  } else if (warp < (WS_PROD + WS_EPI) / 32) {
+    // ---- epilogue: TMEM -> table rows ----------------------------------------
+    const int ew = warp - WS_PROD / 32;                  // TMEM lanes 32 ew .. 32 ew + 31
+    const int row = ew * 32 + lane;
+    const bool leader = tid == WS_PROD;                  // issues the TMA stores
+    const uint32_t mma_wait_limit = g_mma_wait_limit;
+    bool fail = false;
+    for (int k = 0; k < nloc; ++k) {
+      const int s = k & 1;
+      const uint32_t ph = (uint32_t)(k >> 1) & 1u;
+      const bool ok = !fail && ws_wait(sm, &sm.acc_full[s], ph, mma_wait_limit, status);
       tc::tc_fence_after();
+      if (leader) tc::bulk_wait_read1();                  // the stores of tile k - 2 have read stage[s]
+      if (tc::named_bar_or(BAR_EPI, WS_EPI, !ok)) break;
+      const int64_t tile = tile_of(k);
+      const int64_t xr = tile / tpr;
+      const int64_t kx = tile - xr * tpr;
+      const int cnt = kx == tpr - 1 ? rem : S::C;
+      const int64_t row0 = (xr * ncx + kx * S::C) * F;   // first table row of the tile
+      const int E = sm.mexp[k & 3][row];
+      const float rhi = sm.mrhi[k & 3][row], rlo = sm.mrlo[k & 3][row];
+      const float so = __uint_as_float((uint32_t)(E - 13 + 127) << 23);   // 2^(E - 13)
+      const uint32_t t_row = tmem + ((uint32_t)(ew * 32) << 16) + (uint32_t)(256 * s);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {                      // coefficients 16q .. 16q + 15
+        float p0[16], p1[16], p2[16];
+        tc::tmem_ld16(t_row + (uint32_t)(16 * q), p0);
+        tc::tmem_ld16(t_row + (uint32_t)(64 + 16 * q), p1);
+        tc::tmem_ld16(t_row + (uint32_t)(128 + 16 * q), p2);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) p0[j] = __fmul_rn(__fadd_rn(p0[j], __fmaf_rn(p2[j], 0x1p-22f, p1[j])), so);
+        if (q == 0) p0[0] = rhi + (rlo + p0[0]);
+        unsigned char *st_row = sm.stage[s][q >> 1] + row * 128;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int j = (q & 1) * 4 + c;                 // 16-byte chunk of the 128-byte row
+          *reinterpret_cast<float4 *>(st_row + 16 * (j ^ (row & 7))) =
+              make_float4(p0[4 * c], p0[4 * c + 1], p0[4 * c + 2], p0[4 * c + 3]);
+        }
+      }
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&sm.acc_empty[s]);  // this warp has read the accumulator
+      tc::fence_proxy_async_smem();
+      tc::named_bar_sync(BAR_EPI, WS_EPI);
+      if (leader) {
+        const CUtensorMap *tm = cnt == S::C ? &tmap_full : &tmap_part;
+        tc::tma_store_2d(tm, sm.stage[s][0], 0, (int32_t)row0);
+        tc::tma_store_2d(tm, sm.stage[s][1], 32, (int32_t)row0);
+        tc::bulk_commit();
+      }
+    }
+    if (leader) tc::bulk_wait0();
+  } else if (lane == 0) {
+    // ---- loader: footprints two tiles ahead, MMAs --------------------------
+    auto issue_fp = [&](int k) {
+      const int s = k & 1;
+      const int64_t tile = tile_of(k);
+      const int64_t xr = tile / tpr;
+      const int x0 = (int)((tile - xr * tpr) * S::C);
+      const int y = (int)(xr % ncy), z = (int)(xr / ncy);
+      tc::mbar_arrive_expect_tx(&sm.fp_full[s], (uint32_t)(S::HBYTES + S::LBYTES));
+      if constexpr (F == 1) {
+        tc::tma_load_3d(sm.fp[s], &tmap_hi, x0 & ~1, y, z, &sm.fp_full[s]);
+      } else {
+        tc::tma_load_3d(sm.fp[s], &tmap_hi, 4 * x0, y, z, &sm.fp_full[s]);
+        if constexpr (F == 4) tc::tma_load_3d(sm.fp[s] + S::HBYTES, &tmap_lo, x0 & ~3, y, z, &sm.fp_full[s]);
+      }
+    };
+    int fp_issued = 0, mma_done = 0;
+    for (; fp_issued < nloc && fp_issued < 2; ++fp_issued) issue_fp(fp_issued);
+    const uint32_t idesc = tc::idesc_f16(0u, 128u, 64u);
+    const uint32_t b_base = tc::smem_u32(sm.b);
+    for (int k = 0; k < nloc; ++k) {
+      const int s = k & 1;
+      const uint32_t ph = (uint32_t)(k >> 1) & 1u;
+      if (!ws_wait(sm, &sm.a_full[s], ph, WAIT_LIMIT, status)) break;
+      if (k >= 2 && !ws_wait(sm, &sm.acc_empty[s], ph ^ 1u, WAIT_LIMIT, status)) break;
+      tc::tc_fence_after();
+      const uint32_t a_base = tc::smem_u32(sm.a[s]);
 #pragma unroll
       for (int p = 0; p < PARTS; ++p)
 #pragma unroll
         for (int kc = 0; kc < 4; ++kc) {
-          const int s = p * 4 + kc;
-          const uint64_t ad = tc::smem_desc(a_base + (uint32_t)(2 * s) * 128u, 128u, (uint32_t)A_SBO);
+          const int c = p * 4 + kc;
+          const uint64_t ad = tc::smem_desc(a_base + (uint32_t)(2 * c) * 128u, 128u, (uint32_t)A_SBO);
           const uint64_t bd = tc::smem_desc(b_base + (uint32_t)(2 * kc) * 128u, 128u, (uint32_t)B_SBO);
-          tc::mma_f16(tmem + (uint32_t)(64 * p), ad, bd, idesc, kc > 0 ? 1u : 0u);
+          tc::mma_f16(tmem + (uint32_t)(256 * s + 64 * p), ad, bd, idesc, kc > 0 ? 1u : 0u);
         }
-      tc::mma_commit(&sm.mbar);
+      tc::mma_commit(&sm.a_empty[s]);    // A[s] may be rewritten
+      tc::mma_commit(&sm.acc_full[s]);   // the accumulator is ready
+      mma_done = k + 1;
+      if (k + 2 < nloc) {                // the producers have read fp[s] (before they finished A[s])
+        if (!ws_wait(sm, &sm.fp_empty[s], ph, WAIT_LIMIT, status)) break;
+        issue_fp(k + 2);
+        fp_issued = k + 3;
+      }
     }
-    const bool ok = tc::mbar_wait_bounded(&sm.mbar, parity, mma_wait_limit);
-    parity ^= 1u;
-    if (!ok) set_status(status, ARB_ERR_TIMEOUT);
-    tc::tc_fence_after();
-    if (__syncthreads_or(!ok)) {
-      timed_out = true;
-      break;
+    // nothing in flight when the columns are released and the CTA exits: the
+    // last MMAs (they complete in order) and the footprint loads not yet waited on
+    if (mma_done > 0) {
+      const int kl = mma_done - 1;
+      (void)tc::mbar_wait_bounded(&sm.acc_full[kl & 1], (uint32_t)(kl >> 1) & 1u, WAIT_LIMIT);
     }
-    // ---- epilogue: combine the part sums, stage swizzled, TMA-store --------
-    float a[32], t[32];
-    tc::tmem_ld16(t_row + 128u, t);
-    tc::tmem_ld16(t_row + 144u, t + 16);
-    tc::tmem_ld16(t_row + 64u, a);
-    tc::tmem_ld16(t_row + 80u, a + 16);
-    tc::tmem_wait_ld();
-#pragma unroll
-    for (int j = 0; j < 32; ++j) t[j] = __fmaf_rn(t[j], 0x1p-22f, a[j]);
-    tc::tmem_ld16(t_row, a);
-    tc::tmem_ld16(t_row + 16u, a + 16);
-    tc::tmem_wait_ld();
-    const float so = __uint_as_float((uint32_t)(E - 13 + 127) << 23);   // 2^(E - 13)
-#pragma unroll
-    for (int j = 0; j < 32; ++j) a[j] = __fmul_rn(__fadd_rn(a[j], t[j]), so);
-    if (half == 0) a[0] = rhi + (rlo + a[0]);
-#pragma unroll
-    for (int q = 0; q < 8; ++q)
-      *reinterpret_cast<float4 *>(st_row + 16 * (q ^ (row & 7))) =
-          make_float4(a[4 * q], a[4 * q + 1], a[4 * q + 2], a[4 * q + 3]);
-    tc::fence_proxy_async_smem();
-    tc::tc_fence_before();
-    __syncthreads();
-    if (tid == 0) {
-      const CUtensorMap *tm = cnt == S::C ? &tmap_full : &tmap_part;
-      tc::tma_store_2d(tm, sm.stage[0], 0, (int32_t)row0);
-      tc::tma_store_2d(tm, sm.stage[1], 32, (int32_t)row0);
-      tc::bulk_commit();
-    }
+    for (int kf = fp_issued - 2 > 0 ? fp_issued - 2 : 0; kf < fp_issued; ++kf)
+      (void)tc::mbar_wait_bounded(&sm.fp_full[kf & 1], (uint32_t)(kf >> 1) & 1u, WAIT_LIMIT);
   }
-  if (tid == 0) tc::bulk_wait0();
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
-  // after a timed-out wait: one more bounded wait for the MMAs in flight
-  // before the accumulator columns are released, and for a footprint load
-  // still in flight before the CTA's shared memory is given back
-  if (timed_out) (void)tc::mbar_wait_bounded(&sm.mbar, parity ^ 1u, WAIT_LIMIT);
-  if ((timed_out || fp_timed_out) && fp_pending)
-    (void)tc::mbar_wait_bounded(&sm.mbar_fp, fp_timed_out ? pfp ^ 1u : pfp, WAIT_LIMIT);
-  __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+  if (warp == 0) tc::tmem_dealloc(tmem, WS_TMEM_COLS);
 }
 
 static int num_sms() {
@@ -623,7 +708,7 @@ static int coef3_solve_tma(const arb_grid *g, float *table, int32_t *status, cud
   const int64_t ncx = nx - 3;
   const int64_t tpr = (ncx + S::C - 1) / S::C;
   const int rem = (int)(ncx - (tpr - 1) * S::C);
-  const size_t smem = sizeof(TcTmaSmem) + 1024;
+  const size_t smem = sizeof(WsSmem) + 1024;
   static std::once_flag once[MAX_DEVICES];
   static int per_sm_dev[MAX_DEVICES];
   static cudaError_t attr_err[MAX_DEVICES];
@@ -633,12 +718,8 @@ static int coef3_solve_tma(const arb_grid *g, float *table, int32_t *status, cud
     attr_err[dev] = cudaFuncSetAttribute(coef3_tma_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (attr_err[dev] == cudaSuccess)
       attr_err[dev] = cudaFuncSetAttribute(coef3_tma_kernel<F>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    // CTAs per SM from the shared memory (1 KB reserved per CTA); TMEM
-    // (2 x 256 columns) allows two
-    int smem_sm = 0;
-    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    const int n = (int)(smem_sm / (int64_t)(smem + 1024));
-    per_sm_dev[dev] = n < 1 ? 1 : (n > 2 ? 2 : n);
+    // one CTA per SM (its 512 TMEM columns are the whole SM's)
+    per_sm_dev[dev] = 1;
   });
   if (attr_err[dev] != cudaSuccess) return ARB_ERR_CUDA;
   const cuuint32_t estr[3] = {1, 1, 1};
@@ -689,7 +770,7 @@ static int coef3_solve_tma(const arb_grid *g, float *table, int32_t *status, cud
   int64_t grid = (int64_t)num_sms() * per_sm_dev[dev];
   if (grid > tiles) grid = tiles;
   if (grid < 1) return ARB_OK;
-  coef3_tma_kernel<F><<<(unsigned)grid, NT, smem, s>>>(tm_full, tm_part, tm_hi, tm_lo, *g, status);
+  coef3_tma_kernel<F><<<(unsigned)grid, WS_THREADS, smem, s>>>(tm_full, tm_part, tm_hi, tm_lo, *g, status);
   return launch_status();
 }
 
@@ -818,7 +899,7 @@ template <int F>
 __global__ void __launch_bounds__(T4_NT, 1) coef4_tc_kernel(const __grid_constant__ CUtensorMap tmap, arb_grid g,
                                                             int64_t cell0, int64_t ncells, int32_t *status) {
   extern __shared__ unsigned char smem_raw[];
-  Tc4Smem &sm = *reinterpret_cast<Tc4Smem *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  Tc4Smem &sm = smem_aligned_1k<Tc4Smem>(smem_raw);
   const int tid = threadIdx.x, warp = tid >> 5;
   const int row = tid & (T4_M - 1), half = tid >> 7;
   const int64_t rows = ncells * F;

@@ -294,18 +294,22 @@ def test_tensor_core_table_matches_fp64(mode):
     assert not a[:, 3].any()      # unsolved cells stay zero
 
 
+@pytest.mark.parametrize("shape", [(23, 19, 21), (136, 11, 9)])
 @pytest.mark.parametrize("mode", ["both", "vector", "norm", None])
-def test_tensor_core_table_exact_from_deltas(mode):
+def test_tensor_core_table_exact_from_deltas(mode, shape):
     """The tcgen05 solve adds no accumulation error: every float32
     coefficient equals alpha = A d computed exactly from the kernel's float32
     deltas d = (hi - hi_ref) + (lo - lo_ref), up to its own float32 rounding
     and the fixed-point truncation of d (2^-33 of the row's power-of-two
     scale, times the largest row abs-sum 216 of A).  Coarse, fast-varying
-    dipole field; scalar field too."""
+    dipole field; scalar field too.  The 23-point x axis takes the gather
+    kernel (coef3_tc); the 136-point one (a multiple of 4) the warp-
+    specialised TMA kernel, with full and partial tiles for every field
+    count (133 cells per x-row: 4 x 32 + 5, 3 x 42 + 7, 128 + 5)."""
     tricubic, _ = _mods()
     from arbinterp_gb300 import synth
     from oracle.arb_oracle import OracleTricubic
-    f = synth.dipole_field3(n=(23, 19, 21), seed=8).numpy()
+    f = synth.dipole_field3(n=shape, seed=8).numpy()
     if mode is None:
         f = np.hstack([f[:, :3], f[:, 3:4] * f[:, 4:5] + 3.0])
     kw = {} if mode is None else {"mode": mode}
