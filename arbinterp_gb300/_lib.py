@@ -56,6 +56,10 @@ SIGNATURES = {
                                      _P, _P, _P, _P, _P, _P]),
     "arb_ingest_ordered": (C.c_int, [_P, _I32, _I64, _I32, _I32, _I32, _I64, _P, _P, _P, _P, _P, _P, C.c_size_t,
                                      _P, _P]),
+    "arb_ingest_ordered_probe": (C.c_int, [_P, _I32, _I64, _I32, _I32, _I32, _I64, _P, _P, _P, C.c_size_t,
+                                           _P, _P]),
+    "arb_ingest_ordered_fill": (C.c_int, [_P, _I32, _I64, _I32, _I32, _I32, _I64, _P, _P, C.c_size_t, _P, _P,
+                                          _P, _P, _P]),
     "arb_ingest_summary": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P]),
     "arb_fd_planes": (C.c_int, [C.POINTER(ArbGrid), _P, _P]),
     "arb_coef_solve": (C.c_int, [C.POINTER(ArbGrid), _I32, _I64, _I64, _P, _P, _P]),

@@ -109,6 +109,7 @@ def _candidates(interp):
 def _measure(interp, qd, nq, qs):
     """Time each candidate (one warm-up, two timed runs) and return the fastest.
     A table candidate is charged its build when the table does not exist."""
+    interp._settle()       # the grid is written and checked before candidates are timed on it
     best, best_t = None, float("inf")
     had_table = interp._table_complete
     build_t = 0.0

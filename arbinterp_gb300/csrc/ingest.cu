@@ -690,25 +690,32 @@ extern "C" int arb_ingest_scatter(const void *field, int32_t field_is_f32, int64
   return launch_status();
 }
 
-extern "C" int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
-                                  int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,
-                                  int64_t *axis_count, double *grid64, float *grid32, double *raw_out,
-                                  void *work, size_t work_bytes, int32_t *status, arb_stream_t stream) {
-  if (!field || !axis_out || !axis_count || (!grid64 && !grid32) || !work || !status) return ARB_ERR_INVALID;
+static int ordered_args_ok(const void *field, int64_t npts, int32_t ncol, int32_t dim, int32_t kind,
+                           int64_t axis_cap, size_t work_bytes) {
+  if (!field) return ARB_ERR_INVALID;
   if ((dim != 3 && dim != 4) || npts <= 0 || axis_cap <= 0 || axis_cap > ARB_MAX_AXIS_CAP ||
       work_bytes < arb_ingest_axes_work_bytes(dim))
     return ARB_ERR_INVALID;
   const int nval = ncol - dim;
   if (kind == ARB_KIND_SCALAR ? nval != 1 : nval != 3) return ARB_ERR_INVALID;
   if (npts >= (int64_t)0xffffffffLL) return ARB_ERR_UNSUPPORTED;
-  cudaStream_t s = (cudaStream_t)stream;
-  OrderWork *w = (OrderWork *)work;
+  return ARB_OK;
+}
+
+static void launch_ordered_probe(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol, int32_t dim,
+                                 int64_t axis_cap, double *axis_out, int64_t *axis_count, OrderWork *w,
+                                 int32_t *status, cudaStream_t s) {
   if (field_is_f32)
     ordered_probe_kernel<float><<<1, 256, 0, s>>>((const float *)field, npts, ncol, dim, axis_cap, axis_out,
                                                   axis_count, w, status);
   else
     ordered_probe_kernel<double><<<1, 256, 0, s>>>((const double *)field, npts, ncol, dim, axis_cap, axis_out,
                                                    axis_count, w, status);
+}
+
+static int launch_ordered_fill(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol, int32_t dim,
+                               int32_t kind, int64_t axis_cap, const double *axis_out, const OrderWork *w,
+                               double *grid64, float *grid32, double *raw_out, int32_t *status, cudaStream_t s) {
   const int T = 256;
   const int B = grid_blocks(npts, T);
 #define ARB_OGATHER(TF, K)                                                                                 \
@@ -736,7 +743,46 @@ extern "C" int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64
   }
 #undef ARB_OGATHER_KIND
 #undef ARB_OGATHER
+  return ARB_OK;
+}
+
+extern "C" int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                                  int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,
+                                  int64_t *axis_count, double *grid64, float *grid32, double *raw_out,
+                                  void *work, size_t work_bytes, int32_t *status, arb_stream_t stream) {
+  if (!axis_out || !axis_count || (!grid64 && !grid32) || !work || !status) return ARB_ERR_INVALID;
+  int rc = ordered_args_ok(field, npts, ncol, dim, kind, axis_cap, work_bytes);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  OrderWork *w = (OrderWork *)work;
+  launch_ordered_probe(field, field_is_f32, npts, ncol, dim, axis_cap, axis_out, axis_count, w, status, s);
+  rc = launch_ordered_fill(field, field_is_f32, npts, ncol, dim, kind, axis_cap, axis_out, w, grid64, grid32,
+                           raw_out, status, s);
+  return rc ? rc : launch_status();
+}
+
+extern "C" int arb_ingest_ordered_probe(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                                        int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,
+                                        int64_t *axis_count, void *work, size_t work_bytes, int32_t *status,
+                                        arb_stream_t stream) {
+  if (!axis_out || !axis_count || !work || !status) return ARB_ERR_INVALID;
+  const int rc = ordered_args_ok(field, npts, ncol, dim, kind, axis_cap, work_bytes);
+  if (rc) return rc;
+  launch_ordered_probe(field, field_is_f32, npts, ncol, dim, axis_cap, axis_out, axis_count, (OrderWork *)work,
+                       status, (cudaStream_t)stream);
   return launch_status();
+}
+
+extern "C" int arb_ingest_ordered_fill(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                                       int32_t dim, int32_t kind, int64_t axis_cap, const double *axis_out,
+                                       const void *work, size_t work_bytes, double *grid64, float *grid32,
+                                       double *raw_out, int32_t *status, arb_stream_t stream) {
+  if (!axis_out || (!grid64 && !grid32) || !work || !status) return ARB_ERR_INVALID;
+  const int rc = ordered_args_ok(field, npts, ncol, dim, kind, axis_cap, work_bytes);
+  if (rc) return rc;
+  const int r2 = launch_ordered_fill(field, field_is_f32, npts, ncol, dim, kind, axis_cap, axis_out,
+                                     (const OrderWork *)work, grid64, grid32, raw_out, status, (cudaStream_t)stream);
+  return r2 ? r2 : launch_status();
 }
 
 __global__ void ingest_summary_kernel(const double *axes, int64_t cap, const int64_t *count, int dim,

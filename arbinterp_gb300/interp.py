@@ -221,51 +221,44 @@ class _Interpolant:
         ax64 = axes[: dim * cap].view(dim, cap)
         summ = torch.empty(17, dtype=torch.float64, device=dev)
 
-        def summary():
-            # status, axis counts and the axis samples the attributes need, in one copy
-            check(L.arb_ingest_summary(axes.data_ptr(), cap, counts.data_ptr(), dim, status.data_ptr(),
-                                       summ.data_ptr(), s), "arb_ingest_summary")
-            return summ.cpu().numpy()
-
+        self._status = status
+        self._fill_pending = False
+        self._fill_src = None
         done = False
         if _ORDERED_INGEST and npts < 0xFFFFFFFF:
-            # rows in meshgrid order (the common case): one pass, no sort
-            check(L.arb_ingest_ordered(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
-                                       counts.data_ptr(), _ptr(grid64), _ptr(grid32), _ptr(raw),
-                                       work.data_ptr(), wb, status.data_ptr(), s), "arb_ingest_ordered")
-            sm = summary()
+            # rows in meshgrid order (the common case): one pass, no sort.  The
+            # host waits for the single-block axis probe only (its summary
+            # arrives in pinned memory behind an event); the pass that writes
+            # the grid runs while the host sets up and the first query is
+            # queued, and its row check is read at the next synchronisation
+            # (_settle), before any result derived from the grid is returned.
+            check(L.arb_ingest_ordered_probe(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
+                                             counts.data_ptr(), work.data_ptr(), wb, status.data_ptr(), s),
+                  "arb_ingest_ordered_probe")
+            check(L.arb_ingest_summary(axes.data_ptr(), cap, counts.data_ptr(), dim, status.data_ptr(),
+                                       summ.data_ptr(), s), "arb_ingest_summary")
+            summ_h = torch.empty(17, dtype=torch.float64, pin_memory=True)
+            summ_h.copy_(summ, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record()
+            check(L.arb_ingest_ordered_fill(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
+                                            work.data_ptr(), wb, _ptr(grid64), _ptr(grid32), _ptr(raw),
+                                            status.data_ptr(), s), "arb_ingest_ordered_fill")
+            ev.synchronize()
+            sm = summ_h.numpy().copy()
             done = int(sm[0]) == 0
+            if done:
+                self._fill_pending = True
+                self._fill_src = (ft, is32, npts, ncol, cap, axes, counts, work, wb, grid64, grid32, raw)
         if not done:
-            check(L.arb_ingest_axes(ft.data_ptr(), is32, npts, ncol, dim, cap, axes.data_ptr(),
-                                    counts.data_ptr(), work.data_ptr(), wb, status.data_ptr(), s),
-                  "arb_ingest_axes")
-            st = L.arb_status_fetch(status.data_ptr(), s)
-            n = [int(v) for v in counts.cpu()]
-            if st & _lib.ARB_ERR_CAPACITY:
-                raise ValueError(f"an axis has more than {cap} grid samples")
-            if st:
-                raise ValueError("field rows are not a regular grid (NaN coordinates or duplicate points)")
-            if any(v < 4 for v in n):
-                raise ValueError("every axis needs at least 4 grid points")
-            if int(np.prod(n)) != npts:
-                raise ValueError(f"field rows do not form a full regular grid: {npts} rows, axes {n}")
-            claim = torch.empty(npts, dtype=torch.int32, device=dev)
-            n_c = (ctypes.c_int64 * 4)(*(n + [1] * (4 - dim)))
-            check(L.arb_ingest_scatter(ft.data_ptr(), is32, npts, ncol, dim, ax64.data_ptr(), cap,
-                                       n_c, kind, _ptr(grid64), _ptr(grid32), _ptr(raw),
-                                       claim.data_ptr(), status.data_ptr(), s), "arb_ingest_scatter")
-            sm = summary()
-            if self.check and int(sm[0]):
-                raise ValueError("field rows are not a full regular grid (duplicate or off-axis points)")
-            del claim
+            sm = self._ingest_general(ft, is32, npts, ncol, cap, axes, counts, work, wb, grid64, grid32, raw)
         n = [int(sm[1 + a]) for a in range(dim)]
         self._axes_dev = [ax64[a, : n[a]] for a in range(dim)]
         self._n = n
         self._npts = npts
-        self.ingest_path = "ordered" if done else "general"
-        self._grid64_t, self._grid32, self._raw_t = grid64, grid32, raw
+        self._ingest_path = "ordered" if done else "general"
+        self._grid64_t, self._grid32_t, self._raw_t = grid64, grid32, raw
         self._ingest_ordered = done
-        self._status = status
         # reference attributes, computed in the field's own dtype (ARB:541-568)
         dt = self._field_dtype
         h = [np.abs(dt(sm[5 + 3 * a]) - dt(sm[6 + 3 * a])) for a in range(dim)]
@@ -294,17 +287,101 @@ class _Interpolant:
         g.grid32 = _ptr(grid32)
         g.table = None
         g.table_prec = 0
-        self._g = g
+        self._gs = g
+
+    def _ingest_general(self, ft, is32, npts, ncol, cap, axes, counts, work, wb, grid64, grid32, raw):
+        """Rows in any order: axis scan, rank sort and scatter (ARB:528-568);
+        returns the ingest summary, raises ValueError for a field that is not
+        a full regular grid."""
+        L = lib()
+        dim, dev, kind, s = self._dim, self.device, self._kind, _stream()
+        status = self._status
+        summ = torch.empty(17, dtype=torch.float64, device=dev)
+        ax64 = axes[: dim * cap].view(dim, cap)
+        check(L.arb_ingest_axes(ft.data_ptr(), is32, npts, ncol, dim, cap, axes.data_ptr(),
+                                counts.data_ptr(), work.data_ptr(), wb, status.data_ptr(), s),
+              "arb_ingest_axes")
+        st = L.arb_status_fetch(status.data_ptr(), s)
+        n = [int(v) for v in counts.cpu()]
+        if st & _lib.ARB_ERR_CAPACITY:
+            raise ValueError(f"an axis has more than {cap} grid samples")
+        if st:
+            raise ValueError("field rows are not a regular grid (NaN coordinates or duplicate points)")
+        if any(v < 4 for v in n):
+            raise ValueError("every axis needs at least 4 grid points")
+        if int(np.prod(n)) != npts:
+            raise ValueError(f"field rows do not form a full regular grid: {npts} rows, axes {n}")
+        claim = torch.empty(npts, dtype=torch.int32, device=dev)
+        n_c = (ctypes.c_int64 * 4)(*(n + [1] * (4 - dim)))
+        check(L.arb_ingest_scatter(ft.data_ptr(), is32, npts, ncol, dim, ax64.data_ptr(), cap,
+                                   n_c, kind, _ptr(grid64), _ptr(grid32), _ptr(raw),
+                                   claim.data_ptr(), status.data_ptr(), s), "arb_ingest_scatter")
+        check(L.arb_ingest_summary(axes.data_ptr(), cap, counts.data_ptr(), dim, status.data_ptr(),
+                                   summ.data_ptr(), s), "arb_ingest_summary")
+        sm = summ.cpu().numpy()
+        if self.check and int(sm[0]):
+            raise ValueError("field rows are not a full regular grid (duplicate or off-axis points)")
+        return sm
+
+    def _settle(self):
+        """Wait for a single-pass grid fill still in flight and read its row
+        check (see _settle_status)."""
+        if self._fill_pending:
+            self._settle_status(lib().arb_status_fetch(self._status.data_ptr(), _stream()))
+
+    def _settle_status(self, st):
+        """Close the single-pass fill given the status word read after it.
+        If a row was not where meshgrid order puts it, the general ingest
+        rewrites the grid (or raises ValueError for a field that is no full
+        regular grid).  The geometry stays: when the probe's lines through
+        row 0 hold n_a strictly monotone samples per axis with prod n_a rows,
+        a full grid's axes hold exactly those samples.  Returns True when the
+        grid was rewritten (results computed from it before are void)."""
+        self._fill_pending = False
+        src, self._fill_src = self._fill_src, None
+        if not st & _lib.ARB_ERR_IRREGULAR_GRID:
+            return False
+        n_probe = list(self._n)
+        sm = self._ingest_general(*src)
+        if [int(sm[1 + a]) for a in range(self._dim)] != n_probe:
+            raise RuntimeError("the general ingest found other axes than the single-pass probe")
+        self._ingest_ordered = False
+        self._ingest_path = "general"
+        return True
+
+    @property
+    def _g(self):
+        """The arb_grid descriptor, once the grid is written and checked."""
+        if self._fill_pending:
+            self._settle()
+        return self._gs
+
+    @property
+    def _grid32(self):
+        if self._fill_pending:
+            self._settle()
+        return self._grid32_t
+
+    @property
+    def ingest_path(self):
+        """'ordered' (rows in meshgrid order, single pass) or 'general'."""
+        if self._fill_pending:
+            self._settle()
+        return self._ingest_path
 
     @property
     def _grid64(self):
         """[npts*F] float64 grid values (produced on first use in the lazy case)."""
+        if self._fill_pending:
+            self._settle()
         if self._grid64_t is None:
             self._materialise_grid64()
         return self._grid64_t
 
     @property
     def _raw(self):
+        if self._fill_pending:
+            self._settle()
         if self._grid64_t is None and self._src is not None:
             self._materialise_grid64()
         return self._raw_t
@@ -487,7 +564,9 @@ class _Interpolant:
 
     def _launch(self, qd, n, qs, writeback, want_oob, plan, res=None):
         """Launch one evaluation of device rows qd with a given plan (into
-        the preallocated outputs res when given)."""
+        the preallocated outputs res when given).  Does not wait for a
+        single-pass grid fill still in flight (the launches queue behind it);
+        the caller settles it at its next synchronisation."""
         L = lib()
         if res is None:
             res = self._outputs(n, want_oob)
@@ -499,17 +578,17 @@ class _Interpolant:
         prec = _lib.PREC_FP64 if self.precision == "fp64" else _lib.PREC_MIXED
         if plan["binned"]:
             # group queries by spatial bin first (cell-coherent gathers)
-            self._g.bin_shift = int(plan.get("bin_shift", 0))
-            need = int(L.arb_query_sorted_work_bytes(self._g, prec, n))
+            self._gs.bin_shift = int(plan.get("bin_shift", 0))
+            need = int(L.arb_query_sorted_work_bytes(self._gs, prec, n))
             if self._ws is None or self._ws.numel() < need:
                 self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
-            rc = L.arb_query_eval_sorted(self._g, prec, int(table), qd.data_ptr(), n, qs, int(writeback),
+            rc = L.arb_query_eval_sorted(self._gs, prec, int(table), qd.data_ptr(), n, qs, int(writeback),
                                          out, self._ws.data_ptr(), need, self._status.data_ptr(), s)
         elif table:
-            rc = L.arb_query_eval(self._g, qd.data_ptr(), n, qs, int(writeback), out,
+            rc = L.arb_query_eval(self._gs, qd.data_ptr(), n, qs, int(writeback), out,
                                   self._status.data_ptr(), s)
         else:
-            rc = L.arb_query_eval_otf(self._g, prec, qd.data_ptr(), n, qs, int(writeback), out,
+            rc = L.arb_query_eval_otf(self._gs, prec, qd.data_ptr(), n, qs, int(writeback), out,
                                       self._status.data_ptr(), s)
         check(rc, "query evaluation")
         return res
@@ -543,18 +622,29 @@ class _Interpolant:
             direct = query.dtype == torch.float64 and query.is_contiguous()
             qd = query if direct else query.to(torch.float64).contiguous()
             res = self._run(qd, n, qs, True, False)
+            if self.check or self._fill_pending:
+                st = self._fetch_status()
+                if self._fill_pending and self._settle_status(st):
+                    # the grid was rewritten by the general ingest: evaluate
+                    # again (rows already written back; indices of the first run)
+                    st &= ~_lib.ARB_ERR_IRREGULAR_GRID
+                    self._launch(qd, n, qs, False, False, self.last_plan,
+                                 res=(res[0], res[1], res[2], None, None, None))
+                    st |= self._fetch_status()
+                if self.check and st & _lib.ARB_ERR_CELL_INDEX:
+                    if not direct:
+                        query.copy_(qd.to(query.dtype))
+                    self._last_inds = res[3]
+                    raise IndexError("cell index beyond the coefficient table (query on an upper face)")
             if not direct:
                 query.copy_(qd.to(query.dtype))
             self._last_inds = res[3]
-            if self.check:
-                st = self._fetch_status()
-                if st & _lib.ARB_ERR_CELL_INDEX:
-                    raise IndexError("cell index beyond the coefficient table (query on an upper face)")
             return self._pack(*res[:3])
         qa = query if isinstance(query, np.ndarray) else np.asarray(query)
         n, qs = int(qa.shape[0]), int(qa.shape[1])
         if qs < dim:
             raise IndexError("query rows need at least %d columns" % dim)
+        self._settle()
         qc = np.ascontiguousarray(qa, dtype=np.float64)
         if n >= PIPELINE_MIN_ROWS:
             return self._rquery_host_pipelined(qa, qc, n, qs)
@@ -600,18 +690,22 @@ class _Interpolant:
         ev_done = [torch.cuda.Event() for _ in range(K)]
         s_in.wait_stream(cur)                       # the buffers were allocated on the current stream
         with torch.cuda.stream(s_in):
-            for k in range(K):
+            qd[:bounds[1]].copy_(src[:bounds[1]], non_blocking=True)
+            ev_in[0].record(s_in)
+        # the plan for this chunk size, chosen before the other chunks' uploads
+        # are queued: the autotuner times its candidates with the link idle
+        cur.wait_event(ev_in[0])
+        plan = self._plan(qd[:bounds[1]], bounds[1], qs)
+        self.last_plan = plan
+        with torch.cuda.stream(s_in):
+            for k in range(1, K):
                 a, b = bounds[k], bounds[k + 1]
                 qd[a:b].copy_(src[a:b], non_blocking=True)
                 ev_in[k].record(s_in)
-        plan = None
         sl = lambda t, a, b: None if t is None else t[a:b]  # noqa: E731
         for k in range(K):
             a, b = bounds[k], bounds[k + 1]
             cur.wait_event(ev_in[k])
-            if plan is None:
-                plan = self._plan(qd[a:b], b - a, qs)
-                self.last_plan = plan
             res = (sl(comps, a, b), sl(norms, a, b), sl(grads, a, b), inds[a:b], oob[a:b], cnts[k:k + 1])
             self._launch(qd[a:b], b - a, qs, False, True, plan, res=res)
             ev_done[k].record(cur)
@@ -641,6 +735,7 @@ class _Interpolant:
         for a in range(dim):
             if qv[a] < self._lo[a] or qv[a] > self._hi[a]:
                 return np.nan
+        self._settle()
         row = torch.tensor([qv], dtype=torch.float64).to(self.device)
         comps, norms, grads, inds, _, _ = self._run(row, 1, dim, False, False)
         st = self._fetch_status()

@@ -1097,10 +1097,10 @@ def main():
         cpu = cpu_baseline(field.cpu().numpy(), q.cpu().numpy())
 
     if rank == 0:
-        # this library's kernels per step: ingest (meshgrid-order rows: probe, gather, summary;
-        # otherwise those three plus axes init/collect/sort, index, gather, summary) and the
-        # query (binned: count, two scan passes, place, evaluate; plain: one)
-        launches_per_step = ((3 if o.ingest_path == "ordered" else 9) +
+        # this library's kernels per step: ingest (meshgrid-order rows: probe, summary, gather,
+        # tile; otherwise those four plus axes init/collect/sort, index, gather, summary) and
+        # the query (binned: count, two scan passes, place, evaluate; plain: one)
+        launches_per_step = ((4 if o.ingest_path == "ordered" else 10) +
                              (5 if o.last_plan.get("binned") else 1))
         line = {
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,

@@ -146,6 +146,23 @@ int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64_t npts, in
                        int64_t *axis_count, double *grid64, float *grid32, double *raw_out,
                        void *work, size_t work_bytes, int32_t *status, arb_stream_t stream);
 
+/* arb_ingest_ordered in two launches on the same stream, so that the host
+ * can read the axes (arb_ingest_summary after the probe) while the grid is
+ * still being written: _probe reads the axes off the lines through row 0
+ * (ARB_ERR_IRREGULAR_GRID in *status if those lines are not a meshgrid);
+ * _fill writes every grid slot and checks every row, with the same axes and
+ * work (ARB_ERR_IRREGULAR_GRID for rows in another order; it does nothing
+ * after a failed probe).  The same reference code (ARB:528-568, 1264-1320). */
+int arb_ingest_ordered_probe(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                             int32_t dim, int32_t kind, int64_t axis_cap, double *axis_out,
+                             int64_t *axis_count, void *work, size_t work_bytes, int32_t *status,
+                             arb_stream_t stream);
+
+int arb_ingest_ordered_fill(const void *field, int32_t field_is_f32, int64_t npts, int32_t ncol,
+                            int32_t dim, int32_t kind, int64_t axis_cap, const double *axis_out,
+                            const void *work, size_t work_bytes, double *grid64, float *grid32,
+                            double *raw_out, int32_t *status, arb_stream_t stream);
+
 /* Everything the host needs after an ingest, for one device-to-host copy:
  * out[0] = *status (then cleared), out[1 + a] = axis_count[a], and per axis
  * a the samples 0, 1 and n_a - 2 at out[5 + 3a .. 7 + 3a] (the reference's

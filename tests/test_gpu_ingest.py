@@ -104,14 +104,51 @@ def test_other_orders_fall_back():
         o = tricubic(g, "quiet")
         assert o.ingest_path == "general"
         assert np.array_equal(o.Query(q.copy())[0], ref.Query(q.copy())[0], equal_nan=True)
+    # a field that is no full regular grid raises ValueError: at construction
+    # when the axis probe sees it, else at the first use of the grid
     off = f.copy()
-    off[33, 1] += 1e-3                                  # a point off its axis
+    off[33, 1] += 1e-3                                  # a point off its axis (not on the probed lines)
     with pytest.raises(ValueError):
-        tricubic(off, "quiet")
+        tricubic(off, "quiet").Query(q.copy())
     dup = f.copy()
     dup[5] = dup[6]                                     # duplicate point, one slot empty
     with pytest.raises(ValueError):
-        tricubic(dup, "quiet")
+        tricubic(dup, "quiet").Query(q.copy())
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("binned", [False, True])
+def test_single_pass_check_read_at_first_query(prec, binned):
+    """The constructor waits for the axis probe only; the pass that writes the
+    grid is checked at the first synchronisation.  Rows that pass the probe
+    (the lines through row 0 form a meshgrid) but are out of order elsewhere
+    make the first device query rewrite the grid with the general ingest and
+    evaluate again: the same outputs, write-back and indices as an
+    interpolant built from the rows in order; a point off its axis raises
+    ValueError there."""
+    import torch
+    from arbinterp_gb300 import tricubic
+    f = _field(3, (2, 1, 0), (), vector=True)
+    g = f.copy()
+    g[[10, 57]] = g[[57, 10]]
+    q = np.random.default_rng(6).uniform(f[:, :3].min(0) - 0.05, f[:, :3].max(0) + 0.05, (500, 3))
+    kw = dict(mode="both", precision=prec, sort_threshold=0 if binned else 1 << 30)
+    ref = tricubic(torch.from_numpy(f).cuda(), "quiet", **kw)
+    o = tricubic(torch.from_numpy(g).cuda(), "quiet", **kw)
+    assert o._fill_pending
+    qa, qb = torch.from_numpy(q).cuda(), torch.from_numpy(q).cuda()
+    ra, rb = ref.Query(qa), o.Query(qb)
+    assert not o._fill_pending and o._ingest_path == "general" and ref.ingest_path == "ordered"
+    assert torch.equal(qa.isnan(), qb.isnan())
+    assert np.array_equal(ref.queryInds, o.queryInds)
+    for x, y in zip(ra, rb):
+        assert torch.equal(x.isnan(), y.isnan())
+        assert torch.equal(torch.nan_to_num(x), torch.nan_to_num(y))
+    off = f.copy()
+    off[33, 1] += 1e-3
+    o = tricubic(torch.from_numpy(off).cuda(), "quiet", **kw)
+    with pytest.raises(ValueError):
+        o.Query(torch.from_numpy(q).cuda())
 
 
 @pytest.mark.parametrize("mode", ["both", "norm"])
