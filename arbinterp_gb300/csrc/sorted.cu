@@ -65,17 +65,20 @@ struct BinGeom {
   int64_t nb[4];     // bins per axis
   int64_t nbins;     // product
   int shift;         // log2 cells per bin edge
-  int cls;           // log2 bank classes per bin (3: 3D mixed 8^3-cell bins; 4: 4D mixed scalar
+  int cls;           // log2 bank classes per bin (4: 3D mixed 8^3-cell bins and 4D mixed scalar
                      // 4^4-cell bins; 0 otherwise)
   int64_t nsub;      // nbins << cls sub-bins (bin-major); the special sub-bin is index nsub
 };
 
-// Bank class of a cell inside its 8^3-cell bin: the 16-byte bank group
-// (mod 8) of the cell's corner point in an unpadded 11 x 11 x 11 tile
-// (x + 11 y + 121 z, with 11 = 3 and 121 = 1 mod 8).  The bin origin is a
-// multiple of 8 on every axis, so the global cell coordinates give it.
+// Bank class of a cell inside its 8^3-cell bin: the index, mod 16, of the
+// cell's corner point in an unpadded 11 x 11 x 11 tile (x + 11 y + 121 z,
+// with 121 = 9 mod 16).  Mod 8 it is the corner's 16-byte bank group in the
+// tile of float4 points, mod 16 its 8-byte slot in the tile of float2 pairs.
+// Bin origins are multiples of 8 on every axis, so the class from the global
+// cell coordinates is the local one plus 0 or 8 for the whole bin: 8
+// consecutive classes stay distinct mod 8, and 16 distinct mod 16.
 __host__ __device__ __forceinline__ int bank_class(int64_t cx, int64_t cy, int64_t cz) {
-  return (int)((cx + 3 * cy + cz) & 7);
+  return (int)((cx + 11 * cy + 9 * cz) & 15);
 }
 
 // 4D: the 8-byte bank slot (mod 16) of the cell's corner point in an unpadded
@@ -102,7 +105,7 @@ static inline BinGeom bin_geom(const arb_grid *g, int precision) {
   }
   b.cls = 0;
   if (precision == ARB_PREC_MIXED) {
-    if (g->dim == 3 && b.shift == 3) b.cls = 3;
+    if (g->dim == 3 && b.shift == 3) b.cls = 4;
     if (g->dim == 4 && b.shift == 2 && g->nfield == 1) b.cls = 4;
   }
   b.nsub = b.nbins << b.cls;
@@ -168,7 +171,7 @@ __device__ __forceinline__ CoordStep bin_step(const arb_grid &g, const KParams &
 #pragma unroll
     for (int a = DIM - 2; a >= 0; --a) bin = bin * bg.nb[a] + (c[a] >> bg.shift);
     if constexpr (DIM == 3) {
-      if (bg.cls) bin = (bin << 3) | bank_class(c[0], c[1], c[2]);
+      if (bg.cls) bin = (bin << 4) | bank_class(c[0], c[1], c[2]);
     } else {
       if (bg.cls) bin = (bin << 4) | bank_class4(c[0], c[1], c[2], c[3]);
     }
@@ -229,7 +232,7 @@ __global__ void __launch_bounds__(256) bin_place_kernel(arb_grid g, KParams kp, 
   const uint32_t r = atomicSub(&w.hist[bin], 1u) - 1u;
   uint32_t pos;
   if (bg.cls && bin < bg.nsub) {
-    constexpr int NC = DIM == 3 ? 8 : 16;  // the class sub-bins of one bin, 32- or 64-byte aligned
+    constexpr int NC = 16;  // the class sub-bins of one bin (64-byte aligned)
     const int64_t b0 = bin & ~(int64_t)(NC - 1);
     uint32_t o[NC + 1];
 #pragma unroll
@@ -385,15 +388,18 @@ __global__ void __launch_bounds__(DIM == 3 ? 256 : 128) eval_sorted_kernel(arb_g
 // unbinned queries return the same bits, and every gradient component is
 // differenced along its own axis first.
 //
-// Bank order.  The tile is unpadded, x fastest: point (x, y, z) at
-// x + 11 y + 121 z, so point (i, j, k) of the block of local cell
-// (cx, cy, cz) lies in 16-byte bank group (bank_class(cx, cy, cz) +
-// i + 3 j + k) mod 8.  The placement pass orders each bin's queries into
-// eight sub-bins by bank class, and each group of 8 consecutive threads takes
-// 8 queries of 8 distinct classes (round robin over the classes), so every
-// 8-thread phase of a 16-byte shared load touches 8 distinct bank groups: one
-// wavefront, where 8 random queries would need about three.  Where fewer
-// than 8 classes are left in a bin, its last queries conflict as random
+// Bank order.  The tiles are unpadded, x fastest: point (x, y, z) at
+// e = x + 11 y + 121 z, so point (i, j, k) of the block of local cell
+// (cx, cy, cz) has e = bank_class(cx, cy, cz) + i + 11 j + 9 k + const
+// (mod 16): in the float4 tile its 16-byte bank group is e mod 8, in the
+// float2 tile of lo pairs its 8-byte slot e mod 16.  The placement pass
+// orders each bin's queries into 16 sub-bins by class and writes them round
+// robin over the classes 0..15, so in a level with all 16 classes each
+// quarter-warp (the 8 threads of one phase of a 16-byte load) holds 8
+// consecutive classes, distinct mod 8, and each half-warp (one phase of an
+// 8-byte load) 16 distinct classes: one wavefront each, where random queries
+// need about three for the 16-byte loads and two for the 8-byte ones.  Where
+// fewer classes are left in a bin, its last queries conflict as random
 // queries would.
 constexpr int BIN_EDGE = 8;
 constexpr int TILE_EDGE = BIN_EDGE + 3;
@@ -516,9 +522,10 @@ __global__ void __launch_bounds__(BINC_THREADS, F == 4 ? 3 : (F == 3 ? 5 : 4)) e
   BinTile<F> *tiles = reinterpret_cast<BinTile<F> *>(binc_smem);
   const int64_t nbins = bg.nbins;
   const QRec<float> *recs = reinterpret_cast<const QRec<float> *>(w.rec);
-  // bin b holds records [offs[8b], offs[8b + 8]) (its 8 class sub-bins)
-  auto begin = [&](int64_t bb) { return w.offs[bb << 3]; };
-  auto count = [&](int64_t bb) { return bb < nbins ? w.offs[(bb + 1) << 3] - begin(bb) : 0u; };
+  // bin b holds records [offs[16 b], offs[16 b + 16]) (its 16 class sub-bins)
+  const int cls = bg.cls;
+  auto begin = [&](int64_t bb) { return w.offs[bb << cls]; };
+  auto count = [&](int64_t bb) { return bb < nbins ? w.offs[(bb + 1) << cls] - begin(bb) : 0u; };
   auto origin = [&](int64_t bb, int og[3]) {
     og[0] = (int)((bb % bg.nb[0]) * BIN_EDGE);
     const int64_t r = bb / bg.nb[0];
@@ -615,7 +622,7 @@ static bool launch_eval_binc_f(const arb_grid *g, const KParams &kp, const BinGe
 
 static bool launch_eval_binc(const arb_grid *g, const KParams &kp, const BinGeom &bg, int64_t nq,
                              const arb_query_out *out, const SortedWork &w, cudaStream_t s) {
-  if (g->dim != 3 || bg.shift != 3 || bg.cls != 3) return false;
+  if (g->dim != 3 || bg.shift != 3 || bg.cls != 4) return false;
   if (g->nfield == 1) return launch_eval_binc_f<1>(g, kp, bg, nq, out, w, s);
   if (g->nfield == 3) return launch_eval_binc_f<3>(g, kp, bg, nq, out, w, s);
   if (g->nfield == 4) return launch_eval_binc_f<4>(g, kp, bg, nq, out, w, s);

@@ -286,9 +286,9 @@ int arb_query_eval_binned(const arb_grid *g, int32_t precision, int32_t use_tabl
  *      on every GPU that loads the library, held until the process exits.
  *      Calls whose scratch need (arb_query_sorted_work_bytes) exceeds it
  *      return ARB_ERR_CAPACITY without touching the GPU — on a 256^3 grid
- *      (32768 bins, 8 sub-bins each in mixed precision) at most 344,048
+ *      (32768 bins, 16 sub-bins each in mixed precision) at most 344,048
  *      query rows per call in float64 and
- *      458,728 in mixed precision (48- and 32-byte records); split larger
+ *      393,184 in mixed precision (48- and 32-byte records); split larger
  *      query sets into several calls.  Arguments are checked first, as
  *      arb_query_eval_sorted checks them.
  *
