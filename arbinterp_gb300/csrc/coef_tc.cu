@@ -343,13 +343,18 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
 // Grids that miss these rules, and partial solves, take coef3_tc_kernel.
 //
 // One CTA per SM, three roles working on consecutive tiles at once, each
-// hand-off an mbarrier and every resource two-deep:
+// hand-off an mbarrier; footprints three-deep, A tiles and accumulators
+// two-deep, one staging area (the epilogue waits for the previous tile's
+// stores to have read it):
 //   producers (8 warps): the gather of a footprint into row deltas, the
 //       per-row scale, the three-part FP16 split into an A tile; thread t
 //       owns half t >> 7 (block layers 2h, 2h+1) of row t & 127;
-//   loader (one thread): the footprint boxes two tiles ahead and the 12
-//       MMAs of each tile into one of two TMEM accumulator stages
-//       (3 x 64 columns each, at columns 0 and 256);
+//   footprint loader (one thread of warp 12): the boxes three tiles ahead,
+//       issued as soon as the producers have gathered from the buffer;
+//   MMA issuer (one thread of warp 13): the 12 MMAs of each tile into one
+//       of two TMEM accumulator stages (3 x 64 columns each, at columns 0
+//       and 256).  Issuing a tile's MMAs takes about 1000 cycles; with the
+//       box loads in the same thread the loads fell behind the producers;
 //   epilogue (4 warps): warp 8 + w reads TMEM lanes 32w..32w+31 (a whole
 //       row per thread), combines the three part sums, stages the rows
 //       128-byte swizzled and one thread writes them with two TMA stores.
@@ -359,8 +364,8 @@ __global__ void __launch_bounds__(NT, 2) coef3_tc_kernel(const __grid_constant__
 // ARB_ERR_TIMEOUT into the status word and raises a shared abort flag that
 // ends every role's waits; the producer and epilogue warps leave their loops
 // together (a barrier that ORs their failures), and before the accumulator
-// columns are released and the CTA exits, the loader waits with the full
-// limit for its last MMAs and for any footprint load still in flight.
+// columns are released and the CTA exits, the MMA issuer waits with the full
+// limit for its last MMAs and the footprint loader for any box in flight.
 namespace {
 template <int F>
 struct TmaShape;
@@ -380,19 +385,22 @@ constexpr int FP_BYTES = 17408;  // >= every shape's HBYTES + LBYTES, a multiple
 
 constexpr int WS_PROD = 256;                        // producer threads (warps 0-7)
 constexpr int WS_EPI = 128;                         // epilogue threads (warps 8-11)
-constexpr int WS_THREADS = WS_PROD + WS_EPI + 32;   // + warp 12: loader and MMA issue
+constexpr int WS_WARP_FP = (WS_PROD + WS_EPI) / 32;  // warp 12: footprint loads
+constexpr int WS_WARP_MMA = WS_WARP_FP + 1;           // warp 13: MMA issue
+constexpr int WS_THREADS = WS_PROD + WS_EPI + 64;
 constexpr int WS_TMEM_COLS = 512;                   // two accumulator stages of 3 x 64 columns
 constexpr uint32_t BAR_PROD = 1, BAR_EPI = 2;       // named barriers of the producer and epilogue warps
+constexpr int WS_FP = 3;                            // footprint buffers: boxes three tiles ahead
 
 struct WsSmem {
   unsigned char a[2][A_BYTES];             // A tiles, no-swizzle K-major (offset 0)
-  unsigned char stage[2][2][BOX_BYTES];    // output rows of a tile: two 128-byte swizzled boxes (1 KB aligned)
+  unsigned char stage[2][BOX_BYTES];       // output rows of a tile: two 128-byte swizzled boxes (1 KB aligned)
   unsigned char b[B_BYTES];                // B = 8 A
-  unsigned char fp[2][FP_BYTES];           // footprints
+  unsigned char fp[WS_FP][FP_BYTES];       // footprints
   float amax[2][2][TM];                    // [tile parity][half][row]
   float mrhi[4][TM], mrlo[4][TM];          // each row's corner value (hi, lo), by tile mod 4
   int mexp[4][TM];                         // each row's scale exponent
-  uint64_t fp_full[2], fp_empty[2], a_full[2], a_empty[2], acc_full[2], acc_empty[2];
+  uint64_t fp_full[WS_FP], fp_empty[WS_FP], a_full[2], a_empty[2], acc_full[2], acc_empty[2];
   uint32_t tmem_base;
   int abort;
 };
@@ -443,9 +451,11 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
     tc::tmem_relinquish();
   }
   if (tid == 0) {
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < WS_FP; ++s) {
       tc::mbar_init(&sm.fp_full[s], 1);
       tc::mbar_init(&sm.fp_empty[s], WS_PROD / 32);
+    }
+    for (int s = 0; s < 2; ++s) {
       tc::mbar_init(&sm.a_full[s], WS_PROD / 32);
       tc::mbar_init(&sm.a_empty[s], 1);
       tc::mbar_init(&sm.acc_full[s], 1);
@@ -473,12 +483,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
       const int64_t xr = tile / tpr;
       const int x0 = (int)((tile - xr * tpr) * S::C);
       const int cnt = tile - xr * tpr == tpr - 1 ? rem : S::C;
-      bool ok = !fail && ws_wait(sm, &sm.fp_full[s], ph, WAIT_LIMIT, status);
+      const int fs = k % WS_FP;
+      bool ok = !fail && ws_wait(sm, &sm.fp_full[fs], (uint32_t)(k / WS_FP) & 1u, WAIT_LIMIT, status);
       float rhi = 0.f, rlo = 0.f, d[32], amax = 0.f;
 #pragma unroll
       for (int j = 0; j < 32; ++j) d[j] = 0.f;
       if (ok && cl < cnt) {
-        const unsigned char *fpb = sm.fp[s];
+        const unsigned char *fpb = sm.fp[fs];
         const float *fh = reinterpret_cast<const float *>(fpb);
         auto pt = [&](int ox, int oy, int oz, float &h, float &l) {
           const int P = (oz * 4 + oy) * S::HX + cl + ox;
@@ -513,7 +524,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
             }
       }
       __syncwarp();
-      if (ok && lane == 0) tc::mbar_arrive(&sm.fp_empty[s]);  // this warp has read the footprint
+      if (ok && lane == 0) tc::mbar_arrive(&sm.fp_empty[fs]);  // this warp has read the footprint
       sm.amax[s][half][row] = amax;
       if (tc::named_bar_or(BAR_PROD, WS_PROD, !ok)) break;   // every producer leaves together
       const int E = scale_exp(fmaxf(amax, sm.amax[s][half ^ 1][row]));
@@ -553,7 +564,6 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
     // ---- epilogue: TMEM -> table rows ----------------------------------------
     const int ew = warp - WS_PROD / 32;                  // TMEM lanes 32 ew .. 32 ew + 31
     const int row = ew * 32 + lane;
-    const bool leader = tid == WS_PROD;                  // issues the TMA stores
     const uint32_t mma_wait_limit = g_mma_wait_limit;
     bool fail = false;
     for (int k = 0; k < nloc; ++k) {
@@ -561,7 +571,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
       const uint32_t ph = (uint32_t)(k >> 1) & 1u;
       const bool ok = !fail && ws_wait(sm, &sm.acc_full[s], ph, mma_wait_limit, status);
       tc::tc_fence_after();
-      if (leader) tc::bulk_wait_read1();                  // the stores of tile k - 2 have read stage[s]
+      if (tid == WS_PROD) tc::bulk_wait_read0();          // the stores of tile k - 1 have read the staging
       if (tc::named_bar_or(BAR_EPI, WS_EPI, !ok)) break;
       const int64_t tile = tile_of(k);
       const int64_t xr = tile / tpr;
@@ -582,7 +592,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
 #pragma unroll
         for (int j = 0; j < 16; ++j) p0[j] = __fmul_rn(__fadd_rn(p0[j], __fmaf_rn(p2[j], 0x1p-22f, p1[j])), so);
         if (q == 0) p0[0] = rhi + (rlo + p0[0]);
-        unsigned char *st_row = sm.stage[s][q >> 1] + row * 128;
+        unsigned char *st_row = sm.stage[q >> 1] + row * 128;
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           const int j = (q & 1) * 4 + c;                 // 16-byte chunk of the 128-byte row
@@ -595,18 +605,18 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
       if (lane == 0) tc::mbar_arrive(&sm.acc_empty[s]);  // this warp has read the accumulator
       tc::fence_proxy_async_smem();
       tc::named_bar_sync(BAR_EPI, WS_EPI);
-      if (leader) {
+      if (tid == WS_PROD) {
         const CUtensorMap *tm = cnt == S::C ? &tmap_full : &tmap_part;
-        tc::tma_store_2d(tm, sm.stage[s][0], 0, (int32_t)row0);
-        tc::tma_store_2d(tm, sm.stage[s][1], 32, (int32_t)row0);
+        tc::tma_store_2d(tm, sm.stage[0], 0, (int32_t)row0);
+        tc::tma_store_2d(tm, sm.stage[1], 32, (int32_t)row0);
         tc::bulk_commit();
       }
     }
-    if (leader) tc::bulk_wait0();
-  } else if (lane == 0) {
-    // ---- loader: footprints two tiles ahead, MMAs --------------------------
+    if (tid == WS_PROD) tc::bulk_wait0();
+  } else if (warp == WS_WARP_FP && lane == 0) {
+    // ---- footprint loader: boxes WS_FP tiles ahead ---------------------------
     auto issue_fp = [&](int k) {
-      const int s = k & 1;
+      const int s = k % WS_FP;
       const int64_t tile = tile_of(k);
       const int64_t xr = tile / tpr;
       const int x0 = (int)((tile - xr * tpr) * S::C);
@@ -619,8 +629,21 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
         if constexpr (F == 4) tc::tma_load_3d(sm.fp[s] + S::HBYTES, &tmap_lo, x0 & ~3, y, z, &sm.fp_full[s]);
       }
     };
-    int fp_issued = 0, mma_done = 0;
-    for (; fp_issued < nloc && fp_issued < 2; ++fp_issued) issue_fp(fp_issued);
+    int fp_issued = 0;
+    for (; fp_issued < nloc && fp_issued < WS_FP; ++fp_issued) issue_fp(fp_issued);
+    // the footprint WS_FP tiles ahead, as soon as the producers have read
+    // tile k's buffer (after their gather, long before its A tile is ready)
+    for (int k = 0; k + WS_FP < nloc; ++k) {
+      if (!ws_wait(sm, &sm.fp_empty[k % WS_FP], (uint32_t)(k / WS_FP) & 1u, WAIT_LIMIT, status)) break;
+      issue_fp(k + WS_FP);
+      fp_issued = k + WS_FP + 1;
+    }
+    // no box load in flight when the CTA's shared memory is given back
+    for (int kf = fp_issued - WS_FP > 0 ? fp_issued - WS_FP : 0; kf < fp_issued; ++kf)
+      (void)tc::mbar_wait_bounded(&sm.fp_full[kf % WS_FP], (uint32_t)(kf / WS_FP) & 1u, WAIT_LIMIT);
+  } else if (warp == WS_WARP_MMA && lane == 0) {
+    // ---- MMA issue -----------------------------------------------------------
+    int mma_done = 0;
     const uint32_t idesc = tc::idesc_f16(0u, 128u, 64u);
     const uint32_t b_base = tc::smem_u32(sm.b);
     for (int k = 0; k < nloc; ++k) {
@@ -642,20 +665,13 @@ __global__ void __launch_bounds__(WS_THREADS, 1) coef3_tma_kernel(const __grid_c
       tc::mma_commit(&sm.a_empty[s]);    // A[s] may be rewritten
       tc::mma_commit(&sm.acc_full[s]);   // the accumulator is ready
       mma_done = k + 1;
-      if (k + 2 < nloc) {                // the producers have read fp[s] (before they finished A[s])
-        if (!ws_wait(sm, &sm.fp_empty[s], ph, WAIT_LIMIT, status)) break;
-        issue_fp(k + 2);
-        fp_issued = k + 3;
-      }
     }
-    // nothing in flight when the columns are released and the CTA exits: the
-    // last MMAs (they complete in order) and the footprint loads not yet waited on
+    // no MMA in flight when the accumulator columns are released (they
+    // complete in order: the last one suffices)
     if (mma_done > 0) {
       const int kl = mma_done - 1;
       (void)tc::mbar_wait_bounded(&sm.acc_full[kl & 1], (uint32_t)(kl >> 1) & 1u, WAIT_LIMIT);
     }
-    for (int kf = fp_issued - 2 > 0 ? fp_issued - 2 : 0; kf < fp_issued; ++kf)
-      (void)tc::mbar_wait_bounded(&sm.fp_full[kf & 1], (uint32_t)(kf >> 1) & 1u, WAIT_LIMIT);
   }
   tc::tc_fence_before();
   __syncthreads();
