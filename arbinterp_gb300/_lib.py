@@ -70,6 +70,9 @@ SIGNATURES = {
     "arb_query_eval_sorted": (C.c_int, [C.POINTER(ArbGrid), _I32, _I32, _P, _I64, _I64, _I32,
                                         C.POINTER(ArbQueryOut), _P, C.c_size_t, _P, _P]),
     "arb_adjoint": (C.c_int, [C.POINTER(ArbGrid), _I32, _P, _I64, _I64, _P, _P, _P, _P, _P, _P]),
+    "arb_adjoint_work_bytes": (C.c_size_t, [C.POINTER(ArbGrid), _I64]),
+    "arb_adjoint_binned": (C.c_int, [C.POINTER(ArbGrid), _I32, _P, _I64, _I64, _P, _P, _P, _P, _P, C.c_size_t,
+                                     _P, _P]),
     "arb_grid_set_values": (C.c_int, [C.POINTER(ArbGrid), _P, _I32, _P, _P, _P]),
     "arb_batched_launch": (C.c_int, [_P, _I32, _I32, _P, _P, _I64, _I32, _I32, _P, _I64, _I32,
                                      C.POINTER(ArbQueryOut), _P, _P, _P]),

@@ -9,7 +9,11 @@ is differentiable with respect to the grid sample values (1-D tensor in grid
 order: z-major, x fastest) and the query coordinates.  Forward runs the
 query kernels of ``libarbinterp.so``; backward runs ``arb_adjoint`` (atomic
 scatter of dL/dvalue and dL/dgrad through the Catmull-Rom weights, and
-dL/dq from the interpolant's gradient and Hessian).
+dL/dq from the interpolant's gradient and Hessian), or in mixed precision
+with at least as many query rows as cells on ``arb_adjoint_binned`` (the
+same with the queries grouped by bin and the scatter accumulated per bin in
+shared memory).  A row whose upstream dL/dvalue is NaN scatters nothing and gets a
+NaN query gradient.
 
 Rows outside the interpolation volume give NaN values (as the reference
 does) and no gradient; mask them out of the loss.
@@ -68,11 +72,25 @@ class TricubicFunction(torch.autograd.Function):
         dv = None if dvalue is None else dvalue.detach().to(torch.float64).contiguous()
         dgr = None if dgrad is None else dgrad.detach().to(torch.float64).contiguous()
         prec = _lib.PREC_MIXED if mixed else _lib.PREC_FP64
-        _lib.check(L.arb_adjoint(interp._g, prec, q.data_ptr(), n, q.shape[1],
-                                 None if dv is None else dv.data_ptr(),
-                                 None if dgr is None else dgr.data_ptr(), gg.data_ptr(),
-                                 None if qg is None else qg.data_ptr(), interp._status.data_ptr(),
-                                 _stream()), "arb_adjoint")
+        args = (None if dv is None else dv.data_ptr(), None if dgr is None else dgr.data_ptr(), gg.data_ptr(),
+                None if qg is None else qg.data_ptr())
+        binned = ctx.field.binned_adjoint
+        if binned is None:
+            # grouping pays once a bin holds several hundred queries (the
+            # binning passes, each bin's tile and one flush of its 1331
+            # points): at least as many queries as cells
+            binned = n >= max(interp.sort_threshold, interp.nc)
+        if mixed and binned:
+            # grouped by bin: dL/df accumulated per bin in shared memory
+            need = int(L.arb_adjoint_work_bytes(interp._g, n))
+            if interp._ws is None or interp._ws.numel() < need:
+                interp._ws = torch.empty(need, dtype=torch.uint8, device=q.device)
+            _lib.check(L.arb_adjoint_binned(interp._g, prec, q.data_ptr(), n, q.shape[1], *args,
+                                            interp._ws.data_ptr(), need, interp._status.data_ptr(), _stream()),
+                       "arb_adjoint_binned")
+        else:
+            _lib.check(L.arb_adjoint(interp._g, prec, q.data_ptr(), n, q.shape[1], *args,
+                                     interp._status.data_ptr(), _stream()), "arb_adjoint")
         gvals = gg.to(ctx.values_dtype) if ctx.needs_input_grad[0] else None
         gq = qg.to(ctx.queries_dtype) if want_q else None
         return gvals, gq, None
@@ -86,9 +104,10 @@ class TricubicField:
     the initial values (NumPy or torch).  precision: 'fp64' or 'mixed'.
     """
 
-    def __init__(self, field_rows, precision="fp64", device=None, sort_threshold=1 << 15):
+    def __init__(self, field_rows, precision="fp64", device=None, sort_threshold=1 << 15, binned_adjoint=None):
         self.interp = tricubic(field_rows, "quiet", precision=precision, strategy="otf", device=device,
                                sort_threshold=sort_threshold)
+        self.binned_adjoint = binned_adjoint   # None: by query density; True / False: forced (mixed only)
         if self.interp._F != 1:
             raise ValueError("TricubicField needs a scalar field (N x 4 rows)")
 

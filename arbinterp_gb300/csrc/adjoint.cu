@@ -13,14 +13,6 @@
 
 namespace arb {
 
-template <typename T>
-__device__ __forceinline__ void cr_d2weights(T t, T d[4]) {
-  d[0] = T(2) - T(3) * t;
-  d[1] = T(-5) + T(9) * t;
-  d[2] = T(4) - T(9) * t;
-  d[3] = T(-1) + T(3) * t;
-}
-
 template <bool MIXED>
 __global__ void __launch_bounds__(256) adjoint3_kernel(arb_grid g, KParams kp, const double *q, int64_t nq,
                                                        int64_t qs, const double *dval, const double *dgrad,
@@ -51,7 +43,10 @@ __global__ void __launch_bounds__(256) adjoint3_kernel(arb_grid g, KParams kp, c
     dg[1] = (T)dgrad[i * 3 + 1];
     dg[2] = (T)dgrad[i * 3 + 2];
   }
-  if (dv != dv) return;  // a NaN upstream contributes nothing
+  if (dv != dv) {  // a NaN upstream: no scatter, a NaN query gradient
+    if (q_grad) q_grad[i * 3] = q_grad[i * 3 + 1] = q_grad[i * 3 + 2] = qnan();
+    return;
+  }
   int64_t c[3];
   cell_from_step<3>(s, g, c);
   T w[3][4], d1[3][4], d2[3][4];

@@ -67,6 +67,14 @@ __device__ __forceinline__ void cr_dweights(T t, T d[4]) {
   d[3] = t * (T(-1) + T(1.5) * t);
 }
 
+template <typename T>
+__device__ __forceinline__ void cr_d2weights(T t, T d[4]) {
+  d[0] = T(2) - T(3) * t;
+  d[1] = T(-5) + T(9) * t;
+  d[2] = T(4) - T(9) * t;
+  d[3] = T(-1) + T(3) * t;
+}
+
 // Cubic Hermite basis for the slope at t=0 (c=0) and at t=1 (c=1), and their
 // derivatives: the 1D factors of the inv(B) columns of the d4f/dxdydzdt rows.
 template <typename T>

@@ -234,6 +234,19 @@ int arb_adjoint(const arb_grid *g, int32_t precision, const double *q, int64_t n
                 const double *dval, const double *dgrad, void *grid_grad, double *q_grad,
                 int32_t *status, arb_stream_t stream);
 
+/* ---- the same adjoint (3D scalar, ARB_PREC_MIXED only) with the queries
+ *      grouped by 8^3-cell bins first, as arb_query_eval_sorted does: the
+ *      scatter of dL/df goes to a shared-memory tile of each bin's points
+ *      and reaches grid_grad with one atomic per point and bin (64 per query
+ *      in arb_adjoint).  Same arguments and results (float32 sums in another
+ *      order); work: caller-owned scratch of arb_adjoint_work_bytes(g, nq)
+ *      bytes.  nq < 2^32.  No counterpart in the reference. */
+size_t arb_adjoint_work_bytes(const arb_grid *g, int64_t nq);
+
+int arb_adjoint_binned(const arb_grid *g, int32_t precision, const double *q, int64_t nq, int64_t q_stride,
+                       const double *dval, const double *dgrad, void *grid_grad, double *q_grad, void *work,
+                       size_t work_bytes, int32_t *status, arb_stream_t stream);
+
 /* Replaces the sample values of a scalar (F = 1) interpolant: values[npts]
  * in grid order (z-major, x fastest), float32 (values_f32) or float64;
  * rewrites grid64 and, when given, the float32 split grid32.  The geometry

@@ -460,11 +460,12 @@ def test_autotuner_plans_and_caches(tmp_path, monkeypatch):
     assert o2.last_plan == plan
 
 
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_adjoint_gradients(prec):
+@pytest.mark.parametrize("prec,binned", [("fp64", False), ("mixed", False), ("mixed", True)])
+def test_adjoint_gradients(prec, binned):
     """Backward kernel: dL/d(grid values) against the float64 reference
     adjoint (dense A^T scatter of the reference's monomial form) and against
-    central finite differences; dL/d(query) against finite differences."""
+    central finite differences; dL/d(query) against finite differences.
+    binned: the bin-grouped adjoint (shared-memory scatter per bin)."""
     import torch
     from arbinterp_gb300 import synth
     from arbinterp_gb300.autograd import TricubicField
@@ -473,7 +474,7 @@ def test_adjoint_gradients(prec):
     f = synth.gaussian_field3(n=(18, 16, 20), h=(0.1, 0.12, 0.08), seed=41).numpy()
     if prec == "mixed":
         f = f.astype(np.float32)
-    fld = TricubicField(f, precision=prec)
+    fld = TricubicField(f, precision=prec, binned_adjoint=binned)
     ref = OracleTricubic(f.astype(np.float64))
     vals = fld.initial_values().to(dt).cuda().requires_grad_()
     lo, hi = np.array(ref.lo), np.array(ref.hi)
