@@ -462,6 +462,26 @@ __device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
   lo = sign ? -l : l;
 }
 
+// Asynchronous global -> shared copies (cp.async): 16 bytes bypassing L1,
+// 8 and 4 bytes through it; groups committed and waited on per thread.
+__device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *sdst, const void *gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 // Warp-aggregated append of an out-of-volume row index.
 __device__ __forceinline__ void append_oob(const arb_query_out &o, int64_t row, bool pred) {
   if (!o.oob_rows) return;

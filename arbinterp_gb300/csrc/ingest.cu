@@ -188,13 +188,21 @@ __device__ __forceinline__ double to_f64(TF v) {
 }
 
 // ||(bx, by, bz)|| for float64 components as a float32 pair hi + lo, in
-// float32 arithmetic only: the components are rescaled by the power of two
-// of the largest (exact, on the exponent bits), then double-float: error-free
-// squares via FMA, two-sum accumulation, one Newton correction of the float32
-// square root.  Accurate to ~2^-46 relative, below the pair's own
-// resolution.  Returns false (caller takes the float64 norm) for a largest
-// component outside [2^-90, 2^90], zeros, infinities and NaN.
-__device__ __forceinline__ bool norm_f32pair(double bx, double by, double bz, float &hi, float &lo) {
+// float32 arithmetic only, and each component rounded to float32 (ch, the
+// grid's hi of that component).  The components are rescaled by the power of
+// two of the largest (exact, on the exponent bits) and split on their bits:
+// h = the top 24 significand bits (truncated), l = the remaining 29 bits
+// rounded once to float32, so h + l is the scaled component to 2^-47
+// relative.  Then double-float: error-free squares via FMA, two-sum
+// accumulation, one Newton correction of the float32 square root.  Accurate
+// to ~2^-45 relative, below the pair's own resolution.  ch is h rounded to
+// nearest-even from the dropped bits, rescaled (exact where the component
+// and its scaled value are normal float32 numbers; other components take
+// split_f32).  Scaled components below 2^-60 add nothing to the norm.
+// Returns false (caller takes the float64 norm) for a largest component
+// outside [2^-90, 2^90], zeros, infinities and NaN.
+__device__ __forceinline__ bool norm_f32pair(double bx, double by, double bz, float &hi, float &lo,
+                                             float ch[3]) {
   const long long bb[3] = {__double_as_longlong(bx), __double_as_longlong(by), __double_as_longlong(bz)};
   int ex[3], em = 0;
 #pragma unroll
@@ -204,14 +212,34 @@ __device__ __forceinline__ bool norm_f32pair(double bx, double by, double bz, fl
   }
   if (em < 1023 - 90 || em > 1023 + 90) return false;
   const int sc = em - 1023;
+  const float f = __int_as_float((sc + 127) << 23);        // 2^sc, exact rescale
   float h[3], l[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    if (ex[a] - sc >= 1) {
-      split_f32(__longlong_as_double(bb[a] - ((long long)sc << 52)), h[a], l[a]);
+    const int es = ex[a] - sc;                              // biased exponent of the scaled component
+    const unsigned hi32 = (unsigned)((unsigned long long)bb[a] >> 32);
+    const unsigned sign = hi32 & 0x80000000u;
+    const unsigned top23 = ((hi32 & 0xfffffu) << 3) | ((unsigned)bb[a] >> 29);   // significand bits 51..29
+    const unsigned rem = (unsigned)bb[a] & 0x1fffffffu;                           // bits 28..0
+    if (es >= 963) {
+      const unsigned hb = sign | ((unsigned)(es - 896) << 23) | top23;
+      h[a] = __uint_as_float(hb);
+      // rem as float without the conversion instruction: rem = x 2^12 + y,
+      // both halves exact as magic-number floats, one rounded add
+      const float fx = __fsub_rn(__int_as_float(0x4b400000 + (int)(rem >> 12)), 12582912.f);
+      const float fy = __fsub_rn(__int_as_float(0x4b400000 + (int)(rem & 0xfffu)), 12582912.f);
+      const float r = __fadd_rn(__fmul_rn(fx, 4096.f), fy) * __int_as_float((es - 1075 + 127) << 23);
+      l[a] = sign ? -r : r;
     } else {
-      h[a] = 0.f;  // below 2^-1022 of the largest: no contribution
+      h[a] = 0.f;
       l[a] = 0.f;
+    }
+    if (es >= 963 && ex[a] >= 897) {
+      const bool up = rem > 0x10000000u || (rem == 0x10000000u && (top23 & 1u));
+      ch[a] = __uint_as_float(__float_as_uint(h[a]) + (up ? 1u : 0u)) * f;
+    } else {
+      float t;
+      split_f32(__longlong_as_double(bb[a]), ch[a], t);
     }
   }
   float s = 0.f, e = 0.f;
@@ -230,7 +258,6 @@ __device__ __forceinline__ bool norm_f32pair(double bx, double by, double bz, fl
   const float res = __fadd_rn(__fmaf_rn(-r, r, S), Slo);   // S + Slo - r^2
   const float rc = __fmul_rn(res, __fdividef(0.5f, r));
   const float h0 = __fadd_rn(r, rc);
-  const float f = __int_as_float((sc + 127) << 23);        // 2^sc, exact rescale
   hi = h0 * f;
   lo = __fsub_rn(rc, __fsub_rn(h0, r)) * f;
   return true;
@@ -246,8 +273,8 @@ __device__ __forceinline__ void write_slot(const TF *row, int64_t dest, int64_t 
                                            float *grid32, double *raw_out) {
   constexpr int F = (KIND == ARB_KIND_VECTOR) ? 3 : (KIND == ARB_KIND_BOTH ? 4 : 1);
   double out[4];
-  float nhi = 0.f, nlo = 0.f;
-  bool nsplit = false;
+  float nhi = 0.f, nlo = 0.f, chi[3];
+  bool nsplit = false;   // norm pair and component hi from norm_f32pair
   if (KIND == ARB_KIND_SCALAR) {
     out[0] = to_f64(row[dim]);
   } else {
@@ -259,7 +286,7 @@ __device__ __forceinline__ void write_slot(const TF *row, int64_t dest, int64_t 
       // ||B|| at the grid point in the field's own precision, as NumPy's
       // norm evaluates it: sqrt((bx*bx + by*by) + bz*bz).
       double nrm;
-      if (sizeof(TF) == 8 && grid32 && norm_f32pair(out[0], out[1], out[2], nhi, nlo)) {
+      if (sizeof(TF) == 8 && grid32 && norm_f32pair(out[0], out[1], out[2], nhi, nlo, chi)) {
         // the float64 value is needed only for grid64 (grid32 takes the pair)
         nrm = grid64 ? f2d_exact(nhi) + f2d_exact(nlo) : 0.0;
         nsplit = true;
@@ -297,6 +324,9 @@ __device__ __forceinline__ void write_slot(const TF *row, int64_t dest, int64_t 
       if (nsplit && f == F - 1) {
         hi[f] = nhi;
         lo[f] = nlo;
+      } else if (nsplit && F == 4) {
+        hi[f] = chi[f];   // components: hi only
+        lo[f] = 0.f;
       } else {
         split_f32(out[f], hi[f], lo[f]);
       }
@@ -491,7 +521,10 @@ __global__ void __launch_bounds__(256) ordered_gather_kernel(const TF *field, in
 // 32 (x) x 32 (S) tile at fixed other coordinates, reads its 1024 rows with
 // consecutive threads on consecutive rows (S runs along the rows), keeps them
 // in shared memory, and writes the slots with consecutive threads on
-// consecutive x.  Persistent over tiles.
+// consecutive x.  Persistent over tiles.  The kernel is bound by instruction
+// issue, so the indices are 32-bit (npts < 2^32) and a tile's digits (x tile,
+// S tile, the other axes) advance by the grid stride with carries instead of
+// being divided out of the tile number.
 constexpr int OT = 32;
 
 template <typename TF, int KIND, int DIM>
@@ -505,43 +538,63 @@ __global__ void __launch_bounds__(256) ordered_tile_kernel(const TF *field, int6
   // consecutive words, the write phase reads words 2 (OT + 1) / 2 apart,
   // both without bank conflicts beyond the two wavefronts 8-byte values need
   TF(*tile)[OT][OT + 1] = reinterpret_cast<TF(*)[OT][OT + 1]>(ot_smem);
-  int64_t nn[DIM], st[DIM];
+  uint32_t nn[DIM], sa[DIM], ps[DIM];
+  bool neg[DIM];
   int S = 1;
 #pragma unroll
   for (int a = 0; a < DIM; ++a) {
-    nn[a] = w->n[a];
-    st[a] = w->stride[a];
-    if (st[a] == 1 || st[a] == -1) S = a;
+    const int64_t st = w->stride[a];
+    nn[a] = (uint32_t)w->n[a];
+    neg[a] = st < 0;
+    sa[a] = (uint32_t)(st < 0 ? -st : st);
+    if (st == 1 || st == -1) S = a;
   }
-  int64_t pstride[DIM];  // slot strides (x fastest)
-  pstride[0] = 1;
+  ps[0] = 1;  // slot strides (x fastest)
 #pragma unroll
-  for (int a = 1; a < DIM; ++a) pstride[a] = pstride[a - 1] * nn[a - 1];
-  const int64_t tx_n = (nn[0] + OT - 1) / OT, ts_n = (nn[S] + OT - 1) / OT;
-  const int64_t ntiles = tx_n * ts_n * (npts / (nn[0] * nn[S]));
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    int64_t i[DIM];
-    const int64_t xt = t % tx_n;
-    int64_t r = t / tx_n;
-    const int64_t stile = r % ts_n;
-    r /= ts_n;
+  for (int a = 1; a < DIM; ++a) ps[a] = ps[a - 1] * nn[a - 1];
+  // digits of a tile number: x tile, S tile, then the other axes (slowest last)
+  uint32_t rad[DIM];
+  int ax[DIM];  // axis of digit k >= 2
+  rad[0] = (nn[0] + OT - 1) / OT;
+  rad[1] = (nn[S] + OT - 1) / OT;
+  uint32_t ntiles = rad[0] * rad[1];
+  {
+    int k = 2;
 #pragma unroll
-    for (int a = 1; a < DIM; ++a) {  // the remaining axes, slowest last
-      if (a == S) continue;
-      i[a] = r % nn[a];
-      r /= nn[a];
+    for (int a = 1; a < DIM; ++a)
+      if (a != S) {
+        ax[k] = a;
+        rad[k] = nn[a];
+        ntiles *= nn[a];
+        ++k;
+      }
+  }
+  uint32_t dig[DIM], step[DIM];
+  {
+    uint32_t t = blockIdx.x, g = gridDim.x;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      dig[k] = k + 1 < DIM ? t % rad[k] : t;
+      step[k] = k + 1 < DIM ? g % rad[k] : g;
+      t /= rad[k];
+      g /= rad[k];
     }
+  }
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    uint32_t i[DIM];
+#pragma unroll
+    for (int k = 2; k < DIM; ++k) i[ax[k]] = dig[k];
     // load: consecutive threads read consecutive rows (along S)
     for (int k = ty; k < OT; k += 8) {
-      i[0] = xt * OT + k;
-      i[S] = stile * OT + tx;
+      i[0] = dig[0] * OT + k;
+      i[S] = dig[1] * OT + tx;
       if (i[0] < nn[0] && i[S] < nn[S]) {
-        int64_t src = 0;
+        uint32_t src = 0;
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) src += st[a] > 0 ? i[a] * st[a] : (nn[a] - 1 - i[a]) * (-st[a]);
+        for (int a = 0; a < DIM; ++a) src += (neg[a] ? nn[a] - 1u - i[a] : i[a]) * sa[a];
         TF v[NC];
-        load_field_row<TF, NC>(field + src * NC, v);
+        load_field_row<TF, NC>(field + (size_t)src * NC, v);
 #pragma unroll
         for (int c = 0; c < NC; ++c) tile[c][k][tx] = v[c];
       }
@@ -549,17 +602,17 @@ __global__ void __launch_bounds__(256) ordered_tile_kernel(const TF *field, int6
     __syncthreads();
     // write: consecutive threads write consecutive slots (along x)
     for (int k = ty; k < OT; k += 8) {
-      i[0] = xt * OT + tx;
-      i[S] = stile * OT + k;
+      i[0] = dig[0] * OT + tx;
+      i[S] = dig[1] * OT + k;
       if (i[0] < nn[0] && i[S] < nn[S]) {
         TF row[NC];
 #pragma unroll
         for (int c = 0; c < NC; ++c) row[c] = tile[c][tx][k];
-        int64_t dest = 0;
+        uint32_t dest = 0;
         bool ok = true;
 #pragma unroll
         for (int a = 0; a < DIM; ++a) {
-          dest += i[a] * pstride[a];
+          dest += i[a] * ps[a];
           ok &= __double_as_longlong(to_f64(row[a])) == __double_as_longlong(__ldg(axes + a * cap + i[a]));
         }
         if (!ok) set_status(status, ARB_ERR_IRREGULAR_GRID);
@@ -567,6 +620,17 @@ __global__ void __launch_bounds__(256) ordered_tile_kernel(const TF *field, int6
       }
     }
     __syncthreads();
+    // next tile: add the grid stride digit by digit (each digit stays below
+    // twice its radix, so one conditional subtraction carries it)
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      dig[k] += step[k] + c;
+      if (k + 1 < DIM) {
+        c = dig[k] >= rad[k] ? 1u : 0u;
+        dig[k] -= c ? rad[k] : 0u;
+      }
+    }
   }
 }
 

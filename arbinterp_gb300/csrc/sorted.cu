@@ -11,11 +11,12 @@
 //              bookkeeping of rQuery (NaN rows, queryInds) and the sub-bin
 //              histogram (fire-and-forget atomics)
 //   scan     : exclusive prefix sum of the histogram into a second array
-//              (the counts stay)
+//              (the counts stay), and with bank classes one 32-byte header
+//              per bin (its start and its 16 class counts)
 //   place    : the same coordinate step again, a rank inside the query's
 //              sub-bin (an atomic that counts the histogram back down to
-//              zero) and one 32-byte record (packed cell, row, fraction)
-//              written at its final position
+//              zero), the bin's header (one load) and one 32-byte record
+//              (packed cell, row, fraction) written at its final position
 //   evaluate : on-the-fly or table evaluation in record order, outputs
 //              written to the query's original row
 // Recomputing the coordinate step (float32 pipe in mixed precision) is
@@ -52,11 +53,23 @@ struct __align__(16) QRec<double> {
 };
 static_assert(sizeof(QRec<float>) == 32 && sizeof(QRec<double>) == 48, "record sizes");
 
+// Placement header of a bin with 16 bank classes: where its records start
+// and how many each class holds, so the placement pass reads one sector
+// per query instead of the bin's 17 offsets.
+struct __align__(32) BinHdr {
+  uint32_t cnt[4];  // class k's count in byte k & 3 of cnt[k >> 2] (when ovf == 0)
+  uint32_t start;   // offs of the bin's class 0 sub-bin
+  uint32_t ovf;     // a class holds more than 255 queries: read the offsets instead
+  uint32_t pad[2];
+};
+static_assert(sizeof(BinHdr) == 32, "header size");
+
 struct SortedWork {
   uint32_t *hist;   // nsub + 1 sub-bin counts; placement counts them back down to zero
   uint32_t *offs;   // nsub + 1 exclusive offsets: sub-bin sb holds records [offs[sb], offs[sb + 1]),
                     // the special sub-bin nsub [offs[nsub], nq)
   uint32_t *part;   // per-block totals of the scan
+  BinHdr *hdr;      // nbins placement headers (bins with bank classes; null otherwise)
   void *rec;        // nq records (QRec<float> or QRec<double>) in bin order; with bank classes each
                     // bin's records are in its bank schedule (see bank_slot)
 };
@@ -135,6 +148,7 @@ static size_t carve(SortedWork *w, void *base, const arb_grid *g, int precision,
   t.hist = (uint32_t *)take(sizeof(uint32_t) * (bg.nsub + 1));
   t.offs = (uint32_t *)take(sizeof(uint32_t) * (bg.nsub + 1));
   t.part = (uint32_t *)take(sizeof(uint32_t) * scan_blocks(bg.nsub + 1));
+  t.hdr = bg.cls ? (BinHdr *)take(sizeof(BinHdr) * bg.nbins) : nullptr;
   t.rec = take((tsz == 4 ? sizeof(QRec<float>) : sizeof(QRec<double>)) * nq);
   if (w) *w = t;
   return off;
@@ -218,6 +232,17 @@ __device__ __forceinline__ uint32_t bank_slot(const uint32_t o[NC + 1], int c, u
   return pos;
 }
 
+// bank_slot from a bin header: start, and the 16 class counts as bytes.
+__device__ __forceinline__ uint32_t bank_slot_hdr(const uint32_t cnt[4], uint32_t start, int c, uint32_t r) {
+  uint32_t pos = start;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const uint32_t n = (cnt[k >> 2] >> (8 * (k & 3))) & 255u;
+    pos += min(n, r) + ((k < c && n > r) ? 1u : 0u);
+  }
+  return pos;
+}
+
 template <int DIM, bool EXACT, typename T>
 __global__ void __launch_bounds__(256) bin_place_kernel(arb_grid g, KParams kp, BinGeom bg, const double *q,
                                                         int64_t nq, int64_t qs, SortedWork w) {
@@ -232,19 +257,20 @@ __global__ void __launch_bounds__(256) bin_place_kernel(arb_grid g, KParams kp, 
   const uint32_t r = atomicSub(&w.hist[bin], 1u) - 1u;
   uint32_t pos;
   if (bg.cls && bin < bg.nsub) {
-    constexpr int NC = 16;  // the class sub-bins of one bin (64-byte aligned)
-    const int64_t b0 = bin & ~(int64_t)(NC - 1);
-    uint32_t o[NC + 1];
+    constexpr int NC = 16;  // the class sub-bins of one bin
+    uint32_t h[8];
+    asm volatile("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(h[0]), "=r"(h[1]), "=r"(h[2]), "=r"(h[3]), "=r"(h[4]), "=r"(h[5]), "=r"(h[6]), "=r"(h[7])
+                 : "l"(w.hdr + (bin >> 4)));
+    if (!h[5]) {
+      pos = bank_slot_hdr(h, h[4], (int)(bin & (NC - 1)), r);
+    } else {
+      const int64_t b0 = bin & ~(int64_t)(NC - 1);
+      uint32_t o[NC + 1];
 #pragma unroll
-    for (int k = 0; k < NC; k += 4) {
-      const uint4 a = *reinterpret_cast<const uint4 *>(w.offs + b0 + k);
-      o[k] = a.x;
-      o[k + 1] = a.y;
-      o[k + 2] = a.z;
-      o[k + 3] = a.w;
+      for (int k = 0; k <= NC; ++k) o[k] = w.offs[b0 + k];
+      pos = bank_slot<NC>(o, (int)(bin & (NC - 1)), r);
     }
-    o[NC] = w.offs[b0 + NC];
-    pos = bank_slot<NC>(o, (int)(bin & (NC - 1)), r);
   } else {
     pos = w.offs[bin] + r;
   }
@@ -288,7 +314,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_part_kernel(const uint32_t 
 // Exclusive scan of each chunk into offs, offset by the totals of the chunks
 // before it (the counts in hist stay for the placement pass).
 __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(const uint32_t *hist, int64_t n,
-                                                                  const uint32_t *part, uint32_t *offs) {
+                                                                  const uint32_t *part, uint32_t *offs,
+                                                                  BinHdr *hdr, int64_t nbins) {
   __shared__ uint32_t wsum[SCAN_THREADS / 32];
   __shared__ uint32_t carry_s;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -339,6 +366,26 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(const uint32_t
   for (int k = 0; k < SCAN_PER; ++k) {
     if (b + k < n) offs[b + k] = run;
     run += v[k];
+  }
+  if (hdr) {
+    // bins of 16 class counters: this thread holds classes 0-7 (even lane)
+    // or 8-15 (odd lane) of bin b / 16; the even lane writes the header
+    uint32_t c0 = 0, c1 = 0, ovf = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      c0 |= min(v[k], 255u) << (8 * k);
+      c1 |= min(v[k + 4], 255u) << (8 * k);
+      ovf |= (v[k] > 255u) | (v[k + 4] > 255u);
+    }
+    const uint32_t d0 = __shfl_down_sync(0xffffffffu, c0, 1), d1 = __shfl_down_sync(0xffffffffu, c1, 1);
+    const uint32_t dovf = __shfl_down_sync(0xffffffffu, ovf, 1);
+    const int64_t bin = b >> 4;
+    if (!(lane & 1) && bin < nbins) {
+      const uint32_t start = carry + wsum[warp] + (incl - sum);
+      asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(hdr + bin), "r"(c0), "r"(c1),
+                   "r"(d0), "r"(d1), "r"(start), "r"(ovf | dovf), "r"(0u), "r"(0u)
+                   : "memory");
+    }
   }
 }
 
@@ -421,24 +468,6 @@ template <>
 struct BinTile<3> {          // (hi_x, hi_y, hi_z, 0) per point
   float4 v[TILE_PTS];
 };
-
-__device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
-               "l"(gsrc)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async8(void *sdst, const void *gsrc) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
-               "l"(gsrc)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async4(void *sdst, const void *gsrc) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
-               "l"(gsrc)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Copy the footprint of the bin whose tile origin is o into `t` (points
 // outside the grid are skipped: no cell of the bin reads them).
@@ -779,7 +808,7 @@ static void launch_bin(const arb_grid *g, const KParams &kp, const BinGeom &bg, 
   bin_count_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, wb, *out, status, w);
   const int64_t nh = bg.nsub + 1, nb = scan_blocks(nh);
   scan_part_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(w.hist, nh, w.part);
-  scan_apply_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(w.hist, nh, w.part, w.offs);
+  scan_apply_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(w.hist, nh, w.part, w.offs, w.hdr, bg.nbins);
   bin_place_kernel<DIM, !MIXED, T><<<B, TB, 0, s>>>(*g, kp, bg, q, nq, qs, w);
 }
 

@@ -301,7 +301,7 @@ int arb_query_eval_binned(const arb_grid *g, int32_t precision, int32_t use_tabl
  *      return ARB_ERR_CAPACITY without touching the GPU — on a 256^3 grid
  *      (32768 bins, 16 sub-bins each in mixed precision) at most 344,048
  *      query rows per call in float64 and
- *      393,184 in mixed precision (48- and 32-byte records); split larger
+ *      360,416 in mixed precision (48- and 32-byte records); split larger
  *      query sets into several calls.  Arguments are checked first, as
  *      arb_query_eval_sorted checks them.
  *
