@@ -149,6 +149,14 @@ __host__ __device__ __forceinline__ unsigned long long ord_key_bits(unsigned lon
 }
 
 __device__ __forceinline__ void split_f32(double v, float &hi, float &lo);
+__device__ __forceinline__ void split_f32_trunc(unsigned long long b, float &hi, float &lo);
+
+// x unchanged, its origin hidden from the optimiser (no instruction): bit
+// tests on a reinterpreted double are then not turned into float64 compares.
+__device__ __forceinline__ unsigned long long opaque_u64(unsigned long long x) {
+  asm("" : "+l"(x));
+  return x;
+}
 
 struct FastAxis {
   unsigned long long lo_key, hi_key;  // ord keys of IntMin / IntMax
@@ -243,7 +251,10 @@ __device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const F
 #pragma unroll
   for (int a = 0; a < DIM; ++a) {
     const double q = qrow[a];
-    const unsigned long long qb = (unsigned long long)__double_as_longlong(q);
+    // the bits are opaque to the optimiser, so the NaN and range tests below
+    // stay integer operations instead of being folded into float64 compares
+    // (the float64 pipe issues about one warp instruction per 15 cycles per SM)
+    const unsigned long long qb = opaque_u64((unsigned long long)__double_as_longlong(q));
     const bool isnan = (qb & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL;
     const unsigned long long k = ord_key_bits(qb);
     const bool out = !isnan && (k < ax[a].lo_key || k > ax[a].hi_key);
@@ -256,14 +267,14 @@ __device__ __forceinline__ CoordStep coord_step_fast(const double *qrow, const F
     }
     if (ax[a].df) {
       // (q - IntMin) / h in float32 double-float arithmetic: q and IntMin
-      // as float pairs (residual 2^-48 relative), an exact two-sum of the
-      // high parts, times the pair of 1/h.  Error <= 2^-25 in cell units
-      // (span <= 2^20 cells); the reference's own float64 roundings move iu
-      // by <= 2^-31.  So the floor is the reference's whenever the fraction
-      // is 2^-20 or more away from a cell face; otherwise the float64 steps
-      // below decide.
+      // as float pairs (residuals 2^-47 and 2^-48 relative), an exact
+      // two-sum of the high parts, times the pair of 1/h.  Error < 2^-24 in
+      // cell units (span <= 2^20 cells); the reference's own float64
+      // roundings move iu by <= 2^-31.  So the floor is the reference's
+      // whenever the fraction is 2^-20 or more away from a cell face;
+      // otherwise the float64 steps below decide.
       float qh, ql;
-      split_f32(q, qh, ql);
+      split_f32_trunc(qb, qh, ql);
       const float sh = __fsub_rn(qh, ax[a].loh);
       const float bv = __fsub_rn(sh, qh);
       const float se = __fadd_rn(__fsub_rn(qh, __fsub_rn(sh, bv)), __fsub_rn(-ax[a].loh, bv));
@@ -481,6 +492,44 @@ __device__ __forceinline__ void cp_async4(void *sdst, const void *gsrc) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Split a double into float32 hi + lo with hi = v truncated to 24
+// significand bits and lo = RN(v - hi) (the 29 dropped bits, rounded once),
+// so |v - (hi + lo)| <= 2^-47 |v|: cheaper than split_f32 (no rounding of
+// hi) where only the sum matters.  Both forms take the bits of v; the _bits
+// form requires the biased exponent E of v in [949, 1149]
+// (2^-74 <= |v| < 2^127).
+__device__ __forceinline__ void split_f32_trunc_bits(unsigned long long b, float &hi, float &lo) {
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const int E = (int)((h32 >> 20) & 0x7ff);
+  const unsigned sign = h32 & 0x80000000u;
+  hi = __uint_as_float(sign | ((unsigned)(E - 896) << 23) | ((h32 & 0xfffffu) << 3) | (l32 >> 29));
+  // the dropped bits as a float without the conversion instruction:
+  // r = x 2^12 + y, both halves exact as magic-number floats, one rounded add
+  const unsigned r = l32 & 0x1fffffffu;
+  const float fx = __fsub_rn(__int_as_float(0x4b400000 + (int)(r >> 12)), 12582912.f);
+  const float fy = __fsub_rn(__int_as_float(0x4b400000 + (int)(r & 0xfffu)), 12582912.f);
+  const float l = __fadd_rn(__fmul_rn(fx, 4096.f), fy) * __uint_as_float((unsigned)(E - 948) << 23);
+  lo = sign ? -l : l;
+}
+
+// Other magnitudes: split_f32, out of line (never speculated on the fast path).
+static __device__ __noinline__ float2 split_f32_trunc_slow(double v) {
+  float hi, lo;
+  split_f32(v, hi, lo);
+  return make_float2(hi, lo);
+}
+
+__device__ __forceinline__ void split_f32_trunc(unsigned long long b, float &hi, float &lo) {
+  const int E = (int)((b >> 52) & 0x7ff);
+  if (E < 949 || E > 1023 + 126) {
+    const float2 r = split_f32_trunc_slow(__longlong_as_double((long long)b));
+    hi = r.x;
+    lo = r.y;
+    return;
+  }
+  split_f32_trunc_bits(b, hi, lo);
+}
 
 // Warp-aggregated append of an out-of-volume row index.
 __device__ __forceinline__ void append_oob(const arb_query_out &o, int64_t row, bool pred) {

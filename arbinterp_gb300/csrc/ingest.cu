@@ -190,17 +190,16 @@ __device__ __forceinline__ double to_f64(TF v) {
 // ||(bx, by, bz)|| for float64 components as a float32 pair hi + lo, in
 // float32 arithmetic only, and each component rounded to float32 (ch, the
 // grid's hi of that component).  The components are rescaled by the power of
-// two of the largest (exact, on the exponent bits) and split on their bits:
-// h = the top 24 significand bits (truncated), l = the remaining 29 bits
-// rounded once to float32, so h + l is the scaled component to 2^-47
-// relative.  Then double-float: error-free squares via FMA, two-sum
-// accumulation, one Newton correction of the float32 square root.  Accurate
-// to ~2^-45 relative, below the pair's own resolution.  ch is h rounded to
-// nearest-even from the dropped bits, rescaled (exact where the component
-// and its scaled value are normal float32 numbers; other components take
-// split_f32).  Scaled components below 2^-60 add nothing to the norm.
-// Returns false (caller takes the float64 norm) for a largest component
-// outside [2^-90, 2^90], zeros, infinities and NaN.
+// two of the largest (exact, on the exponent bits) and split on their bits
+// (split_f32_trunc_bits: h + l is the scaled component to 2^-47 relative).  Then
+// double-float: error-free squares via FMA, two-sum accumulation, one Newton
+// correction of the float32 square root.  Accurate to ~2^-45 relative, below
+// the pair's own resolution.  ch is h rounded to nearest-even on the dropped
+// bits, rescaled (exact where the component and its scaled value are normal
+// float32 numbers; other components take split_f32).  Scaled components
+// below 2^-74 add nothing to the norm.  Returns false (caller takes the
+// float64 norm) for a largest component outside [2^-90, 2^90], zeros,
+// infinities and NaN.
 __device__ __forceinline__ bool norm_f32pair(double bx, double by, double bz, float &hi, float &lo,
                                              float ch[3]) {
   const long long bb[3] = {__double_as_longlong(bx), __double_as_longlong(by), __double_as_longlong(bz)};
@@ -217,26 +216,18 @@ __device__ __forceinline__ bool norm_f32pair(double bx, double by, double bz, fl
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const int es = ex[a] - sc;                              // biased exponent of the scaled component
-    const unsigned hi32 = (unsigned)((unsigned long long)bb[a] >> 32);
-    const unsigned sign = hi32 & 0x80000000u;
-    const unsigned top23 = ((hi32 & 0xfffffu) << 3) | ((unsigned)bb[a] >> 29);   // significand bits 51..29
-    const unsigned rem = (unsigned)bb[a] & 0x1fffffffu;                           // bits 28..0
-    if (es >= 963) {
-      const unsigned hb = sign | ((unsigned)(es - 896) << 23) | top23;
-      h[a] = __uint_as_float(hb);
-      // rem as float without the conversion instruction: rem = x 2^12 + y,
-      // both halves exact as magic-number floats, one rounded add
-      const float fx = __fsub_rn(__int_as_float(0x4b400000 + (int)(rem >> 12)), 12582912.f);
-      const float fy = __fsub_rn(__int_as_float(0x4b400000 + (int)(rem & 0xfffu)), 12582912.f);
-      const float r = __fadd_rn(__fmul_rn(fx, 4096.f), fy) * __int_as_float((es - 1075 + 127) << 23);
-      l[a] = sign ? -r : r;
+    if (es >= 949) {
+      split_f32_trunc_bits((unsigned long long)(bb[a] - ((long long)sc << 52)), h[a], l[a]);
     } else {
       h[a] = 0.f;
       l[a] = 0.f;
     }
-    if (es >= 963 && ex[a] >= 897) {
-      const bool up = rem > 0x10000000u || (rem == 0x10000000u && (top23 & 1u));
-      ch[a] = __uint_as_float(__float_as_uint(h[a]) + (up ? 1u : 0u)) * f;
+    if (es >= 949 && ex[a] >= 897) {
+      // round h to nearest even on the dropped bits (the same bits scaled or not)
+      const unsigned rem = (unsigned)bb[a] & 0x1fffffffu;
+      const unsigned hb = __float_as_uint(h[a]);
+      const bool up = rem > 0x10000000u || (rem == 0x10000000u && (hb & 1u));
+      ch[a] = __uint_as_float(hb + (up ? 1u : 0u)) * f;
     } else {
       float t;
       split_f32(__longlong_as_double(bb[a]), ch[a], t);
