@@ -449,7 +449,7 @@ static __device__ __noinline__ float2 split_f32_slow(double v) {
 }
 
 __device__ __forceinline__ void split_f32(double v, float &hi, float &lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned long long b = opaque_u64((unsigned long long)__double_as_longlong(v));  // integer tests only
   const int E = (int)((b >> 52) & 0x7ff);
   if (E < 978 || E > 1023 + 126) {
     const float2 r = split_f32_slow(v);  // out of line: never speculated

@@ -644,10 +644,10 @@ class _Interpolant:
         n, qs = int(qa.shape[0]), int(qa.shape[1])
         if qs < dim:
             raise IndexError("query rows need at least %d columns" % dim)
-        self._settle()
         qc = np.ascontiguousarray(qa, dtype=np.float64)
         if n >= PIPELINE_MIN_ROWS:
             return self._rquery_host_pipelined(qa, qc, n, qs)
+        self._settle()
         qd = torch.from_numpy(qc).to(self.device, non_blocking=True)
         comps, norms, grads, inds, oob, cnt = self._run(qd, n, qs, False, True)
         # one copy of the interleaved rows; the outputs are column views of it
@@ -673,7 +673,10 @@ class _Interpolant:
         current stream as soon as it has arrived, and its output rows go back
         on a copy-out stream (the other direction of the link) while later
         chunks upload and evaluate.  Results, in-place NaN rows and
-        queryInds are those of the single-shot path."""
+        queryInds are those of the single-shot path.  A single-pass grid fill
+        still in flight is not waited for: the uploads start at once, the
+        evaluations queue behind the fill, and its row check is read with the
+        status at the end."""
         dev = self.device
         K = max(2, min(PIPELINE_MAX_CHUNKS, n // PIPELINE_MIN_CHUNK_ROWS))
         bounds = [n * k // K for k in range(K + 1)]
@@ -713,6 +716,12 @@ class _Interpolant:
             with torch.cuda.stream(s_out):
                 hrows[a:b].copy_(rows[a:b], non_blocking=True)
         st = self._fetch_status()                   # synchronises the current stream
+        if self._fill_pending and self._settle_status(st):
+            # the single-pass fill found a row out of meshgrid order and the
+            # general ingest rewrote the grid: evaluate again on it (nothing
+            # was written to the caller's array yet)
+            s_out.synchronize()
+            return self._rquery_host_pipelined(qa, qc, n, qs)
         c = cnts.cpu().numpy()
         if c.any():
             bad = torch.cat([oob[bounds[k]:bounds[k] + int(c[k])] + bounds[k] for k in range(K) if c[k]])

@@ -176,3 +176,34 @@ def test_mixed_device_field_float64_grid_on_first_use(mode):
     f[0, 3] += 1.0                                   # the caller changes the field in place
     with pytest.raises(RuntimeError):
         again.inputfield
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_single_pass_check_read_after_pipelined_host_query(prec):
+    """A large host query starts its uploads without waiting for the grid
+    fill and reads the fill's row check with the status at the end: rows out
+    of meshgrid order (past the probe) make it rewrite the grid and evaluate
+    again, with the outputs, in-place NaN rows and indices of an interpolant
+    built from the rows in order; a point off its axis raises ValueError."""
+    from arbinterp_gb300 import interp, tricubic
+    f = _field(3, (2, 1, 0), (), vector=True)
+    g = f.copy()
+    g[[10, 57]] = g[[57, 10]]
+    n = interp.PIPELINE_MIN_ROWS + 777
+    q = np.random.default_rng(8).uniform(f[:, :3].min(0) - 0.05, f[:, :3].max(0) + 0.05, (n, 3))
+    kw = dict(mode="both", precision=prec, strategy="otf")
+    ref = tricubic(f, "quiet", **kw)
+    o = tricubic(g, "quiet", **kw)
+    assert o._fill_pending
+    qa, qb = q.copy(), q.copy()
+    ra, rb = ref.Query(qa), o.Query(qb)
+    assert not o._fill_pending and o._ingest_path == "general" and ref.ingest_path == "ordered"
+    assert np.array_equal(np.isnan(qa), np.isnan(qb)) and np.isnan(qb).any()
+    assert np.array_equal(ref.queryInds, o.queryInds)
+    for x, y in zip(ra, rb):
+        assert np.array_equal(x, y, equal_nan=True)
+    off = f.copy()
+    off[33, 1] += 1e-3
+    o = tricubic(off, "quiet", **kw)
+    with pytest.raises(ValueError):
+        o.Query(q.copy())
