@@ -72,6 +72,17 @@ def _ptr(t):
     return None if t is None else t.data_ptr()
 
 
+def _nan_rows(qa, rows):
+    """qa[rows] = NaN for a host array qa and a CPU int64 tensor of row
+    indices: through torch's multithreaded index_fill_ on a view of qa when
+    it is a C-contiguous float array (numpy's row-wise fancy assignment is
+    about five times slower for 1e5 scattered rows), else by numpy."""
+    if qa.dtype in (np.float32, np.float64) and qa.flags.c_contiguous and qa.flags.writeable:
+        torch.from_numpy(qa).index_fill_(0, rows, float("nan"))
+    else:
+        qa[rows.numpy()] = np.nan
+
+
 def _stream():
     return torch.cuda.current_stream().cuda_stream
 
@@ -659,8 +670,7 @@ class _Interpolant:
         st = self._fetch_status()          # synchronises the stream
         nbad = int(cnt.item())
         if nbad:
-            rows = oob[:nbad].cpu().numpy()
-            qa[rows] = np.nan              # in-place on the caller's array
+            _nan_rows(qa, oob[:nbad].cpu())  # in-place on the caller's array
         self._last_inds = inds
         if st & _lib.ARB_ERR_CELL_INDEX:
             raise IndexError("cell index beyond the coefficient table (query on an upper face)")
@@ -725,7 +735,7 @@ class _Interpolant:
         c = cnts.cpu().numpy()
         if c.any():
             bad = torch.cat([oob[bounds[k]:bounds[k] + int(c[k])] + bounds[k] for k in range(K) if c[k]])
-            qa[bad.cpu().numpy()] = np.nan          # in-place on the caller's array
+            _nan_rows(qa, bad.cpu())                # in-place on the caller's array
         s_out.synchronize()                         # every stream is idle before the buffers are released
         self._last_inds = inds
         if st & _lib.ARB_ERR_CELL_INDEX:

@@ -80,3 +80,30 @@ def test_noalloc_capacity_stated_in_header():
     g.nc = 253 ** 3
     for prec, rows in zip((_lib.PREC_FP64, _lib.PREC_MIXED), stated):
         assert L.arb_query_sorted_work_bytes(g, prec, rows) <= cap < L.arb_query_sorted_work_bytes(g, prec, rows + 1)
+
+
+def test_nan_rows_write_back():
+    """The in-place NaN rows of a host query array (rQuery's write-back):
+    the threaded path for C-contiguous float arrays and the NumPy path for
+    other layouts give the same array; a read-only array raises as NumPy's
+    assignment does."""
+    import numpy as np
+    import torch
+    from arbinterp_gb300.interp import _nan_rows
+    rng = np.random.default_rng(0)
+    rows = torch.from_numpy(rng.choice(5000, 300, replace=False).astype(np.int64))
+    for dt in (np.float64, np.float32):
+        base = rng.standard_normal((5000, 4)).astype(dt)
+        want = base.copy()
+        want[rows.numpy()] = np.nan
+        a = base.copy()
+        _nan_rows(a, rows)                          # threaded path
+        b = np.asfortranarray(base.copy())
+        _nan_rows(b, rows)                          # NumPy path
+        for x in (a, b):
+            assert np.array_equal(np.isnan(x), np.isnan(want))
+            assert np.array_equal(np.nan_to_num(x), np.nan_to_num(want))
+    ro = np.zeros((10, 3))
+    ro.setflags(write=False)
+    with pytest.raises(ValueError):
+        _nan_rows(ro, torch.tensor([1, 2]))
