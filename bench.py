@@ -78,11 +78,33 @@ def parse():
 
 
 EVAL_SMALL_TRAFFIC = 246.96e6  # dram read + write of eval_binc_kernel<4> on the 160^3 case (ncu capture)
+# the same capture's shared-memory load wavefronts and warp instructions per query: the kernel's two
+# on-chip limits, turned into time bounds for the launch at one wavefront per SM per clock and at one
+# warp instruction per scheduler per clock
+EVAL_SMALL_WAVEFRONTS_PER_QUERY = 30.584051e6 / 2.02e6
+EVAL_SMALL_WARP_INSTR_PER_QUERY = 104.498808e6 / 2.02e6
 # dram read + write of eval_tab_coop_kernel<4, mixed> per query: 1.902 GB for 2.02e6 queries on the
 # 160^3 table (3.94M cells; ncu capture)
 TAB_SMALL_TRAFFIC_PER_QUERY = (1.777388e9 + 0.124713e9) / 2.02e6
 # dram read + write of parse_kernel per byte of text: 444.0 MB for the 128^3 field file (324.0 MB; ncu capture)
 CSV_PARSE_TRAFFIC_PER_BYTE = (366.16e6 + 77.83e6) / 324.01e6
+
+
+def on_chip_bounds(kt, nq, clks):
+    """Time bounds of the evaluation kernel's on-chip limits for nq queries at
+    the median SM clock sampled during the run, from the per-query counts of
+    its ncu capture, and the fraction of the measured kernel time kt (s)
+    each accounts for."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    hz = 1e6 * (clks.get("sm_mhz") or 2070.0)
+    smem = EVAL_SMALL_WAVEFRONTS_PER_QUERY * nq / (sms * hz)
+    issue = EVAL_SMALL_WARP_INSTR_PER_QUERY * nq / (sms * 4 * hz)
+    return {"shared_memory": {"per_query": EVAL_SMALL_WAVEFRONTS_PER_QUERY, "unit": "wavefronts",
+                              "bound_ms": 1000 * smem, "frac": smem / kt},
+            "issue": {"per_query": EVAL_SMALL_WARP_INSTR_PER_QUERY, "unit": "warp instructions",
+                      "bound_ms": 1000 * issue, "frac": issue / kt},
+            "source": "ncu capture of the same kernel on the 160^3 case (bench.py --profile small)"}
 
 
 def run_profile(args):
@@ -1100,6 +1122,7 @@ def main():
         # this library's kernels per step: ingest (meshgrid-order rows: probe, summary, gather,
         # tile; otherwise those four plus axes init/collect/sort, index, gather, summary) and
         # the query (binned: count, two scan passes, place, evaluate; plain: one)
+        clks = clk.summary()
         launches_per_step = ((4 if o.ingest_path == "ordered" else 10) +
                              (5 if o.last_plan.get("binned") else 1))
         line = {
@@ -1114,8 +1137,9 @@ def main():
                        "l2": "inputs larger than L2 (field 805 MB, queries 242 MB); no flush"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": kname,
-                         "kernel_ms": 1000 * kt, "algorithmic_bytes": algo, "peak_source": peak_src},
-            "clocks": clk.summary(),
+                         "kernel_ms": 1000 * kt, "algorithmic_bytes": algo, "peak_source": peak_src,
+                         "on_chip": on_chip_bounds(kt, nq, clks) if (prec == "mixed" and not use_tab) else None},
+            "clocks": clks,
             "gpu_launches": launches_per_step * args.steps,
             "e2e": e2e, "cpu_baseline": cpu,
         }
