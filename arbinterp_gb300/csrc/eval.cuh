@@ -664,9 +664,13 @@ __device__ __forceinline__ void eval_otf4_mixed_block(const BLK &blk, const KPar
 #pragma unroll
     for (int m = 0; m < 16; ++m) S[m] = 0;
     float hl = 0.f, ll = 0.f;  // point (1, 1, 1, l): reference of the z-deltas of slab l
-#pragma unroll
+    // the slab loop stays rolled: unrolled, the 256-point body overflowed the
+    // instruction cache (instruction fetch was the bin kernel's first stall)
+#pragma unroll 1
     for (int li = 0; li < 4; ++li) {
       const int l = li == 0 ? 1 : (li == 1 ? 0 : li);
+      const T w3 = l == 0 ? w[3][0] : (l == 1 ? w[3][1] : (l == 2 ? w[3][2] : w[3][3]));
+      const T dw3 = l == 0 ? dw[3][0] : (l == 1 ? dw[3][1] : (l == 2 ? dw[3][2] : dw[3][3]));
       T Az = 0, Azg[3] = {0, 0, 0};
       T E2[8];
 #pragma unroll
@@ -719,16 +723,21 @@ __device__ __forceinline__ void eval_otf4_mixed_block(const BLK &blk, const KPar
         for (int m = 0; m < 4; ++m) E2[m + 4 * (k & 1)] += sk * E1[m];
       }
       const T Al = Az + ((hl - rhi) + (ll - rlo));  // slab reference against the corner
-      V += w[3][l] * Al;
+      V += w3 * Al;
       if (gradf) {
-        Vg[0] += w[3][l] * Azg[0];
-        Vg[1] += w[3][l] * Azg[1];
-        Vg[2] += w[3][l] * Azg[2];
-        Vg[3] += dw[3][l] * Al;
+        Vg[0] += w3 * Azg[0];
+        Vg[1] += w3 * Azg[1];
+        Vg[2] += w3 * Azg[2];
+        Vg[3] += dw3 * Al;
       }
       const T sl = (l >= 2) ? T(0.5) : T(-0.5);
+      if (l & 1) {
 #pragma unroll
-      for (int m = 0; m < 8; ++m) S[m + 8 * (l & 1)] += sl * E2[m];
+        for (int m = 0; m < 8; ++m) S[m + 8] += sl * E2[m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < 8; ++m) S[m] += sl * E2[m];
+      }
     }
     // T_c = S_{c-1} - S_c, contracted with the slope-Hermite tensor
     T Tc[16];
