@@ -52,19 +52,35 @@ __global__ void __launch_bounds__(128) rk4_kernel(arb_grid g, KParams kp, double
   for (int a = 0; a < 3; ++a) alive &= (x[a] == x[a]) && (v[a] == v[a]);
   int64_t rec = 0;
   for (int64_t s = 0; s < nsteps && alive; ++s) {
-    double k1v[3], k2v[3], k3v[3], k4v[3], xs[3];
-    alive = rk4_accel<F, MIXED>(g, kp, x, coef, grav, k1v);
-    if (alive) {
-      for (int a = 0; a < 3; ++a) xs[a] = x[a] + h2 * v[a];
-      alive = rk4_accel<F, MIXED>(g, kp, xs, coef, grav, k2v);
-    }
-    if (alive) {
-      for (int a = 0; a < 3; ++a) xs[a] = x[a] + h2 * (v[a] + h2 * k1v[a]);
-      alive = rk4_accel<F, MIXED>(g, kp, xs, coef, grav, k3v);
-    }
-    if (alive) {
-      for (int a = 0; a < 3; ++a) xs[a] = x[a] + dt * (v[a] + h2 * k2v[a]);
-      alive = rk4_accel<F, MIXED>(g, kp, xs, coef, grav, k4v);
+    double k1v[3], k2v[3], k3v[3], k4v[3];
+    // the four stages share one copy of the field evaluation (a rolled loop:
+    // four inlined copies made instruction fetch the kernel's first stall)
+#pragma unroll 1
+    for (int stg = 0; stg < 4 && alive; ++stg) {
+      double xs[3], k[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        if (stg == 0)
+          xs[a] = x[a];
+        else if (stg == 1)
+          xs[a] = x[a] + h2 * v[a];
+        else if (stg == 2)
+          xs[a] = x[a] + h2 * (v[a] + h2 * k1v[a]);
+        else
+          xs[a] = x[a] + dt * (v[a] + h2 * k2v[a]);
+      }
+      alive = rk4_accel<F, MIXED>(g, kp, xs, coef, grav, k);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        if (stg == 0)
+          k1v[a] = k[a];
+        else if (stg == 1)
+          k2v[a] = k[a];
+        else if (stg == 2)
+          k3v[a] = k[a];
+        else
+          k4v[a] = k[a];
+      }
     }
     if (!alive) break;
     // position stages are v + dt/2 k1v, v + dt/2 k2v, v + dt k3v
