@@ -16,21 +16,65 @@
 
 namespace arb {
 
+// Axis a of the kernel parameters of grid g (make_kparams, on the device).
+__device__ void make_kparams_axis(const arb_grid &g, int a, KParams &kp) {
+  const double h = a < g.dim ? g.h[a] : 1.0;
+  const double lo = a < g.dim ? g.lo[a] : 0.0, hi = a < g.dim ? g.hi[a] : 0.0;
+  kp.inv_h[a] = 1.0 / h;
+  kp.inv_hf[a] = (float)(1.0 / h);
+  kp.ax[a].lo_key = ord_key_bits((unsigned long long)__double_as_longlong(lo));
+  kp.ax[a].hi_key = ord_key_bits((unsigned long long)__double_as_longlong(hi));
+  kp.ax[a].lo = lo;
+  kp.ax[a].h = h;
+  kp.ax[a].inv_h = 1.0 / h;
+  fast_axis_pairs(kp.ax[a], lo, hi, h);
+}
+
 __device__ KParams make_kparams_dev(const arb_grid &g) {
   KParams kp;
-  for (int a = 0; a < 4; ++a) {
-    const double h = a < g.dim ? g.h[a] : 1.0;
-    const double lo = a < g.dim ? g.lo[a] : 0.0, hi = a < g.dim ? g.hi[a] : 0.0;
-    kp.inv_h[a] = 1.0 / h;
-    kp.inv_hf[a] = (float)(1.0 / h);
-    kp.ax[a].lo_key = ord_key_bits((unsigned long long)__double_as_longlong(lo));
-    kp.ax[a].hi_key = ord_key_bits((unsigned long long)__double_as_longlong(hi));
-    kp.ax[a].lo = lo;
-    kp.ax[a].h = h;
-    kp.ax[a].inv_h = 1.0 / h;
-    fast_axis_pairs(kp.ax[a], lo, hi, h);
-  }
+  for (int a = 0; a < 4; ++a) make_kparams_axis(g, a, kp);
   return kp;
+}
+
+// One warp takes the next tile from the counter and fills descriptor slot
+// `slot` (tile, field, grid, kernel parameters): a 32-ary search of the
+// fields' first tiles (one load per lane and step), the grid copied by the
+// lanes, the parameters of axis a by lane a.
+static_assert(sizeof(arb_grid) % 8 == 0, "grid descriptor copied in 8-byte words");
+struct TileSlot {
+  arb_grid g;
+  KParams kp;
+  int64_t tile;
+  int32_t field;
+};
+
+__device__ __forceinline__ void acquire_tile(const arb_grid *grids, int32_t nfields, const int64_t *tile_off,
+                                             int64_t ntiles, unsigned long long *counter, TileSlot &ts) {
+  const int lane = threadIdx.x & 31;
+  unsigned long long t = 0;
+  if (lane == 0) t = atomicAdd(counter, 1ULL);
+  const int64_t tile = (int64_t)__shfl_sync(0xffffffffu, t, 0);
+  if (tile < ntiles) {
+    // last field f with tile_off[f] <= tile (tile_off[0] = 0)
+    int32_t lo = 0, hi = nfields - 1;
+    while (lo < hi) {
+      const int32_t step = (hi - lo + 32) / 32;  // ceil((hi - lo + 1) / 32)
+      const int32_t piv = lo + lane * step;
+      const bool ok = piv <= hi && tile_off[piv] <= tile;
+      const unsigned m = __ballot_sync(0xffffffffu, ok);  // lane 0 always holds
+      const int last = 31 - __clz(m);
+      const int32_t nlo = lo + last * step;
+      hi = min(hi, nlo + step - 1);
+      lo = nlo;
+    }
+    const arb_grid &src = grids[lo];
+    const uint64_t *w = reinterpret_cast<const uint64_t *>(&src);
+    uint64_t *d = reinterpret_cast<uint64_t *>(&ts.g);
+    for (int k = lane; k < (int)(sizeof(arb_grid) / 8); k += 32) d[k] = w[k];
+    if (lane < 4) make_kparams_axis(src, lane, ts.kp);
+    if (lane == 0) ts.field = lo;
+  }
+  if (lane == 0) ts.tile = tile;
 }
 
 template <int F, bool MIXED>
@@ -56,51 +100,38 @@ __device__ __forceinline__ void batched_rows(const arb_grid &g, const KParams &k
 // FF: the fields' common count (1, 3, 4), compiled alone (no registers or
 // spills for the other counts' paths); 0 dispatches on each descriptor's
 // count.  Mixed precision: two CTAs per SM (the register file caps the
-// on-the-fly evaluator at 16 warps per SM).
+// on-the-fly evaluator at 16 warps per SM).  Tiles come from an atomic
+// counter; warp 0 takes the next tile and fills its descriptor slot while
+// the CTA evaluates the current one (two slots), so the dependent loads of
+// the take (counter, field search, descriptor) do not hold the CTA at the
+// barrier between tiles.
 template <bool MIXED, int FF>
 __global__ void __launch_bounds__(256, MIXED ? 2 : 1) batched_kernel(const arb_grid *grids, int32_t nfields,
                                                       const int64_t *q_off, const int64_t *tile_off,
                                                       int64_t ntiles, int32_t tile_rows, double *q,
                                                       int64_t qs, int wb, arb_query_out o,
                                                       unsigned long long *counter, int32_t *status) {
-  __shared__ arb_grid sg;
-  __shared__ KParams skp;
-  __shared__ int64_t stile;
-  __shared__ int32_t sfield;
-  for (;;) {
-    if (threadIdx.x == 0) {
-      const int64_t tile = (int64_t)atomicAdd(counter, 1ULL);
-      stile = tile;
-      if (tile < ntiles) {
-        int32_t lo = 0, hi = nfields - 1;  // last field with tile_off[f] <= tile
-        while (lo < hi) {
-          const int32_t mid = (lo + hi + 1) >> 1;
-          if (tile_off[mid] <= tile)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-        sfield = lo;
-        sg = grids[lo];
-        skp = make_kparams_dev(sg);
-      }
-    }
-    __syncthreads();
-    const int64_t tile = stile;
+  __shared__ TileSlot slots[2];
+  if (threadIdx.x < 32) acquire_tile(grids, nfields, tile_off, ntiles, counter, slots[0]);
+  __syncthreads();
+  for (int cur = 0;; cur ^= 1) {
+    const TileSlot &ts = slots[cur];
+    const int64_t tile = ts.tile;
     if (tile >= ntiles) break;
-    const int32_t f = sfield;
+    if (threadIdx.x < 32) acquire_tile(grids, nfields, tile_off, ntiles, counter, slots[cur ^ 1]);
+    const int32_t f = ts.field;
     const int64_t q0 = q_off[f] + (tile - tile_off[f]) * tile_rows;
     const int64_t q1 = min(q0 + (int64_t)tile_rows, q_off[f + 1]);
     if constexpr (FF != 0) {
-      batched_rows<FF, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status);
+      batched_rows<FF, MIXED>(ts.g, ts.kp, q, q0, q1, qs, wb, o, status);
     } else {
-      switch (sg.nfield) {
-        case 1: batched_rows<1, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
-        case 3: batched_rows<3, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
-        default: batched_rows<4, MIXED>(sg, skp, q, q0, q1, qs, wb, o, status); break;
+      switch (ts.g.nfield) {
+        case 1: batched_rows<1, MIXED>(ts.g, ts.kp, q, q0, q1, qs, wb, o, status); break;
+        case 3: batched_rows<3, MIXED>(ts.g, ts.kp, q, q0, q1, qs, wb, o, status); break;
+        default: batched_rows<4, MIXED>(ts.g, ts.kp, q, q0, q1, qs, wb, o, status); break;
       }
     }
-    __syncthreads();  // the descriptor in shared memory is replaced next round
+    __syncthreads();  // this slot is refilled two tiles later; the other one is complete
   }
 }
 
