@@ -23,13 +23,9 @@ from __future__ import annotations
 import torch
 
 from . import _lib
-from .interp import tricubic
+from .interp import _stream, tricubic
 
 __all__ = ["TricubicField", "TricubicFunction"]
-
-
-def _stream():
-    return torch.cuda.current_stream().cuda_stream
 
 
 class TricubicFunction(torch.autograd.Function):

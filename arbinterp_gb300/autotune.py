@@ -136,5 +136,6 @@ def _measure(interp, qd, nq, qs):
     if not best["table"] and not had_table and interp._table is not None:
         interp._drop_table()                                    # tuning built it; not chosen
     lib = _lib.lib()
-    lib.arb_status_fetch(interp._status.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    from .interp import _stream
+    lib.arb_status_fetch(interp._status.data_ptr(), _stream())
     return best

@@ -25,7 +25,7 @@ import torch
 
 from . import _lib, autotune
 from ._lib import ArbGrid, ArbQueryOut, lib, check
-from .interp import tricubic
+from .interp import _stream, tricubic
 
 __all__ = ["BatchedTricubic"]
 
@@ -33,8 +33,6 @@ TILE_CHOICES = (256, 512, 1024, 2048)
 TABLE_RATIOS = (None, 64.0, 8.0, 1.0)      # table when rows >= ratio * cells; None: never
 
 
-def _stream():
-    return torch.cuda.current_stream().cuda_stream
 
 
 class BatchedTricubic:

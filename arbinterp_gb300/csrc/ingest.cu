@@ -374,6 +374,8 @@ __global__ void __launch_bounds__(256) ordered_probe_kernel(const TF *field, int
                                                             OrderWork *w, int32_t *status) {
   __shared__ long long first_stop;
   const int tid = threadIdx.x;
+  if (tid == 0)  // axes the probe does not find keep a count of 0 (the caller need not clear them)
+    for (int a = 0; a < dim; ++a) axis_count[a] = 0;
   double r0[4];
   for (int a = 0; a < dim; ++a) r0[a] = (double)field[a];
   int64_t stride = 1;

@@ -149,7 +149,8 @@ int arb_ingest_ordered(const void *field, int32_t field_is_f32, int64_t npts, in
 /* arb_ingest_ordered in two launches on the same stream, so that the host
  * can read the axes (arb_ingest_summary after the probe) while the grid is
  * still being written: _probe reads the axes off the lines through row 0
- * (ARB_ERR_IRREGULAR_GRID in *status if those lines are not a meshgrid);
+ * (ARB_ERR_IRREGULAR_GRID in *status if those lines are not a meshgrid) and
+ * writes all dim axis counts (0 for an axis it did not find);
  * _fill writes every grid slot and checks every row, with the same axes and
  * work (ARB_ERR_IRREGULAR_GRID for rows in another order; it does nothing
  * after a failed probe).  The same reference code (ARB:528-568, 1264-1320). */
