@@ -229,13 +229,18 @@ class _Interpolant:
         lazy64 = (self.precision == "mixed" and isinstance(field, torch.Tensor)
                   and ft.data_ptr() == field.data_ptr())
         self._src = (ft, ft._version, is32, ncol) if lazy64 else None
-        grid64 = None if lazy64 else torch.empty(npts * F, dtype=torch.float64, device=dev)
-        # mixed-precision grid: F=1 (hi, lo); F=3 float4 of hi; F=4 float4 of hi + lo of |B|
-        g32_floats = {1: 2, 3: 4, 4: 5}[F]
-        grid32 = (torch.empty(npts * g32_floats, dtype=torch.float32, device=dev)
-                  if self.precision == "mixed" else None)
-        raw = (torch.empty(npts * 3, dtype=torch.float64, device=dev)
-               if kind == _lib.KIND_NORM and not lazy64 else None)
+
+        def grids():
+            # allocated once the probe is queued (the GPU starts on it meanwhile)
+            g64 = None if lazy64 else torch.empty(npts * F, dtype=torch.float64, device=dev)
+            # mixed-precision grid: F=1 (hi, lo); F=3 float4 of hi; F=4 float4 of hi + lo of |B|
+            g32 = (torch.empty(npts * {1: 2, 3: 4, 4: 5}[F], dtype=torch.float32, device=dev)
+                   if self.precision == "mixed" else None)
+            r = (torch.empty(npts * 3, dtype=torch.float64, device=dev)
+                 if kind == _lib.KIND_NORM and not lazy64 else None)
+            return g64, g32, r
+
+        grid64 = grid32 = raw = None
         ax64 = axes[: dim * cap].view(dim, cap)
         summ = torch.empty(17, dtype=torch.float64, device=dev)
 
@@ -259,6 +264,7 @@ class _Interpolant:
             summ_h.copy_(summ, non_blocking=True)
             ev = torch.cuda.Event()
             ev.record()
+            grid64, grid32, raw = grids()
             check(L.arb_ingest_ordered_fill(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
                                             work.data_ptr(), wb, _ptr(grid64), _ptr(grid32), _ptr(raw),
                                             status.data_ptr(), s), "arb_ingest_ordered_fill")
@@ -269,6 +275,8 @@ class _Interpolant:
                 self._fill_pending = True
                 self._fill_src = (ft, is32, npts, ncol, cap, axes, counts, work, wb, grid64, grid32, raw)
         if not done:
+            if grid32 is None and grid64 is None:
+                grid64, grid32, raw = grids()
             sm = self._ingest_general(ft, is32, npts, ncol, cap, axes, counts, work, wb, grid64, grid32, raw)
         n = [int(sm[1 + a]) for a in range(dim)]
         self._axes_dev = [ax64[a, : n[a]] for a in range(dim)]
