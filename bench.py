@@ -698,8 +698,8 @@ def cuda_time(fn, steps, warmup, barrier=None):
 # ---------------------------------------------------------------- CPU baseline
 # The reference's own code (oracle/_ref: its module byte-compiled by
 # oracle/ref_build.py; the oracle port where that file is absent) runs the
-# job on the host cores as N worker processes that split the query set, the
-# way SURVEY's CPU plan describes: every worker constructs its own
+# job on the host cores as N worker processes that split the query set:
+# every worker constructs its own
 # interpolant from the whole 256^3 field (the reference's getFieldParams,
 # unchanged), then evaluates, with `Query`, the queries of its share of the
 # cells.  Shares are contiguous ranges of the flat cell index (z-slabs), so a
