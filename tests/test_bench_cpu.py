@@ -1,8 +1,8 @@
-"""CPU checks of bench.py's contract with the driver: the reference arm (the
+"""CPU checks of bench.py's output contract: the reference arm (the
 reference's own module, or the oracle port where that is not built, timed on
-host cores) prints one JSON line with the keys the driver reads, on the same
-metric as the GPU arm, and a rank other than 0 of a multi-process launch
-exits 0 without work."""
+host cores) prints one JSON line with the keys a benchmark harness reads, on
+the same metric as the GPU arm, and a rank other than 0 of a multi-process
+launch exits 0 without work."""
 import json
 import os
 import subprocess
