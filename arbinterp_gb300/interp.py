@@ -29,6 +29,7 @@ from __future__ import annotations
 
 import ctypes
 import sys
+import threading
 
 import numpy as np
 import torch
@@ -49,6 +50,21 @@ PIPELINE_MIN_ROWS = 1 << 21
 PIPELINE_MIN_CHUNK_ROWS = 1 << 20
 PIPELINE_MAX_CHUNKS = 8
 _COPY_STREAMS: dict = {}
+_PER_THREAD = threading.local()
+
+
+def _probe_summary_slot(device):
+    """(pinned host buffer of the 17-double ingest summary, event) for this
+    thread and device, made once: the summary kernel writes the buffer in
+    place (pinned host memory is addressable from the device), so
+    construction needs no device buffer and no copy, and waits on the event."""
+    key = torch.device(device).index
+    slots = getattr(_PER_THREAD, "summary", None)
+    if slots is None:
+        slots = _PER_THREAD.summary = {}
+    if key not in slots:
+        slots[key] = (torch.empty(17, dtype=torch.float64, pin_memory=True), torch.cuda.Event())
+    return slots[key]
 
 
 def _copy_streams(device):
@@ -242,8 +258,6 @@ class _Interpolant:
 
         grid64 = grid32 = raw = None
         ax64 = axes[: dim * cap].view(dim, cap)
-        summ = torch.empty(17, dtype=torch.float64, device=dev)
-
         self._status = status
         self._fill_pending = False
         self._fill_src = None
@@ -258,11 +272,9 @@ class _Interpolant:
             check(L.arb_ingest_ordered_probe(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
                                              counts.data_ptr(), work.data_ptr(), wb, status.data_ptr(), s),
                   "arb_ingest_ordered_probe")
+            summ_h, ev = _probe_summary_slot(dev)
             check(L.arb_ingest_summary(axes.data_ptr(), cap, counts.data_ptr(), dim, status.data_ptr(),
-                                       summ.data_ptr(), s), "arb_ingest_summary")
-            summ_h = torch.empty(17, dtype=torch.float64, pin_memory=True)
-            summ_h.copy_(summ, non_blocking=True)
-            ev = torch.cuda.Event()
+                                       summ_h.data_ptr(), s), "arb_ingest_summary")
             ev.record()
             grid64, grid32, raw = grids()
             check(L.arb_ingest_ordered_fill(ft.data_ptr(), is32, npts, ncol, dim, kind, cap, axes.data_ptr(),
