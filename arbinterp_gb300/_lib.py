@@ -90,6 +90,7 @@ SIGNATURES = {
     "arb_csv_split": (C.c_int, [_P, _I64, _I64, _I32, _I32, _I64, _P, _P, C.c_size_t, _P, _P, _P]),
     "arb_csv_parse": (C.c_int, [_P, _I64, _I64, _I32, _I32, _P, C.c_size_t, _P, _P, _I64, _I64, _P, _P]),
     "arb_status_fetch": (C.c_int, [_P, _P]),
+    "arb_status_clear": (C.c_int, [_P, _P]),
     "arb_test_set_mma_wait_limit": (C.c_int, [_I64]),
     "arb_version": (C.c_char_p, []),
 }

@@ -887,4 +887,9 @@ extern "C" int arb_status_fetch(int32_t *status, arb_stream_t stream) {
   return h;
 }
 
+extern "C" int arb_status_clear(int32_t *status, arb_stream_t stream) {
+  if (!status) return ARB_ERR_INVALID;
+  return cudaMemsetAsync(status, 0, sizeof(int32_t), (cudaStream_t)stream) == cudaSuccess ? ARB_OK : ARB_ERR_CUDA;
+}
+
 extern "C" const char *arb_version(void) { return "arbinterp-gb300 0.1.0 sm_103a"; }

@@ -236,8 +236,9 @@ class _Interpolant:
         counts = torch.empty(dim, dtype=torch.int64, device=dev)   # written by the probe or the axis pass
         wb = L.arb_ingest_axes_work_bytes(dim)
         work = torch.empty(int(wb), dtype=torch.uint8, device=dev)
-        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        status = torch.empty(1, dtype=torch.int32, device=dev)
         s = _stream()
+        check(L.arb_status_clear(status.data_ptr(), s), "arb_status_clear")
         kind, F = self._kind, self._F
         # Mixed precision with the caller's own CUDA tensor: the float64 grid is
         # not needed by the float32 query path and is produced on first use from
@@ -257,7 +258,6 @@ class _Interpolant:
             return g64, g32, r
 
         grid64 = grid32 = raw = None
-        ax64 = axes[: dim * cap].view(dim, cap)
         self._status = status
         self._fill_pending = False
         self._fill_src = None
@@ -291,6 +291,7 @@ class _Interpolant:
                 grid64, grid32, raw = grids()
             sm = self._ingest_general(ft, is32, npts, ncol, cap, axes, counts, work, wb, grid64, grid32, raw)
         n = [int(sm[1 + a]) for a in range(dim)]
+        ax64 = axes[: dim * cap].view(dim, cap)
         self._axes_dev = [ax64[a, : n[a]] for a in range(dim)]
         self._n = n
         self._npts = npts

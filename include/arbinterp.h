@@ -391,6 +391,10 @@ int arb_test_set_mma_wait_limit(int64_t limit);
  * done; returns ARB_OK, an arb_status bit set, or ARB_ERR_CUDA. */
 int arb_status_fetch(int32_t *status, arb_stream_t stream);
 
+/* Clears a device status word on the stream (one memset; for a new word,
+ * without waiting). */
+int arb_status_clear(int32_t *status, arb_stream_t stream);
+
 /* Library version string ("arbinterp-gb300 <ver> sm_103a"). */
 const char *arb_version(void);
 
