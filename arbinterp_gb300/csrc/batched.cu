@@ -30,12 +30,6 @@ __device__ void make_kparams_axis(const arb_grid &g, int a, KParams &kp) {
   fast_axis_pairs(kp.ax[a], lo, hi, h);
 }
 
-__device__ KParams make_kparams_dev(const arb_grid &g) {
-  KParams kp;
-  for (int a = 0; a < 4; ++a) make_kparams_axis(g, a, kp);
-  return kp;
-}
-
 // One warp takes the next tile from the counter and fills descriptor slot
 // `slot` (tile, field, grid, kernel parameters): a 32-ary search of the
 // fields' first tiles (one load per lane and step), the grid copied by the
